@@ -1,0 +1,179 @@
+/*
+ * sayram_gpu.h -- C-ABI of the GB300 (sm_103a) implementation of Sayram-2D's per-time-step hot
+ * path: the PPFV (Gao-Wu) assembly of nonlinear two-point-flux coefficients with cross
+ * diffusion, the loss term folded into the matrix, and the implicit linear solve.
+ *
+ * Plain C types only (no CUDA or torch types), so any FFI (ctypes, cgo, JNI, a C++ wrapper) can
+ * bind it.  Every function returns a status code (SAYRAM_OK = 0) and never throws; the message
+ * of the last failure on the calling thread is available from sayram_last_error().
+ *
+ * Reference interface each group replaces (Sayram-2D, paths relative to its repository):
+ *   sayram_create / sayram_update / sayram_t / sayram_get_f / sayram_destroy
+ *       -> class Solver (source/Solver.h:18-26): Solver(const Mesh&, Equation*) [Solver.cc:14-34],
+ *          void update() [Solver.cc:270-290], double t() const [Solver.h:23],
+ *          const Xtensor2d& f() const [Solver.h:24].
+ *   sayram_problem
+ *       -> what Solver reads from Mesh (source/Mesh.h:38-63: edges, dt) and from Equation
+ *          (source/Equation.h:44-65: G, Dxx, Dxy, Dyy, inv_tau, init_f, bc_type,
+ *          dirichlet_vertex_value), evaluated into arrays.
+ *   sayram_set_dirichlet / sayram_set_coeffs
+ *       -> the per-step re-reads after eq.update(t) (Solver.cc:286-289: update_Lambda and
+ *          fill_vertex_from_bcs), for cases whose coefficients or boundary values change.
+ *   sayram_batch_*   -> no counterpart (many independent Solver instances advanced together).
+ *   sayram_server_*  -> no counterpart (continuous-batching service of solve requests).
+ *
+ * Array layouts follow the reference: per-cell fields are (nx, ny) alpha-major, element (i, j)
+ * at i*ny + j (xtensor row-major, as Equation::G_ etc.).  Dirichlet vertex values of sides
+ * XMIN/XMAX are indexed by j = 0..ny, of YMIN/YMAX by i = 0..nx (Solver.cc:398-419).
+ */
+#ifndef SAYRAM_GPU_H
+#define SAYRAM_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------------------- */
+#define SAYRAM_OK 0
+#define SAYRAM_ERR_ARG 1           /* invalid argument (bad grid, missing Dirichlet values, ...) */
+#define SAYRAM_ERR_OOM 2           /* device or host allocation failed */
+#define SAYRAM_ERR_NOT_CONVERGED 3 /* a step ended above the residual target (state still advanced) */
+#define SAYRAM_ERR_NEGATIVE 4      /* a negative cell survived the positivity polish */
+#define SAYRAM_ERR_TIMEOUT 5       /* a bounded device wait ran out */
+#define SAYRAM_ERR_CUDA 6          /* CUDA runtime error (no device, launch failure, ...) */
+#define SAYRAM_ERR_BUDGET 7        /* request does not fit the serving HBM budget */
+#define SAYRAM_ERR_STATE 8         /* call not valid in the object's current state */
+
+/* ---- boundary ids and types (source/BCTypes.h:13-16) ------------------------------------ */
+#define SAYRAM_XMIN 0
+#define SAYRAM_XMAX 1
+#define SAYRAM_YMIN 2
+#define SAYRAM_YMAX 3
+#define SAYRAM_DIRICHLET 0
+#define SAYRAM_ZEROFLUX 1
+
+/* ---- precision modes --------------------------------------------------------------------- */
+#define SAYRAM_FP64 0        /* FP64 everywhere (the plain drop-in) */
+#define SAYRAM_FP32_REFINE 1 /* FP32 matrix/Krylov, FP64 residual + refinement + checks */
+
+/* One instance: grid, time step, coefficients, initial state and boundary conditions. All
+ * arrays are read during the call that receives the struct and are not retained. */
+typedef struct sayram_problem {
+  int nx, ny;               /* cells in alpha0 (x) and log E (y) */
+  const double* x_edges;    /* nx+1, strictly increasing (Grid2D.h:44-67) */
+  const double* y_edges;    /* ny+1, strictly increasing */
+  double dt;                /* time step (Mesh::dt, Mesh.h:55) */
+  int bc[4];                /* SAYRAM_DIRICHLET or SAYRAM_ZEROFLUX for XMIN, XMAX, YMIN, YMAX */
+  const double* G;          /* (nx, ny) alpha-major: Jacobian factor */
+  const double* Dxx;        /* diffusion tensor components */
+  const double* Dxy;
+  const double* Dyy;
+  const double* inv_tau;    /* loss rate 1/tau (0 = no loss) */
+  const double* f0;         /* initial state (Equation::init_f at cell centres) */
+  const double* dirichlet[4]; /* vertex values per side; NULL for zero-flux sides */
+} sayram_problem;
+
+typedef struct sayram_options {
+  int precision;    /* SAYRAM_FP64 (default) or SAYRAM_FP32_REFINE */
+  double tol;       /* target ||R - M f|| / ||R|| in the Jacobi-scaled system (FP64 residual);
+                       default 1e-12 (FP64) / 1e-10 (FP32_REFINE) */
+  double inner_tol; /* residual reduction asked of each inner Krylov solve; default 0 (FP64:
+                       solve to tol at once) / 1e-4 (FP32_REFINE) */
+  int max_iters;    /* inner BiCGSTAB iterations per solve; default 500 */
+  int max_refine;   /* FP64 residual evaluations (outer refinements) per step; default 6 */
+  int device;       /* CUDA device ordinal; default 0 */
+  int use_graph;    /* 1 (default): each step runs as one CUDA graph with device-side loops */
+} sayram_options;
+
+typedef struct sayram_stats {
+  long long steps;        /* steps taken since creation */
+  double t;               /* simulated time = steps * dt (Solver::t, Solver.h:23) */
+  int status;             /* status of the last step: SAYRAM_OK / NOT_CONVERGED / NEGATIVE */
+  int refinements;        /* FP64 residual evaluations in the last step */
+  int iterations;         /* inner Krylov iterations in the last step */
+  double rel_residual;    /* final FP64 ||R - M f||/||R|| of the last step (scaled system) */
+  double min_f;           /* minimum cell value after the positivity polish */
+  long long clamped;      /* cells the polish lifted from a negative Krylov value */
+  double mass_drift;      /* |1^T M f - 1^T R| / 1^T R after the last step */
+} sayram_stats;
+
+/* ---- library -------------------------------------------------------------------------- */
+const char* sayram_last_error(void); /* message of the last failure on this thread ("" if none) */
+const char* sayram_version(void);
+void sayram_default_options(sayram_options* opt);
+/* Pinned host memory for fast host<->device copies (cudaMallocHost); NULL on failure. */
+void* sayram_host_alloc(size_t bytes);
+void sayram_host_free(void* p);
+
+/* ---- single instance: the drop-in for class Solver -------------------------------------- */
+typedef struct sayram_batch_s* sayram_solver;
+
+/* Solver::Solver(const Mesh&, Equation*): copies the problem to the device. */
+int sayram_create(const sayram_problem* p, const sayram_options* opt, sayram_solver* out);
+/* Solver::update(): one backward-Euler step (assembly from the current f, solve, polish). */
+int sayram_update(sayram_solver s);
+/* nsteps calls of update() without returning to the host in between. */
+int sayram_step(sayram_solver s, int nsteps);
+/* Solver::t() */
+double sayram_t(sayram_solver s);
+/* Solver::f(): copies f (alpha-major, nx*ny doubles) to the host. */
+int sayram_get_f(sayram_solver s, double* f_out);
+/* Replaces f (alpha-major). */
+int sayram_set_f(sayram_solver s, const double* f);
+/* New Dirichlet vertex values for one side (n = ny+1 for XMIN/XMAX, nx+1 for YMIN/YMAX). */
+int sayram_set_dirichlet(sayram_solver s, int side, const double* v, int n);
+/* New G, D and 1/tau fields (alpha-major); all five are required. */
+int sayram_set_coeffs(sayram_solver s, const double* G, const double* Dxx, const double* Dxy,
+                      const double* Dyy, const double* inv_tau);
+int sayram_get_stats(sayram_solver s, sayram_stats* out);
+void sayram_destroy(sayram_solver s);
+
+/* ---- batches: many independent instances advanced by the same launches ------------------- */
+typedef struct sayram_batch_s* sayram_batch;
+
+int sayram_batch_create(const sayram_problem* probs, int n, const sayram_options* opt,
+                        sayram_batch* out);
+int sayram_batch_size(sayram_batch b);
+/* Advances every instance by nsteps. Returns NOT_CONVERGED / NEGATIVE if any instance's last
+ * step did (per-instance detail in sayram_batch_stats). */
+int sayram_batch_step(sayram_batch b, int nsteps);
+/* The end-to-end form: if f_in is not NULL it first replaces every instance's f from the packed
+ * host array (instances concatenated, each alpha-major), then steps, then, if f_out is not
+ * NULL, writes every instance's f back the same way. Pinned buffers (sayram_host_alloc) copy
+ * fastest. */
+int sayram_batch_step_host(sayram_batch b, int nsteps, const double* f_in, double* f_out);
+int sayram_batch_get_f(sayram_batch b, int idx, double* f_out);
+int sayram_batch_set_f(sayram_batch b, int idx, const double* f);
+int sayram_batch_set_dirichlet(sayram_batch b, int idx, int side, const double* v, int n);
+int sayram_batch_set_coeffs(sayram_batch b, int idx, const double* G, const double* Dxx,
+                            const double* Dxy, const double* Dyy, const double* inv_tau);
+int sayram_batch_stats(sayram_batch b, int idx, sayram_stats* out);
+/* Assembles instance idx's linear system from its current f (without stepping) and returns it
+ * in the reference's unscaled form M f = R (the M_ and R_ members of Solver, Solver.h:37-41),
+ * system order K = j*nx + i: M5 holds five diagonals of nx*ny each -- M(K,K), M(K,K-1),
+ * M(K,K+1), M(K,K-nx), M(K,K+nx) (0 where the neighbour does not exist) -- and R nx*ny. */
+int sayram_batch_export_system(sayram_batch b, int idx, double* M5, double* R);
+/* Total device bytes held by the batch. */
+size_t sayram_batch_device_bytes(sayram_batch b);
+/* The CUDA stream the batch launches on (a cudaStream_t, as void*), for event timing. */
+void* sayram_batch_stream(sayram_batch b);
+/* Per-kernel timing: when enabled, every launch is bracketed by CUDA events on the batch's
+ * stream (steps then run without graphs). sayram_batch_kernel_times fills up to cap entries of
+ * names/total milliseconds/launch counts and returns the number of kernels. */
+int sayram_batch_enable_timing(sayram_batch b, int enable);
+int sayram_batch_kernel_times(sayram_batch b, const char** names, double* total_ms,
+                              long long* launches, int cap);
+/* Kernel launches issued by this batch since creation (counted on the device). */
+long long sayram_batch_launches(sayram_batch b);
+void sayram_batch_destroy(sayram_batch b);
+
+/* Bytes of device memory an instance of nx*ny cells needs (admission control). */
+size_t sayram_instance_bytes(int nx, int ny, int precision);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SAYRAM_GPU_H */

@@ -1,0 +1,223 @@
+"""TEST INFRASTRUCTURE: Python front end of the CPU oracle (the checker, never the product).
+
+Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` may import this
+module.  It wraps
+
+  * ``_build/libppfv_oracle.so`` -- ppfv_oracle.c, the C restatement of Sayram-2D's
+    ``Solver::update()`` (source/Solver.cc:270-290) with a banded direct LU;
+  * scipy's SuperLU (``splu``, COLAMD column ordering) -- the same supernodal-LU/COLAMD family
+    as the reference's ``Eigen::SparseLU<SpMat, COLAMDOrdering<int>>`` (Solver.h:35), used as a
+    second direct solver and for grids where banded LU is too slow;
+  * ``_ref/libsayram_ref.so`` when it exists -- the reference's own Solver.cc/Mesh.cc built
+    against the shim headers (Makefile target ``ref``), used to pin the restatement.
+
+Problems are any object with the attributes of ``cases.Problem``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libppfv_oracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libsayram_ref.so")
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_lock = threading.Lock()
+_lib = None
+_ref = None
+
+
+class _OrcProblem(ctypes.Structure):
+    _fields_ = [
+        ("nx", ctypes.c_int), ("ny", ctypes.c_int),
+        ("x_edges", _dp), ("y_edges", _dp),
+        ("dt", ctypes.c_double),
+        ("bc", ctypes.c_int * 4),
+        ("G", _dp), ("Dxx", _dp), ("Dxy", _dp), ("Dyy", _dp), ("inv_tau", _dp),
+        ("dir", _dp * 4),
+    ]
+
+
+def build(force: bool = False) -> str:
+    """Compiles the C restatement (make in this directory)."""
+    if force or not os.path.exists(LIB_PATH):
+        subprocess.run(["make", "-C", HERE, "-s", "all"], check=True)
+    return LIB_PATH
+
+
+def build_ref(reference_root: str = "/root/reference") -> str | None:
+    """Compiles the reference's own solver sources when they are present; returns the path."""
+    if not os.path.isdir(os.path.join(reference_root, "source")):
+        return REF_PATH if os.path.exists(REF_PATH) else None
+    subprocess.run(["make", "-C", HERE, "-s", "ref", f"REF={reference_root}"], check=True)
+    return REF_PATH
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            L = ctypes.CDLL(LIB_PATH)
+            P = ctypes.POINTER(_OrcProblem)
+            L.orc_vertex_f.argtypes = [P, _dp, _dp]
+            L.orc_face_coeffs.argtypes = [P, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp]
+            L.orc_assemble.argtypes = [P, _dp, _dp, _dp]
+            L.orc_solve.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]
+            L.orc_step.argtypes = [P, _dp, ctypes.c_int]
+            for fn in (L.orc_vertex_f, L.orc_face_coeffs, L.orc_assemble, L.orc_solve, L.orc_step):
+                fn.restype = ctypes.c_int
+            _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(_dp)
+
+
+class _Packed:
+    """Keeps contiguous float64 copies alive while the C struct points at them."""
+
+    def __init__(self, prob):
+        c = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        self.keep = [c(prob.x_edges), c(prob.y_edges), c(prob.G), c(prob.Dxx), c(prob.Dxy),
+                     c(prob.Dyy), c(prob.inv_tau)]
+        self.dirs = [None if d is None else c(d) for d in prob.dirichlet]
+        s = _OrcProblem()
+        s.nx, s.ny, s.dt = int(prob.nx), int(prob.ny), float(prob.dt)
+        xe, ye, G, Dxx, Dxy, Dyy, it = self.keep
+        s.x_edges, s.y_edges = _ptr(xe), _ptr(ye)
+        s.G, s.Dxx, s.Dxy, s.Dyy, s.inv_tau = _ptr(G), _ptr(Dxx), _ptr(Dxy), _ptr(Dyy), _ptr(it)
+        for k in range(4):
+            s.bc[k] = int(prob.bc[k])
+            s.dir[k] = _dp() if self.dirs[k] is None else _ptr(self.dirs[k])
+        self.s = s
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise RuntimeError(f"oracle {what} failed with code {rc}")
+
+
+def vertex_f(prob, f):
+    P = _Packed(prob)
+    f = np.ascontiguousarray(f, dtype=np.float64)
+    vf = np.empty((prob.nx + 1, prob.ny + 1))
+    _check(lib().orc_vertex_f(ctypes.byref(P.s), _ptr(f), _ptr(vf)), "vertex_f")
+    return vf
+
+
+def face_coeffs(prob, f, i, j, inbr):
+    """(a_sigma_A, a_sigma_B, a_sigma) of cell (i, j) toward neighbour direction inbr."""
+    P = _Packed(prob)
+    f = np.ascontiguousarray(f, dtype=np.float64)
+    out = np.empty(3)
+    _check(lib().orc_face_coeffs(ctypes.byref(P.s), _ptr(f), i, j, inbr, _ptr(out)), "face_coeffs")
+    return out
+
+
+def assemble(prob, f):
+    """M as five diagonals (5, N) [diag, W, E, S, N] and R (N,), system order K = j*nx + i."""
+    P = _Packed(prob)
+    f = np.ascontiguousarray(f, dtype=np.float64)
+    N = prob.nx * prob.ny
+    M5 = np.empty((5, N))
+    R = np.empty(N)
+    _check(lib().orc_assemble(ctypes.byref(P.s), _ptr(f), _ptr(M5), _ptr(R)), "assemble")
+    return M5, R
+
+
+def to_csc(nx, ny, M5):
+    """scipy CSC matrix of the five diagonals (the reference's SpMat is column-major)."""
+    import scipy.sparse as sp
+
+    N = nx * ny
+    K = np.arange(N)
+    i = K % nx
+    rows, cols, vals = [K], [K], [M5[0]]
+    for d, off, ok in ((1, -1, i > 0), (2, 1, i < nx - 1), (3, -nx, K - nx >= 0), (4, nx, K + nx < N)):
+        rows.append(K[ok]); cols.append(K[ok] + off); vals.append(M5[d][ok])
+    return sp.csc_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(N, N))
+
+
+def solve(nx, ny, M5, R, solver="banded"):
+    """Direct solve of M x = R: banded LU without pivoting, or SuperLU with COLAMD."""
+    if solver == "splu":
+        import scipy.sparse.linalg as spla
+
+        return spla.splu(to_csc(nx, ny, M5), permc_spec="COLAMD").solve(np.asarray(R, dtype=np.float64))
+    M5 = np.ascontiguousarray(M5, dtype=np.float64)
+    R = np.ascontiguousarray(R, dtype=np.float64)
+    x = np.empty(nx * ny)
+    _check(lib().orc_solve(nx, ny, _ptr(M5), _ptr(R), _ptr(x)), "solve")
+    return x
+
+
+def sys_to_field(nx, ny, x):
+    """System order K = j*nx + i -> alpha-major (nx, ny) (the copy back of Solver.cc:280-284)."""
+    return np.ascontiguousarray(np.asarray(x).reshape(ny, nx).T)
+
+
+def field_to_sys(f):
+    return np.ascontiguousarray(np.asarray(f).T).reshape(-1)
+
+
+def step(prob, f=None, nsteps=1, solver="banded"):
+    """nsteps of Solver::update from f (default prob.f0); returns the new alpha-major f."""
+    f = np.array(prob.f0 if f is None else f, dtype=np.float64, copy=True)
+    if solver == "banded":
+        P = _Packed(prob)
+        _check(lib().orc_step(ctypes.byref(P.s), _ptr(f), int(nsteps)), "step")
+        return f
+    for _ in range(nsteps):
+        M5, R = assemble(prob, f)
+        f = sys_to_field(prob.nx, prob.ny, solve(prob.nx, prob.ny, M5, R, solver))
+    return f
+
+
+def column_sums(nx, ny, M5):
+    """1^T M per column (the discrete conservation law 1^T M f = 1^T R)."""
+    return np.asarray(to_csc(nx, ny, M5).sum(axis=0)).ravel()
+
+
+# ----------------------------------------------------------------------------- reference build
+def ref_lib():
+    global _ref
+    with _lock:
+        if _ref is None:
+            if not os.path.exists(REF_PATH):
+                return None
+            L = ctypes.CDLL(REF_PATH)
+            L.ref_run.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, ctypes.c_double,
+                                  ctypes.POINTER(ctypes.c_int), _dp, _dp, _dp, _dp, _dp, _dp,
+                                  ctypes.POINTER(_dp), ctypes.c_int, _dp, _dp, _dp]
+            L.ref_run.restype = ctypes.c_int
+            L.ref_last_error.restype = ctypes.c_char_p
+            _ref = L
+    return _ref
+
+
+def ref_run(prob, nsteps):
+    """Runs the reference's own Solver (oracle/_ref). Returns (M5, R, f): the matrix and RHS that
+    its constructor assembles from f0, and f after nsteps updates."""
+    L = ref_lib()
+    if L is None:
+        raise RuntimeError("reference build not available (make -C oracle ref)")
+    P = _Packed(prob)
+    f0 = np.ascontiguousarray(prob.f0, dtype=np.float64)
+    N = prob.nx * prob.ny
+    M5 = np.empty((5, N))
+    R = np.empty(N)
+    f = np.empty((prob.nx, prob.ny))
+    bc = (ctypes.c_int * 4)(*[int(b) for b in prob.bc])
+    dirs = (_dp * 4)(*[P.s.dir[k] for k in range(4)])
+    rc = L.ref_run(prob.nx, prob.ny, P.s.x_edges, P.s.y_edges, prob.dt, bc, P.s.G, P.s.Dxx,
+                   P.s.Dxy, P.s.Dyy, P.s.inv_tau, _ptr(f0), dirs, int(nsteps), _ptr(M5), _ptr(R), _ptr(f))
+    if rc != 0:
+        raise RuntimeError("reference run failed: " + L.ref_last_error().decode())
+    return M5, R, f

@@ -1,0 +1,39 @@
+// TEST INFRASTRUCTURE: a project-written stand-in for the xtensor containers that Sayram-2D's
+// Solver/Mesh/Equation headers use (row-major 2-D storage, resize(shape), operator()(i,j), fill).
+#pragma once
+#include <array>
+#include <cstddef>
+#include <initializer_list>
+#include <vector>
+
+namespace xt {
+
+template <typename T, std::size_t Rank = 2>
+struct xtensor {
+  std::vector<T> data_;
+  std::size_t n0 = 0, n1 = 0;
+  void resize(const std::array<std::size_t, 2>& s) {
+    n0 = s[0];
+    n1 = s[1];
+    data_.assign(n0 * n1, T());
+  }
+  void resize(std::initializer_list<std::size_t> s) {
+    auto it = s.begin();
+    std::array<std::size_t, 2> a = {*it, *(it + 1)};
+    resize(a);
+  }
+  T& operator()(std::size_t i, std::size_t j) { return data_[i * n1 + j]; }
+  const T& operator()(std::size_t i, std::size_t j) const { return data_[i * n1 + j]; }
+  void fill(const T& v) {
+    for (auto& x : data_) x = v;
+  }
+  T* data() { return data_.data(); }
+  const T* data() const { return data_.data(); }
+};
+
+template <typename T>
+struct xarray {
+  std::vector<T> data_;
+};
+
+}  // namespace xt

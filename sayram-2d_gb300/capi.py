@@ -1,0 +1,284 @@
+"""ctypes binding of the C-ABI in ``include/sayram_gpu.h`` -- the binding a Python caller of the
+reference's ``Solver`` would add -- plus thin classes with the reference's names.
+
+``Solver`` mirrors ``class Solver`` (Sayram-2D ``source/Solver.h:18-26``): construct from a
+problem (the Mesh + Equation data), ``update()`` advances one backward-Euler step, ``f()`` returns
+the (nx, ny) alpha-major state, ``t()`` the simulated time.  Failures raise ``RuntimeError`` as the
+reference throws ``std::runtime_error`` (``Grid2D.h:46-66``, ``Solver.cc:393``).
+
+The compute path is the CUDA library only: if ``_build/libsayram_gpu.so`` is missing or no GPU is
+present, construction fails loudly; nothing here falls back to a CPU implementation.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import build as _build
+
+_dp = ctypes.POINTER(ctypes.c_double)
+
+OK, ERR_ARG, ERR_OOM, ERR_NOT_CONVERGED, ERR_NEGATIVE, ERR_TIMEOUT, ERR_CUDA, ERR_BUDGET, ERR_STATE = range(9)
+FP64, FP32_REFINE = 0, 1
+
+
+class sayram_problem(ctypes.Structure):
+    _fields_ = [
+        ("nx", ctypes.c_int), ("ny", ctypes.c_int),
+        ("x_edges", _dp), ("y_edges", _dp),
+        ("dt", ctypes.c_double),
+        ("bc", ctypes.c_int * 4),
+        ("G", _dp), ("Dxx", _dp), ("Dxy", _dp), ("Dyy", _dp), ("inv_tau", _dp), ("f0", _dp),
+        ("dirichlet", _dp * 4),
+    ]
+
+
+class sayram_options(ctypes.Structure):
+    _fields_ = [
+        ("precision", ctypes.c_int), ("tol", ctypes.c_double), ("inner_tol", ctypes.c_double),
+        ("max_iters", ctypes.c_int), ("max_refine", ctypes.c_int), ("device", ctypes.c_int),
+        ("use_graph", ctypes.c_int),
+    ]
+
+
+class sayram_stats(ctypes.Structure):
+    _fields_ = [
+        ("steps", ctypes.c_longlong), ("t", ctypes.c_double), ("status", ctypes.c_int),
+        ("refinements", ctypes.c_int), ("iterations", ctypes.c_int),
+        ("rel_residual", ctypes.c_double), ("min_f", ctypes.c_double),
+        ("clamped", ctypes.c_longlong), ("mass_drift", ctypes.c_double),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+# name -> (restype, argtypes); every symbol the header declares
+_P = ctypes.c_void_p
+SIGNATURES = {
+    "sayram_last_error": (ctypes.c_char_p, []),
+    "sayram_version": (ctypes.c_char_p, []),
+    "sayram_default_options": (None, [ctypes.POINTER(sayram_options)]),
+    "sayram_host_alloc": (ctypes.c_void_p, [ctypes.c_size_t]),
+    "sayram_host_free": (None, [ctypes.c_void_p]),
+    "sayram_create": (ctypes.c_int, [ctypes.POINTER(sayram_problem), ctypes.POINTER(sayram_options), ctypes.POINTER(_P)]),
+    "sayram_update": (ctypes.c_int, [_P]),
+    "sayram_step": (ctypes.c_int, [_P, ctypes.c_int]),
+    "sayram_t": (ctypes.c_double, [_P]),
+    "sayram_get_f": (ctypes.c_int, [_P, _dp]),
+    "sayram_set_f": (ctypes.c_int, [_P, _dp]),
+    "sayram_set_dirichlet": (ctypes.c_int, [_P, ctypes.c_int, _dp, ctypes.c_int]),
+    "sayram_set_coeffs": (ctypes.c_int, [_P, _dp, _dp, _dp, _dp, _dp]),
+    "sayram_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(sayram_stats)]),
+    "sayram_destroy": (None, [_P]),
+    "sayram_batch_create": (ctypes.c_int, [ctypes.POINTER(sayram_problem), ctypes.c_int, ctypes.POINTER(sayram_options), ctypes.POINTER(_P)]),
+    "sayram_batch_size": (ctypes.c_int, [_P]),
+    "sayram_batch_step": (ctypes.c_int, [_P, ctypes.c_int]),
+    "sayram_batch_step_host": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
+    "sayram_batch_get_f": (ctypes.c_int, [_P, ctypes.c_int, _dp]),
+    "sayram_batch_set_f": (ctypes.c_int, [_P, ctypes.c_int, _dp]),
+    "sayram_batch_set_dirichlet": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, _dp, ctypes.c_int]),
+    "sayram_batch_set_coeffs": (ctypes.c_int, [_P, ctypes.c_int, _dp, _dp, _dp, _dp, _dp]),
+    "sayram_batch_stats": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(sayram_stats)]),
+    "sayram_batch_export_system": (ctypes.c_int, [_P, ctypes.c_int, _dp, _dp]),
+    "sayram_batch_device_bytes": (ctypes.c_size_t, [_P]),
+    "sayram_batch_stream": (ctypes.c_void_p, [_P]),
+    "sayram_batch_enable_timing": (ctypes.c_int, [_P, ctypes.c_int]),
+    "sayram_batch_kernel_times": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_char_p), _dp, ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
+    "sayram_batch_launches": (ctypes.c_longlong, [_P]),
+    "sayram_batch_destroy": (None, [_P]),
+    "sayram_instance_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+}
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = False):
+    """Loads libsayram_gpu.so (raises if it is missing, unless build_if_missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError(f"{path} is missing: build it first (build.build() / __graft_entry__.build())")
+        _build.build()
+    L = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    return (load().sayram_last_error() or b"").decode()
+
+
+def check(rc: int, what: str, allow=(OK,)) -> int:
+    if rc not in allow:
+        raise RuntimeError(f"{what} failed (status {rc}): {last_error()}")
+    return rc
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return a.ctypes.data_as(_dp) if a is not None else _dp()
+
+
+class _Pack:
+    """A sayram_problem array and the numpy buffers it points into (kept alive)."""
+
+    def __init__(self, problems: Sequence):
+        self.keep: List[np.ndarray] = []
+        self.arr = (sayram_problem * len(problems))()
+        for k, p in enumerate(problems):
+            s = self.arr[k]
+            s.nx, s.ny, s.dt = int(p.nx), int(p.ny), float(p.dt)
+            for name in ("x_edges", "y_edges", "G", "Dxx", "Dxy", "Dyy", "inv_tau", "f0"):
+                a = _f64(getattr(p, name))
+                self.keep.append(a)
+                setattr(s, name, _ptr(a))
+            for side in range(4):
+                s.bc[side] = int(p.bc[side])
+                d = p.dirichlet[side]
+                if d is None:
+                    s.dirichlet[side] = _dp()
+                else:
+                    a = _f64(d)
+                    self.keep.append(a)
+                    s.dirichlet[side] = _ptr(a)
+
+
+def options(precision: int = FP64, tol: float = 0.0, inner_tol: float = -1.0, max_iters: int = 500,
+            max_refine: int = 6, device: int = 0, use_graph: int = 1) -> sayram_options:
+    o = sayram_options()
+    load().sayram_default_options(ctypes.byref(o))
+    o.precision, o.tol, o.inner_tol = precision, tol, inner_tol
+    o.max_iters, o.max_refine, o.device, o.use_graph = max_iters, max_refine, device, use_graph
+    return o
+
+
+class Batch:
+    """Many independent instances advanced by the same device launches (sayram_batch_*)."""
+
+    def __init__(self, problems: Sequence, opts: Optional[sayram_options] = None, **kw):
+        L = load()
+        self._L = L
+        self.problems = list(problems)
+        self.shapes = [(int(p.nx), int(p.ny)) for p in self.problems]
+        self.offsets = np.cumsum([0] + [a * b for a, b in self.shapes])
+        pack = _Pack(self.problems)
+        opts = opts if opts is not None else options(**kw)
+        h = ctypes.c_void_p()
+        check(L.sayram_batch_create(pack.arr, len(self.problems), ctypes.byref(opts), ctypes.byref(h)), "sayram_batch_create")
+        self.h = h
+        self.opts = opts
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            self._L.sayram_batch_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __len__(self):
+        return len(self.problems)
+
+    def step(self, nsteps: int = 1, allow_not_converged: bool = False) -> int:
+        allow = (OK, ERR_NOT_CONVERGED) if allow_not_converged else (OK,)
+        return check(self._L.sayram_batch_step(self.h, int(nsteps)), "sayram_batch_step", allow)
+
+    def step_host(self, nsteps: int, f_in_ptr: Optional[int], f_out_ptr: Optional[int], allow_not_converged=False) -> int:
+        allow = (OK, ERR_NOT_CONVERGED) if allow_not_converged else (OK,)
+        return check(self._L.sayram_batch_step_host(self.h, int(nsteps), f_in_ptr, f_out_ptr), "sayram_batch_step_host", allow)
+
+    def f(self, idx: int) -> np.ndarray:
+        nx, ny = self.shapes[idx]
+        out = np.empty((nx, ny))
+        check(self._L.sayram_batch_get_f(self.h, idx, _ptr(out)), "sayram_batch_get_f")
+        return out
+
+    def set_f(self, idx: int, f) -> None:
+        a = _f64(f)
+        check(self._L.sayram_batch_set_f(self.h, idx, _ptr(a)), "sayram_batch_set_f")
+
+    def set_dirichlet(self, idx: int, side: int, v) -> None:
+        a = _f64(v)
+        check(self._L.sayram_batch_set_dirichlet(self.h, idx, side, _ptr(a), a.size), "sayram_batch_set_dirichlet")
+
+    def set_coeffs(self, idx: int, G, Dxx, Dxy, Dyy, inv_tau) -> None:
+        arrs = [_f64(a) for a in (G, Dxx, Dxy, Dyy, inv_tau)]
+        check(self._L.sayram_batch_set_coeffs(self.h, idx, *[_ptr(a) for a in arrs]), "sayram_batch_set_coeffs")
+
+    def stats(self, idx: int) -> dict:
+        s = sayram_stats()
+        check(self._L.sayram_batch_stats(self.h, idx, ctypes.byref(s)), "sayram_batch_stats")
+        return s.as_dict()
+
+    def export_system(self, idx: int):
+        """(M5, R) assembled from the current f of instance idx, reference (unscaled) form."""
+        nx, ny = self.shapes[idx]
+        M5 = np.empty((5, nx * ny))
+        R = np.empty(nx * ny)
+        check(self._L.sayram_batch_export_system(self.h, idx, _ptr(M5), _ptr(R)), "sayram_batch_export_system")
+        return M5, R
+
+    def device_bytes(self) -> int:
+        return int(self._L.sayram_batch_device_bytes(self.h))
+
+    def stream(self) -> int:
+        return int(self._L.sayram_batch_stream(self.h) or 0)
+
+    def enable_timing(self, on: bool = True) -> None:
+        check(self._L.sayram_batch_enable_timing(self.h, 1 if on else 0), "sayram_batch_enable_timing")
+
+    def kernel_times(self) -> dict:
+        cap = 64
+        names = (ctypes.c_char_p * cap)()
+        ms = (ctypes.c_double * cap)()
+        cnt = (ctypes.c_longlong * cap)()
+        m = self._L.sayram_batch_kernel_times(self.h, names, ms, cnt, cap)
+        return {names[k].decode(): (ms[k], cnt[k]) for k in range(min(m, cap))}
+
+    def launches(self) -> int:
+        return int(self._L.sayram_batch_launches(self.h))
+
+
+class Solver(Batch):
+    """Drop-in of the reference's ``class Solver`` for one instance (Solver.h:18-26)."""
+
+    def __init__(self, problem, opts: Optional[sayram_options] = None, **kw):
+        super().__init__([problem], opts, **kw)
+        self.problem = problem
+
+    def update(self) -> None:  # Solver::update, Solver.cc:270-290
+        check(self._L.sayram_update(self.h), "sayram_update")
+
+    def t(self) -> float:  # Solver::t, Solver.h:23
+        return float(self._L.sayram_t(self.h))
+
+    def f(self, idx: int = 0) -> np.ndarray:  # Solver::f, Solver.h:24
+        return super().f(0)
+
+    def get_stats(self) -> dict:
+        return self.stats(0)
+
+
+def instance_bytes(nx: int, ny: int, precision: int = FP32_REFINE) -> int:
+    return int(load().sayram_instance_bytes(nx, ny, precision))

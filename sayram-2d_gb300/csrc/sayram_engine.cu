@@ -1,0 +1,717 @@
+// sayram_engine.cu -- host runtime and C-ABI of the GB300 Sayram-2D hot path.
+//
+// An Engine owns one batch of instances (a single Solver is a batch of one): the padded device
+// layout, the chunk/tile work lists, the per-step launch sequence and the optional CUDA graph.
+// Every public function returns a status code and records a message for sayram_last_error().
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "sayram_gpu.h"
+#include "sayram_ops.cuh"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define SG_CUDA(call)                                                                      \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      return fail(SAYRAM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));    \
+  } while (0)
+
+long long round_up(long long a, long long m) { return (a + m - 1) / m * m; }
+
+using sg::Ctl;
+using sg::InstDev;
+using sg::InstState;
+
+struct Stage {  // per-instance host data kept for the layout
+  int nx, ny;
+  std::vector<double> xe, ye;
+};
+
+}  // namespace
+
+struct sayram_batch_s {
+  sayram_options opt{};
+  int dev = 0;
+  int nsm = 0;
+  cudaStream_t stream = nullptr;
+  int n = 0;
+  std::vector<InstDev> hinst;
+  std::vector<Stage> stage;
+  long long ncell = 0;      // padded storage cells
+  long long nreal = 0;      // real cells (packed alpha-major size)
+  int nchunks = 0, ntiles = 0;
+  size_t bytes = 0;
+  bool mixed = false;
+
+  // device memory
+  std::vector<void*> allocs;
+  InstDev* d_inst = nullptr;
+  InstState* d_st = nullptr;
+  Ctl* d_ctl = nullptr;
+  Ctl* h_ctl = nullptr;  // pinned mirror
+  int* d_chunk = nullptr;
+  int* d_tile = nullptr;
+  double *d_xe = nullptr, *d_ye = nullptr, *d_wx = nullptr, *d_wy = nullptr, *d_dirv = nullptr;
+  double* d_part = nullptr;
+  double* d_stage = nullptr;   // 6 * max instance cells (setup) / packed field (get/set)
+  long long stage_cells = 0;
+  sg::Geo geo{};
+  sg::Fields fl{};
+  sg::Coef<double> c64{};
+  sg::Coef<float> c32{};
+  sg::Kry<double> k64{};
+  sg::Kry<float> k32{};
+  sg::Common cm{};
+
+  // timing
+  bool timing = false;
+  std::vector<std::string> tnames;
+  std::vector<double> tms;
+  std::vector<long long> tcount;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+  std::vector<cudaEvent_t> evpool;
+  size_t evused = 0;
+
+  ~sayram_batch_s() { release(); }
+
+  void release() {
+    if (dev >= 0) cudaSetDevice(dev);
+    for (void* p : allocs) cudaFree(p);
+    allocs.clear();
+    if (h_ctl) cudaFreeHost(h_ctl);
+    h_ctl = nullptr;
+    for (auto e : evpool) cudaEventDestroy(e);
+    evpool.clear();
+    if (stream) cudaStreamDestroy(stream);
+    stream = nullptr;
+  }
+
+  template <typename T>
+  int alloc(T** p, long long count) {
+    void* q = nullptr;
+    const size_t nb = (size_t)std::max<long long>(count, 1) * sizeof(T);
+    cudaError_t e = cudaMalloc(&q, nb);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(SAYRAM_ERR_OOM, "cudaMalloc of " + std::to_string(nb) + " bytes failed: " +
+                                      cudaGetErrorString(e));
+    }
+    allocs.push_back(q);
+    bytes += nb;
+    e = cudaMemsetAsync(q, 0, nb, stream);
+    if (e != cudaSuccess) return fail(SAYRAM_ERR_CUDA, cudaGetErrorString(e));
+    *p = (T*)q;
+    return SAYRAM_OK;
+  }
+
+  // ---- timing helpers
+  int tid(const char* name) {
+    for (size_t k = 0; k < tnames.size(); ++k)
+      if (tnames[k] == name) return (int)k;
+    tnames.push_back(name);
+    tms.push_back(0.0);
+    tcount.push_back(0);
+    return (int)tnames.size() - 1;
+  }
+  cudaEvent_t ev() {
+    if (evused == evpool.size()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      evpool.push_back(e);
+    }
+    return evpool[evused++];
+  }
+  template <typename F>
+  void launch(const char* name, F&& f) {
+    if (!timing) {
+      f();
+      return;
+    }
+    cudaEvent_t a = ev(), b = ev();
+    cudaEventRecord(a, stream);
+    f();
+    cudaEventRecord(b, stream);
+    pending.push_back({tid(name), {a, b}});
+  }
+  void collect_timing() {
+    for (auto& p : pending) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, p.second.first, p.second.second);
+      tms[p.first] += ms;
+      tcount[p.first] += 1;
+    }
+    pending.clear();
+    evused = 0;
+  }
+
+  int grid_stream() const { return std::max(1, std::min(nchunks, nsm * 16)); }
+  int grid_tiles() const { return std::max(1, std::min(ntiles, nsm * 8)); }
+
+  int build(const sayram_problem* probs, int count, const sayram_options* o);
+  int upload_instance(int b, const sayram_problem& p, bool coeffs, bool f0);
+  int run_steps(int nsteps);
+  int read_ctl();
+  int finish_status();
+  template <typename T, typename C>
+  int step_once(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, const sg::Kry<T>& kr);
+};
+
+static int validate_problem(const sayram_problem& p) {
+  if (p.nx < 1 || p.ny < 1) return fail(SAYRAM_ERR_ARG, "Grid2D: x_edges/y_edges must have size >= 2.");
+  if ((long long)p.nx * p.ny > (1LL << 31)) return fail(SAYRAM_ERR_ARG, "grid too large");
+  if (!p.x_edges || !p.y_edges) return fail(SAYRAM_ERR_ARG, "missing edges");
+  for (int i = 0; i < p.nx; ++i)
+    if (!(p.x_edges[i + 1] > p.x_edges[i]))
+      return fail(SAYRAM_ERR_ARG, "Grid2D: x_edges must be strictly increasing at i=" + std::to_string(i));
+  for (int j = 0; j < p.ny; ++j)
+    if (!(p.y_edges[j + 1] > p.y_edges[j]))
+      return fail(SAYRAM_ERR_ARG, "Grid2D: y_edges must be strictly increasing at j=" + std::to_string(j));
+  if (!(p.dt > 0) || !std::isfinite(p.dt)) return fail(SAYRAM_ERR_ARG, "dt must be positive");
+  if (!p.G || !p.Dxx || !p.Dxy || !p.Dyy || !p.inv_tau || !p.f0)
+    return fail(SAYRAM_ERR_ARG, "missing coefficient or initial-state array");
+  for (int s = 0; s < 4; ++s) {
+    if (p.bc[s] != SAYRAM_DIRICHLET && p.bc[s] != SAYRAM_ZEROFLUX)
+      return fail(SAYRAM_ERR_ARG, "unknown boundary type");
+    if (p.bc[s] == SAYRAM_DIRICHLET && !p.dirichlet[s])
+      return fail(SAYRAM_ERR_ARG, "Dirichlet BC: missing value.");  // Solver.cc:393
+  }
+  return SAYRAM_OK;
+}
+
+int sayram_batch_s::build(const sayram_problem* probs, int count, const sayram_options* o) {
+  sayram_default_options(&opt);
+  if (o) opt = *o;
+  if (opt.precision != SAYRAM_FP64 && opt.precision != SAYRAM_FP32_REFINE)
+    return fail(SAYRAM_ERR_ARG, "unknown precision");
+  if (!(opt.tol > 0)) opt.tol = opt.precision == SAYRAM_FP64 ? 1e-12 : 1e-10;
+  if (opt.inner_tol < 0) opt.inner_tol = 0;
+  if (opt.max_iters < 1) opt.max_iters = 1;
+  if (opt.max_refine < 2) opt.max_refine = 2;
+  mixed = opt.precision == SAYRAM_FP32_REFINE;
+  for (int b = 0; b < count; ++b) {
+    int rc = validate_problem(probs[b]);
+    if (rc) return fail(rc, "instance " + std::to_string(b) + ": " + g_err);
+  }
+  dev = opt.device;
+  int ndev = 0;
+  SG_CUDA(cudaGetDeviceCount(&ndev));
+  if (dev < 0 || dev >= ndev) return fail(SAYRAM_ERR_ARG, "no such CUDA device");
+  SG_CUDA(cudaSetDevice(dev));
+  SG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  SG_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  n = count;
+  hinst.resize(n);
+  stage.resize(n);
+  // ---- layout
+  long long cursor = 0, hoff = 0;
+  int chunk = 0, tile = 0, xoff = 0, yoff = 0, doff = 0;
+  long long maxcells = 0;
+  std::vector<int> chunk_inst, tile_inst;
+  for (int b = 0; b < n; ++b) {
+    const sayram_problem& p = probs[b];
+    InstDev& I = hinst[b];
+    std::memset(&I, 0, sizeof(I));
+    I.nx = p.nx;
+    I.ny = p.ny;
+    I.pitch = (int)round_up(p.nx, 4);
+    I.enabled = 1;
+    for (int s = 0; s < 4; ++s) I.bc[s] = p.bc[s];
+    I.base = cursor + I.pitch;
+    cursor += round_up((long long)(p.ny + 2) * I.pitch, 32);
+    I.hoff = hoff;
+    hoff += (long long)p.nx * p.ny;
+    I.chunk0 = chunk;
+    I.nchunks = (int)((round_up((long long)p.ny * I.pitch, 4) + sg::kChunk - 1) / sg::kChunk);
+    for (int k = 0; k < I.nchunks; ++k) chunk_inst.push_back(b);
+    chunk += I.nchunks;
+    I.tile0 = tile;
+    I.ntx = (p.nx + sg::kTX - 1) / sg::kTX;
+    I.nty = (p.ny + sg::kTY - 1) / sg::kTY;
+    for (int k = 0; k < I.ntx * I.nty; ++k) tile_inst.push_back(b);
+    tile += I.ntx * I.nty;
+    I.xe = xoff;
+    xoff += p.nx + 1;
+    I.ye = yoff;
+    yoff += p.ny + 1;
+    for (int s = 0; s < 4; ++s) {
+      if (p.bc[s] == SAYRAM_DIRICHLET) {
+        I.dir[s] = doff;
+        doff += (s <= 1) ? p.ny + 1 : p.nx + 1;
+      } else {
+        I.dir[s] = -1;
+      }
+    }
+    I.dt = p.dt;
+    maxcells = std::max(maxcells, (long long)p.nx * p.ny);
+  }
+  ncell = cursor + 64;
+  nreal = hoff;
+  nchunks = chunk;
+  ntiles = tile;
+  stage_cells = std::max(6 * maxcells, nreal);
+  // ---- allocations
+  int rc;
+#define SG_ALLOC(p, cnt) \
+  if ((rc = alloc(&(p), (cnt))) != SAYRAM_OK) return rc
+  SG_ALLOC(d_inst, n);
+  SG_ALLOC(d_st, n);
+  SG_ALLOC(d_ctl, 1);
+  SG_ALLOC(d_chunk, nchunks);
+  SG_ALLOC(d_tile, ntiles);
+  SG_ALLOC(d_xe, xoff);
+  SG_ALLOC(d_ye, yoff);
+  SG_ALLOC(d_wx, 2 * xoff);
+  SG_ALLOC(d_wy, 2 * yoff);
+  SG_ALLOC(d_dirv, std::max(doff, 1));
+  SG_ALLOC(d_part, 4LL * nchunks);
+  SG_ALLOC(d_stage, stage_cells);
+  double** geos[8] = {&geo.aAx, &geo.aBx, &geo.Sx, &geo.aAy, &geo.aBy, &geo.Sy, &geo.ukk, &geo.sdiag};
+  for (auto g : geos) SG_ALLOC(*g, ncell);
+  SG_ALLOC(fl.f, ncell);
+  SG_ALLOC(fl.invD, ncell);
+  SG_ALLOC(fl.R, ncell);
+  SG_ALLOC(fl.colsum, ncell);
+  SG_ALLOC(fl.y64[0], ncell);
+  SG_ALLOC(fl.y64[1], ncell);
+  if (mixed) {
+    float** cs[8] = {&c32.cw, &c32.ce, &c32.cs, &c32.cn, &c32.lw, &c32.le, &c32.ls, &c32.ln};
+    for (auto c : cs) SG_ALLOC(*c, ncell);
+    float** ks[8] = {&k32.r, &k32.rh, &k32.t, &k32.x, &k32.p[0], &k32.p[1], &k32.v[0], &k32.v[1]};
+    for (auto k : ks) SG_ALLOC(*k, ncell);
+  } else {
+    double** cs[4] = {&c64.cw, &c64.ce, &c64.cs, &c64.cn};
+    for (auto c : cs) SG_ALLOC(*c, ncell);
+    double** ks[8] = {&k64.r, &k64.rh, &k64.t, &k64.x, &k64.p[0], &k64.p[1], &k64.v[0], &k64.v[1]};
+    for (auto k : ks) SG_ALLOC(*k, ncell);
+  }
+#undef SG_ALLOC
+  SG_CUDA(cudaMallocHost(&h_ctl, sizeof(Ctl)));
+  std::memset(h_ctl, 0, sizeof(Ctl));
+  // ---- tables
+  std::vector<double> xe(xoff), ye(yoff), wx(2 * xoff, 0.0), wy(2 * yoff, 0.0), dirv(std::max(doff, 1), 0.0);
+  for (int b = 0; b < n; ++b) {
+    const sayram_problem& p = probs[b];
+    const InstDev& I = hinst[b];
+    for (int i = 0; i <= p.nx; ++i) xe[I.xe + i] = p.x_edges[i];
+    for (int j = 0; j <= p.ny; ++j) ye[I.ye + j] = p.y_edges[j];
+    // bilinear weights of Solver.cc:333-336 (per vertex column / row, interior and edges)
+    for (int i = 1; i < p.nx; ++i) {
+      const double xv = p.x_edges[i];
+      const double xl = 0.5 * (p.x_edges[i - 1] + p.x_edges[i]), xr = 0.5 * (p.x_edges[i] + p.x_edges[i + 1]);
+      wx[2 * (I.xe + i)] = (xr - xv) / (xr - xl);
+      wx[2 * (I.xe + i) + 1] = (xv - xl) / (xr - xl);
+    }
+    for (int j = 1; j < p.ny; ++j) {
+      const double yv = p.y_edges[j];
+      const double yb = 0.5 * (p.y_edges[j - 1] + p.y_edges[j]), yt = 0.5 * (p.y_edges[j] + p.y_edges[j + 1]);
+      wy[2 * (I.ye + j)] = (yt - yv) / (yt - yb);
+      wy[2 * (I.ye + j) + 1] = (yv - yb) / (yt - yb);
+    }
+    for (int s = 0; s < 4; ++s)
+      if (I.dir[s] >= 0) {
+        const int m = (s <= 1) ? p.ny + 1 : p.nx + 1;
+        for (int k = 0; k < m; ++k) dirv[I.dir[s] + k] = p.dirichlet[s][k];
+      }
+    stage[b].nx = p.nx;
+    stage[b].ny = p.ny;
+  }
+  SG_CUDA(cudaMemcpyAsync(d_inst, hinst.data(), sizeof(InstDev) * n, cudaMemcpyHostToDevice, stream));
+  SG_CUDA(cudaMemcpyAsync(d_chunk, chunk_inst.data(), sizeof(int) * nchunks, cudaMemcpyHostToDevice, stream));
+  SG_CUDA(cudaMemcpyAsync(d_tile, tile_inst.data(), sizeof(int) * ntiles, cudaMemcpyHostToDevice, stream));
+  SG_CUDA(cudaMemcpyAsync(d_xe, xe.data(), sizeof(double) * xoff, cudaMemcpyHostToDevice, stream));
+  SG_CUDA(cudaMemcpyAsync(d_ye, ye.data(), sizeof(double) * yoff, cudaMemcpyHostToDevice, stream));
+  SG_CUDA(cudaMemcpyAsync(d_wx, wx.data(), sizeof(double) * 2 * xoff, cudaMemcpyHostToDevice, stream));
+  SG_CUDA(cudaMemcpyAsync(d_wy, wy.data(), sizeof(double) * 2 * yoff, cudaMemcpyHostToDevice, stream));
+  SG_CUDA(cudaMemcpyAsync(d_dirv, dirv.data(), sizeof(double) * dirv.size(), cudaMemcpyHostToDevice, stream));
+  SG_CUDA(cudaStreamSynchronize(stream));
+  cm.inst = d_inst;
+  cm.st = d_st;
+  cm.ctl = d_ctl;
+  cm.chunk_inst = d_chunk;
+  cm.nchunks = nchunks;
+  cm.tile_inst = d_tile;
+  cm.ntiles = ntiles;
+  cm.ninst = n;
+  cm.wx = d_wx;
+  cm.wy = d_wy;
+  cm.dirv = d_dirv;
+  cm.part = d_part;
+  for (int b = 0; b < n; ++b) {
+    rc = upload_instance(b, probs[b], true, true);
+    if (rc) return rc;
+  }
+  SG_CUDA(cudaStreamSynchronize(stream));
+  return SAYRAM_OK;
+}
+
+// Copies one instance's coefficient fields (and f0) into the staging buffer and runs k_setup.
+int sayram_batch_s::upload_instance(int b, const sayram_problem& p, bool coeffs, bool f0) {
+  const long long nc = (long long)p.nx * p.ny;
+  const double* src[6] = {p.G, p.Dxx, p.Dxy, p.Dyy, p.inv_tau, p.f0};
+  int mask = 0;
+  for (int k = 0; k < 6; ++k) {
+    const bool want = (k < 5) ? coeffs : f0;
+    if (!want || !src[k]) continue;
+    SG_CUDA(cudaMemcpyAsync(d_stage + k * nc, src[k], sizeof(double) * nc, cudaMemcpyHostToDevice, stream));
+    mask |= 1 << k;
+  }
+  if (coeffs && (mask & 31) != 31) return fail(SAYRAM_ERR_ARG, "all coefficient fields are required");
+  const int threads = 256;
+  const int blocks = (int)std::min<long long>((nc + threads - 1) / threads, (long long)nsm * 8);
+  sg::k_setup<<<blocks, threads, 0, stream>>>(cm, geo, fl.f, d_stage, d_xe, d_ye, b, mask);
+  SG_CUDA(cudaGetLastError());
+  // the staging buffer is reused by the next upload: keep the stream ordered
+  SG_CUDA(cudaStreamSynchronize(stream));
+  return SAYRAM_OK;
+}
+
+int sayram_batch_s::read_ctl() {
+  SG_CUDA(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, stream));
+  SG_CUDA(cudaStreamSynchronize(stream));
+  return SAYRAM_OK;
+}
+
+template <typename T, typename C>
+int sayram_batch_s::step_once(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, const sg::Kry<T>& kr) {
+  using namespace sg;
+  const int gs = grid_stream(), gt = grid_tiles();
+  SG_CUDA(cudaMemsetAsync(d_ctl, 0, 2 * sizeof(int), stream));
+  launch("begin", [&] { k_begin<<<(n + 255) / 256, 256, 0, stream>>>(cm); });
+  launch("assemble", [&] { k_assemble<C><<<gt, kAsmThreads, 0, stream>>>(cm, geo, fl, cfull); });
+  for (int o = 0; o < opt.max_refine; ++o) {
+    launch("resid", [&] {
+      k_resid<T, C><<<gs, kThreads, 0, stream>>>(cm, fl, cfull, kr, opt.tol, opt.inner_tol, opt.max_refine);
+    });
+    SG_CUDA(cudaGetLastError());
+    if (o == opt.max_refine - 1) break;
+    int rc = read_ctl();
+    if (rc) return rc;
+    if (h_ctl->n_outer == 0) break;
+    for (int it = 0; it < opt.max_iters; ++it) {
+      launch("bicg1", [&] { k_bicg1<T><<<gs, kThreads, 0, stream>>>(cm, ck, kr); });
+      launch("bicg2", [&] { k_bicg2<T><<<gs, kThreads, 0, stream>>>(cm, ck, kr); });
+      launch("bicg3", [&] { k_bicg3<T><<<gs, kThreads, 0, stream>>>(cm, kr, opt.max_iters); });
+      SG_CUDA(cudaGetLastError());
+      if (it < 4 || (it & 3) == 3) {
+        rc = read_ctl();
+        if (rc) return rc;
+        if (h_ctl->n_inner == 0) break;
+      }
+    }
+  }
+  launch("polish", [&] { k_polish<C><<<gs, kThreads, 0, stream>>>(cm, fl, cfull); });
+  SG_CUDA(cudaGetLastError());
+  return SAYRAM_OK;
+}
+
+int sayram_batch_s::run_steps(int nsteps) {
+  if (nsteps < 0) return fail(SAYRAM_ERR_ARG, "nsteps must be >= 0");
+  SG_CUDA(cudaSetDevice(dev));
+  for (int s = 0; s < nsteps; ++s) {
+    int rc = mixed ? step_once<float, float>(c32, c32, k32) : step_once<double, double>(c64, c64, k64);
+    if (rc) return rc;
+  }
+  SG_CUDA(cudaStreamSynchronize(stream));
+  if (timing) collect_timing();
+  return finish_status();
+}
+
+int sayram_batch_s::finish_status() {
+  std::vector<InstState> hs(n);
+  SG_CUDA(cudaMemcpyAsync(hs.data(), d_st, sizeof(InstState) * n, cudaMemcpyDeviceToHost, stream));
+  SG_CUDA(cudaStreamSynchronize(stream));
+  int worst = SAYRAM_OK;
+  for (int b = 0; b < n; ++b) {
+    if (!hinst[b].enabled || hs[b].steps == 0) continue;
+    if (hs[b].status == sg::ST_NEGATIVE) worst = SAYRAM_ERR_NEGATIVE;
+    else if (hs[b].status == sg::ST_NOT_CONVERGED && worst == SAYRAM_OK) worst = SAYRAM_ERR_NOT_CONVERGED;
+  }
+  if (worst == SAYRAM_ERR_NEGATIVE) return fail(worst, "a negative cell survived the positivity polish");
+  if (worst == SAYRAM_ERR_NOT_CONVERGED) return fail(worst, "a step ended above the residual target");
+  return SAYRAM_OK;
+}
+
+// ================================================================================== C-ABI
+extern "C" {
+
+const char* sayram_last_error(void) { return g_err.c_str(); }
+const char* sayram_version(void) { return "sayram-gb300 0.1 (sm_103a)"; }
+
+void sayram_default_options(sayram_options* o) {
+  if (!o) return;
+  o->precision = SAYRAM_FP64;
+  o->tol = 0.0;
+  o->inner_tol = -1.0;
+  o->max_iters = 500;
+  o->max_refine = 6;
+  o->device = 0;
+  o->use_graph = 1;
+}
+
+void* sayram_host_alloc(size_t bytes) {
+  void* p = nullptr;
+  if (cudaMallocHost(&p, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    g_err = "cudaMallocHost failed";
+    return nullptr;
+  }
+  return p;
+}
+void sayram_host_free(void* p) {
+  if (p) cudaFreeHost(p);
+}
+
+int sayram_batch_create(const sayram_problem* probs, int n, const sayram_options* opt, sayram_batch* out) {
+  if (!out) return fail(SAYRAM_ERR_ARG, "null output handle");
+  *out = nullptr;
+  if (!probs || n < 1) return fail(SAYRAM_ERR_ARG, "empty batch");
+  sayram_batch_s* b = new (std::nothrow) sayram_batch_s();
+  if (!b) return fail(SAYRAM_ERR_OOM, "host allocation failed");
+  sayram_options o;
+  sayram_default_options(&o);
+  if (opt) o = *opt;
+  if (o.inner_tol < 0) o.inner_tol = (o.precision == SAYRAM_FP32_REFINE) ? 1e-4 : 0.0;
+  int rc = b->build(probs, n, &o);
+  if (rc) {
+    std::string msg = g_err;
+    delete b;
+    return fail(rc, msg);
+  }
+  *out = b;
+  g_err.clear();
+  return SAYRAM_OK;
+}
+
+int sayram_batch_size(sayram_batch b) { return b ? b->n : 0; }
+
+int sayram_batch_step(sayram_batch b, int nsteps) {
+  if (!b) return fail(SAYRAM_ERR_ARG, "null handle");
+  return b->run_steps(nsteps);
+}
+
+int sayram_batch_step_host(sayram_batch b, int nsteps, const double* f_in, double* f_out) {
+  if (!b) return fail(SAYRAM_ERR_ARG, "null handle");
+  SG_CUDA(cudaSetDevice(b->dev));
+  if (f_in) {
+    SG_CUDA(cudaMemcpyAsync(b->d_stage, f_in, sizeof(double) * b->nreal, cudaMemcpyHostToDevice, b->stream));
+    b->launch("field_in", [&] {
+      sg::k_field_in<<<b->grid_tiles(), 256, 0, b->stream>>>(b->cm, b->fl.f, b->d_stage);
+    });
+  }
+  int rc = b->run_steps(nsteps);
+  if (rc != SAYRAM_OK && rc != SAYRAM_ERR_NOT_CONVERGED && rc != SAYRAM_ERR_NEGATIVE) return rc;
+  if (f_out) {
+    b->launch("field_out", [&] {
+      sg::k_field_out<<<b->grid_tiles(), 256, 0, b->stream>>>(b->cm, b->d_stage, b->fl.f);
+    });
+    SG_CUDA(cudaMemcpyAsync(f_out, b->d_stage, sizeof(double) * b->nreal, cudaMemcpyDeviceToHost, b->stream));
+    SG_CUDA(cudaStreamSynchronize(b->stream));
+    if (b->timing) b->collect_timing();
+  }
+  return rc;
+}
+
+int sayram_batch_get_f(sayram_batch b, int idx, double* f_out) {
+  if (!b || !f_out || idx < 0 || idx >= b->n) return fail(SAYRAM_ERR_ARG, "bad handle, index or buffer");
+  SG_CUDA(cudaSetDevice(b->dev));
+  const InstDev& I = b->hinst[idx];
+  // rows of the padded layout -> alpha-major on the host
+  std::vector<double> rows((size_t)I.ny * I.pitch);
+  SG_CUDA(cudaMemcpyAsync(rows.data(), b->fl.f + I.base, sizeof(double) * rows.size(), cudaMemcpyDeviceToHost, b->stream));
+  SG_CUDA(cudaStreamSynchronize(b->stream));
+  for (int i = 0; i < I.nx; ++i)
+    for (int j = 0; j < I.ny; ++j) f_out[(size_t)i * I.ny + j] = rows[(size_t)j * I.pitch + i];
+  return SAYRAM_OK;
+}
+
+int sayram_batch_set_f(sayram_batch b, int idx, const double* f) {
+  if (!b || !f || idx < 0 || idx >= b->n) return fail(SAYRAM_ERR_ARG, "bad handle, index or buffer");
+  SG_CUDA(cudaSetDevice(b->dev));
+  const InstDev& I = b->hinst[idx];
+  std::vector<double> rows((size_t)I.ny * I.pitch, 0.0);
+  for (int i = 0; i < I.nx; ++i)
+    for (int j = 0; j < I.ny; ++j) rows[(size_t)j * I.pitch + i] = f[(size_t)i * I.ny + j];
+  SG_CUDA(cudaMemcpyAsync(b->fl.f + I.base, rows.data(), sizeof(double) * rows.size(), cudaMemcpyHostToDevice, b->stream));
+  SG_CUDA(cudaStreamSynchronize(b->stream));
+  return SAYRAM_OK;
+}
+
+int sayram_batch_set_dirichlet(sayram_batch b, int idx, int side, const double* v, int n) {
+  if (!b || !v || idx < 0 || idx >= b->n || side < 0 || side > 3)
+    return fail(SAYRAM_ERR_ARG, "bad handle, index, side or buffer");
+  const InstDev& I = b->hinst[idx];
+  if (I.dir[side] < 0) return fail(SAYRAM_ERR_ARG, "side is not Dirichlet");
+  const int m = (side <= 1) ? I.ny + 1 : I.nx + 1;
+  if (n != m) return fail(SAYRAM_ERR_ARG, "expected " + std::to_string(m) + " vertex values");
+  SG_CUDA(cudaSetDevice(b->dev));
+  SG_CUDA(cudaMemcpyAsync(b->d_dirv + I.dir[side], v, sizeof(double) * m, cudaMemcpyHostToDevice, b->stream));
+  SG_CUDA(cudaStreamSynchronize(b->stream));
+  return SAYRAM_OK;
+}
+
+int sayram_batch_set_coeffs(sayram_batch b, int idx, const double* G, const double* Dxx, const double* Dxy,
+                            const double* Dyy, const double* inv_tau) {
+  if (!b || idx < 0 || idx >= b->n) return fail(SAYRAM_ERR_ARG, "bad handle or index");
+  SG_CUDA(cudaSetDevice(b->dev));
+  const InstDev& I = b->hinst[idx];
+  const long long nc = (long long)I.nx * I.ny;
+  // fields not given keep their current values: fetch them back is not possible (only derived
+  // factors are stored), so all five are required unless the caller passes every one.
+  if (!G || !Dxx || !Dxy || !Dyy || !inv_tau)
+    return fail(SAYRAM_ERR_ARG, "set_coeffs needs all of G, Dxx, Dxy, Dyy, inv_tau");
+  sayram_problem p{};
+  p.nx = I.nx;
+  p.ny = I.ny;
+  p.G = G;
+  p.Dxx = Dxx;
+  p.Dxy = Dxy;
+  p.Dyy = Dyy;
+  p.inv_tau = inv_tau;
+  (void)nc;
+  return b->upload_instance(idx, p, true, false);
+}
+
+int sayram_batch_stats(sayram_batch b, int idx, sayram_stats* out) {
+  if (!b || !out || idx < 0 || idx >= b->n) return fail(SAYRAM_ERR_ARG, "bad handle, index or buffer");
+  SG_CUDA(cudaSetDevice(b->dev));
+  InstState s;
+  SG_CUDA(cudaMemcpyAsync(&s, b->d_st + idx, sizeof(s), cudaMemcpyDeviceToHost, b->stream));
+  SG_CUDA(cudaStreamSynchronize(b->stream));
+  out->steps = s.steps;
+  out->t = (double)s.steps * b->hinst[idx].dt;
+  out->status = s.steps == 0 ? SAYRAM_OK
+                : s.status == sg::ST_NEGATIVE ? SAYRAM_ERR_NEGATIVE
+                : s.status == sg::ST_NOT_CONVERGED ? SAYRAM_ERR_NOT_CONVERGED : SAYRAM_OK;
+  out->refinements = s.refines;
+  out->iterations = s.iters_total;
+  out->rel_residual = s.rel;
+  out->min_f = s.min_f;
+  out->clamped = s.clamped;
+  out->mass_drift = s.mass_drift;
+  return SAYRAM_OK;
+}
+
+int sayram_batch_export_system(sayram_batch b, int idx, double* M5, double* R) {
+  if (!b || !M5 || !R || idx < 0 || idx >= b->n) return fail(SAYRAM_ERR_ARG, "bad handle, index or buffer");
+  SG_CUDA(cudaSetDevice(b->dev));
+  const InstDev& I = b->hinst[idx];
+  if (b->mixed)
+    sg::k_assemble<float><<<b->grid_tiles(), sg::kAsmThreads, 0, b->stream>>>(b->cm, b->geo, b->fl, b->c32);
+  else
+    sg::k_assemble<double><<<b->grid_tiles(), sg::kAsmThreads, 0, b->stream>>>(b->cm, b->geo, b->fl, b->c64);
+  SG_CUDA(cudaGetLastError());
+  const size_t rows = (size_t)I.ny * I.pitch;
+  std::vector<double> invD(rows), Rr(rows), c[4];
+  SG_CUDA(cudaMemcpyAsync(invD.data(), b->fl.invD + I.base, rows * 8, cudaMemcpyDeviceToHost, b->stream));
+  SG_CUDA(cudaMemcpyAsync(Rr.data(), b->fl.R + I.base, rows * 8, cudaMemcpyDeviceToHost, b->stream));
+  for (int k = 0; k < 4; ++k) {
+    c[k].resize(rows);
+    if (b->mixed) {
+      std::vector<float> hi(rows), lo(rows);
+      float* hs[4] = {b->c32.cw, b->c32.ce, b->c32.cs, b->c32.cn};
+      float* ls[4] = {b->c32.lw, b->c32.le, b->c32.ls, b->c32.ln};
+      SG_CUDA(cudaMemcpyAsync(hi.data(), hs[k] + I.base, rows * 4, cudaMemcpyDeviceToHost, b->stream));
+      SG_CUDA(cudaMemcpyAsync(lo.data(), ls[k] + I.base, rows * 4, cudaMemcpyDeviceToHost, b->stream));
+      SG_CUDA(cudaStreamSynchronize(b->stream));
+      for (size_t q = 0; q < rows; ++q) c[k][q] = (double)hi[q] + (double)lo[q];
+    } else {
+      double* ds[4] = {b->c64.cw, b->c64.ce, b->c64.cs, b->c64.cn};
+      SG_CUDA(cudaMemcpyAsync(c[k].data(), ds[k] + I.base, rows * 8, cudaMemcpyDeviceToHost, b->stream));
+    }
+  }
+  SG_CUDA(cudaStreamSynchronize(b->stream));
+  const int nx = I.nx, ny = I.ny, P = I.pitch;
+  const size_t N = (size_t)nx * ny;
+  auto Dof = [&](int i, int j) { return 1.0 / invD[(size_t)j * P + i]; };
+  for (int j = 0; j < ny; ++j)
+    for (int i = 0; i < nx; ++i) {
+      const size_t K = (size_t)j * nx + i, q = (size_t)j * P + i;
+      M5[K] = Dof(i, j);
+      M5[N + K] = i > 0 ? -c[0][q] * Dof(i - 1, j) : 0.0;
+      M5[2 * N + K] = i < nx - 1 ? -c[1][q] * Dof(i + 1, j) : 0.0;
+      M5[3 * N + K] = j > 0 ? -c[2][q] * Dof(i, j - 1) : 0.0;
+      M5[4 * N + K] = j < ny - 1 ? -c[3][q] * Dof(i, j + 1) : 0.0;
+      R[K] = Rr[q];
+    }
+  return SAYRAM_OK;
+}
+
+size_t sayram_batch_device_bytes(sayram_batch b) { return b ? b->bytes : 0; }
+void* sayram_batch_stream(sayram_batch b) { return b ? (void*)b->stream : nullptr; }
+
+int sayram_batch_enable_timing(sayram_batch b, int enable) {
+  if (!b) return fail(SAYRAM_ERR_ARG, "null handle");
+  b->timing = enable != 0;
+  for (auto& t : b->tms) t = 0.0;
+  for (auto& c : b->tcount) c = 0;
+  return SAYRAM_OK;
+}
+
+int sayram_batch_kernel_times(sayram_batch b, const char** names, double* total_ms, long long* launches, int cap) {
+  if (!b) return fail(SAYRAM_ERR_ARG, "null handle");
+  const int m = (int)b->tnames.size();
+  for (int k = 0; k < m && k < cap; ++k) {
+    if (names) names[k] = b->tnames[k].c_str();
+    if (total_ms) total_ms[k] = b->tms[k];
+    if (launches) launches[k] = b->tcount[k];
+  }
+  return m;
+}
+
+long long sayram_batch_launches(sayram_batch b) {
+  if (!b) return -1;
+  if (cudaSetDevice(b->dev) != cudaSuccess) return -1;
+  Ctl c;
+  if (cudaMemcpyAsync(&c, b->d_ctl, sizeof(c), cudaMemcpyDeviceToHost, b->stream) != cudaSuccess) return -1;
+  if (cudaStreamSynchronize(b->stream) != cudaSuccess) return -1;
+  return (long long)c.launches;
+}
+
+void sayram_batch_destroy(sayram_batch b) { delete b; }
+
+size_t sayram_instance_bytes(int nx, int ny, int precision) {
+  const long long pitch = round_up(nx, 4);
+  const long long cells = round_up((long long)(ny + 2) * pitch, 32);
+  const long long per = 14 * 8 + (precision == SAYRAM_FP32_REFINE ? 8 * 4 + 8 * 4 : 4 * 8 + 8 * 8) + 8;
+  return (size_t)(cells * per + 4096);
+}
+
+// ---- single instance (class Solver drop-in)
+int sayram_create(const sayram_problem* p, const sayram_options* opt, sayram_solver* out) {
+  return sayram_batch_create(p, 1, opt, out);
+}
+int sayram_update(sayram_solver s) { return sayram_batch_step(s, 1); }
+int sayram_step(sayram_solver s, int nsteps) { return sayram_batch_step(s, nsteps); }
+double sayram_t(sayram_solver s) {
+  sayram_stats st;
+  if (!s || sayram_batch_stats(s, 0, &st) != SAYRAM_OK) return 0.0;
+  return st.t;
+}
+int sayram_get_f(sayram_solver s, double* f_out) { return sayram_batch_get_f(s, 0, f_out); }
+int sayram_set_f(sayram_solver s, const double* f) { return sayram_batch_set_f(s, 0, f); }
+int sayram_set_dirichlet(sayram_solver s, int side, const double* v, int n) {
+  return sayram_batch_set_dirichlet(s, 0, side, v, n);
+}
+int sayram_set_coeffs(sayram_solver s, const double* G, const double* Dxx, const double* Dxy,
+                      const double* Dyy, const double* inv_tau) {
+  return sayram_batch_set_coeffs(s, 0, G, Dxx, Dxy, Dyy, inv_tau);
+}
+int sayram_get_stats(sayram_solver s, sayram_stats* out) { return sayram_batch_stats(s, 0, out); }
+void sayram_destroy(sayram_solver s) { sayram_batch_destroy(s); }
+
+}  // extern "C"

@@ -1,0 +1,744 @@
+// sayram_ops.cuh -- the kernels of one backward-Euler step (see sayram_kernels.cuh for layout).
+//
+//   k_setup      once per instance: coefficients -> per-cell face factors, UKK, loss diagonal
+//   k_begin      per step: resets the per-instance solver state
+//   k_assemble   fused vertex interpolation + PPFV face fluxes + diagonal/RHS + Jacobi scaling
+//   k_resid      FP64 true residual r = R - A~ y (adds the last Krylov correction first)
+//   k_bicg1/2/3  one BiCGSTAB iteration in T precision (FP64 or FP32) with fused SpMV + dots
+//   k_polish     positivity polish y' = R + (I - A~) y+, f = y'/D, min / clamp / mass checks
+//   k_field_*    alpha-major <-> padded system order copies for get_f / set_f
+#pragma once
+
+#include "sayram_kernels.cuh"
+
+namespace sg {
+
+// ------------------------------------------------------------------------------ arguments
+struct Geo {  // per-cell face factors (time independent while the coefficients are)
+  double *aAx, *aBx, *Sx, *aAy, *aBy, *Sy, *ukk, *sdiag;
+};
+
+struct Common {
+  const InstDev* inst;
+  InstState* st;
+  Ctl* ctl;
+  const int* chunk_inst;
+  int nchunks;
+  const int* tile_inst;
+  int ntiles;
+  int ninst;
+  const double* wx;    // per vertex column: (wL, wR) bilinear weights (Solver.cc:333-336)
+  const double* wy;    // per vertex row: (wB, wT)
+  const double* dirv;  // Dirichlet vertex values
+  double* part;        // 4 doubles per chunk
+};
+
+template <typename C>
+struct Coef {  // row-oriented scaled off-diagonal magnitudes (hi parts when split)
+  C *cw, *ce, *cs, *cn;
+  float *lw, *le, *ls, *ln;  // low parts for the FP32-split storage (null for FP64)
+};
+
+struct Fields {
+  double* f;       // state, padded system order
+  double* invD;    // 1 / diag(M)
+  double* R;       // right-hand side
+  double* colsum;  // 1^T M per column (conservation check)
+  double* y64[2];  // FP64 scaled solution y = D f (ping-pong)
+};
+
+template <typename T>
+struct Kry {
+  T *r, *rh, *t, *x;
+  T *p[2], *v[2];
+};
+
+// ------------------------------------------------------------------------------ setup
+// Face factors of cell (i,j) from the reference's general formula (Solver.cc:68-97) evaluated on
+// the XNEG and YNEG edges (Mesh.cc:80-151); the XPOS/YPOS edges of a rectangular cell give the
+// same pair. Uses non-contracting intrinsics so the values match the CPU evaluation.
+__device__ __forceinline__ void face_pair(double Kx, double Ky, double Ax, double Ay, double Bx,
+                                          double By, double n0, double n1, const double L[4],
+                                          double* aa, double* ab) {
+  const double ex = __dadd_rn(Bx, -Ax), ey = __dadd_rn(By, -Ay);
+  const double length = __dsqrt_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)));
+  const double vkb0 = __dadd_rn(Bx, -Kx), vkb1 = __dadd_rn(By, -Ky);
+  const double vka0 = __dadd_rn(Ax, -Kx), vka1 = __dadd_rn(Ay, -Ky);
+  const double rvkb0 = vkb1, rvkb1 = -vkb0, rvka0 = vka1, rvka1 = -vka0;
+  const double t0 = __dadd_rn(__dmul_rn(n0, L[0]), __dmul_rn(n1, L[2]));
+  const double t1 = __dadd_rn(__dmul_rn(n0, L[1]), __dmul_rn(n1, L[3]));
+  *aa = __ddiv_rn(__dmul_rn(length, __dadd_rn(__dmul_rn(t0, rvkb0), __dmul_rn(t1, rvkb1))),
+                  __dadd_rn(__dmul_rn(vka0, rvkb0), __dmul_rn(vka1, rvkb1)));
+  *ab = __ddiv_rn(__dmul_rn(length, __dadd_rn(__dmul_rn(t0, rvka0), __dmul_rn(t1, rvka1))),
+                  __dadd_rn(__dmul_rn(vkb0, rvka0), __dmul_rn(vkb1, rvka1)));
+}
+
+// One instance: stage holds alpha-major G, Dxx, Dxy, Dyy, inv_tau, f0 (each nx*ny; a NULL
+// section is skipped by passing has mask bits). Writes the face factors (and f if bit 5 set).
+__global__ void k_setup(Common cm, Geo geo, double* f, const double* stage, const double* xe,
+                        const double* ye, int b, int mask) {
+  const InstDev I = cm.inst[b];
+  const long long ncell = (long long)I.nx * I.ny;
+  const double* G = stage;
+  const double* Dxx = stage + ncell;
+  const double* Dxy = stage + 2 * ncell;
+  const double* Dyy = stage + 3 * ncell;
+  const double* itau = stage + 4 * ncell;
+  const double* f0 = stage + 5 * ncell;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < ncell;
+       c += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(c / I.ny), j = (int)(c % I.ny);
+    const long long K = I.base + (long long)j * I.pitch + i;
+    if (mask & 31) {
+      const double xl = xe[I.xe + i], xr = xe[I.xe + i + 1];
+      const double yb = ye[I.ye + j], yt = ye[I.ye + j + 1];
+      const double dx = __dadd_rn(xr, -xl), dy = __dadd_rn(yt, -yb);
+      const double Kx = __dmul_rn(0.5, __dadd_rn(xl, xr)), Ky = __dmul_rn(0.5, __dadd_rn(yb, yt));
+      const double g = G[c];
+      const double L[4] = {__dmul_rn(Dxx[c], g), __dmul_rn(Dxy[c], g), __dmul_rn(Dxy[c], g),
+                           __dmul_rn(Dyy[c], g)};
+      double aa, ab;
+      face_pair(Kx, Ky, xl, yt, xl, yb, -1.0, 0.0, L, &aa, &ab);  // XNEG: A=(i,j+1) B=(i,j)
+      geo.aAx[K] = aa;
+      geo.aBx[K] = ab;
+      geo.Sx[K] = __dadd_rn(aa, ab);
+      face_pair(Kx, Ky, xl, yb, xr, yb, 0.0, -1.0, L, &aa, &ab);  // YNEG: A=(i,j) B=(i+1,j)
+      geo.aAy[K] = aa;
+      geo.aBy[K] = ab;
+      geo.Sy[K] = __dadd_rn(aa, ab);
+      // UKK = G * (dx*dy/dt); diagonal UKK*(1 + dt/tau) (Solver.cc:190-199, Mesh.h:61-63)
+      const double ukk = __dmul_rn(g, __ddiv_rn(__dmul_rn(dx, dy), I.dt));
+      geo.ukk[K] = ukk;
+      geo.sdiag[K] = __dmul_rn(ukk, __dadd_rn(1.0, __dmul_rn(I.dt, itau[c])));
+    }
+    if (mask & 32) f[K] = f0[c];
+  }
+}
+
+// alpha-major (packed at hoff) -> padded system order, for every enabled instance (tile grid)
+__global__ void k_field_in(Common cm, double* dst, const double* src) {
+  count_launch(cm.ctl);
+  for (int t = blockIdx.x; t < cm.ntiles; t += gridDim.x) {
+    const int b = cm.tile_inst[t];
+    const InstDev I = cm.inst[b];
+    if (!I.enabled) continue;
+    const int lt = t - I.tile0, i0 = (lt % I.ntx) * kTX, j0 = (lt / I.ntx) * kTY;
+    for (int q = threadIdx.x; q < kTX * kTY; q += blockDim.x) {
+      const int i = i0 + (q / kTY), j = j0 + (q % kTY);  // j fastest: reads contiguous in j
+      if (i < I.nx && j < I.ny) dst[I.base + (long long)j * I.pitch + i] = src[I.hoff + (long long)i * I.ny + j];
+    }
+  }
+}
+
+__global__ void k_field_out(Common cm, double* dst, const double* src) {
+  count_launch(cm.ctl);
+  for (int t = blockIdx.x; t < cm.ntiles; t += gridDim.x) {
+    const int b = cm.tile_inst[t];
+    const InstDev I = cm.inst[b];
+    if (!I.enabled) continue;
+    const int lt = t - I.tile0, i0 = (lt % I.ntx) * kTX, j0 = (lt / I.ntx) * kTY;
+    for (int q = threadIdx.x; q < kTX * kTY; q += blockDim.x) {
+      const int i = i0 + (q / kTY), j = j0 + (q % kTY);
+      if (i < I.nx && j < I.ny) dst[I.hoff + (long long)i * I.ny + j] = src[I.base + (long long)j * I.pitch + i];
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------ step control
+__global__ void k_begin(Common cm) {
+  count_launch(cm.ctl);
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < cm.ninst; b += gridDim.x * blockDim.x) {
+    InstState& s = cm.st[b];
+    const bool on = cm.inst[b].enabled != 0;
+    s.outer_active = on ? 1 : 0;
+    s.inner_active = 0;
+    s.restart = 0;
+    s.fresh = 0;
+    s.has_x = 0;
+    s.iters = 0;
+    s.iters_total = 0;
+    s.refines = 0;
+    s.clamped = 0;
+    if (on) atomicAdd(&cm.ctl->n_outer, 1);
+  }
+}
+
+// ------------------------------------------------------------------------------ assembly
+template <typename C>
+struct AsmOut;
+template <>
+struct AsmOut<double> {
+  __device__ static void put(const Coef<double>& c, int which, long long idx, double v) {
+    double* a = which == 0 ? c.cw : which == 1 ? c.ce : which == 2 ? c.cs : c.cn;
+    a[idx] = v;
+  }
+};
+template <>
+struct AsmOut<float> {
+  __device__ static void put(const Coef<float>& c, int which, long long idx, double v) {
+    const float hi = __double2float_rn(v);
+    const float lo = __double2float_rn(v - (double)hi);
+    float* a = which == 0 ? c.cw : which == 1 ? c.ce : which == 2 ? c.cs : c.cn;
+    float* l = which == 0 ? c.lw : which == 1 ? c.le : which == 2 ? c.ls : c.ln;
+    a[idx] = hi;
+    l[idx] = lo;
+  }
+};
+
+// Inner face (Solver.cc:99-141, calculate_mu Solver.h:63-67). K and L one-sided data:
+// a_sigma = aA*fA + aB*fB, S = aA + aB, inv = 1/(f + eps).
+__device__ __forceinline__ void inner_face(double aK, double SK, double invK, double aL, double SL,
+                                           double invL, double* AK, double* AL) {
+  const double absK = fabs(aK), absL = fabs(aL);
+  const double denom = absK + absL + 2 * kEps;
+  const double muK = (absL + kEps) / denom;
+  const double muL = 1 - muK;
+  const double B = muL * aL - muK * aK;
+  const double Bp = fmax(B, 0.0);   // (|B| + B) / 2
+  const double Bm = fmax(-B, 0.0);  // (|B| - B) / 2
+  *AK = muK * SK + Bp * invK;
+  *AL = muL * SL + Bm * invL;
+}
+
+// Dirichlet face (Solver.cc:143-164): B = -a_sigma; A = S + B+/(f+eps); R += B-.
+__device__ __forceinline__ void dirichlet_face(double aK, double SK, double invK, double* A, double* Bm) {
+  *A = SK + fmax(-aK, 0.0) * invK;
+  *Bm = fmax(aK, 0.0);
+}
+
+// One tile of kTX x kTY cells per iteration; vertices and faces are computed once per tile
+// (plus a one-cell halo), in shared memory.
+template <typename C>
+__global__ void __launch_bounds__(kAsmThreads) k_assemble(Common cm, Geo geo, Fields fl, Coef<C> co) {
+  count_launch(cm.ctl);
+  constexpr int HX = kTX + 2, HY = kTY + 2, VX = kTX + 1, VY = kTY + 1;
+  __shared__ double fS[HY][HX];
+  __shared__ double iS[HY][HX];
+  __shared__ double vS[VY][VX];
+  __shared__ double xL[kTY][VX], xR[kTY][VX], xB[kTY][VX];  // x-faces: left/right outflow, R part
+  __shared__ double yB[VY][kTX], yT[VY][kTX], yR[VY][kTX];  // y-faces: below/above outflow, R part
+  for (int t = blockIdx.x; t < cm.ntiles; t += gridDim.x) {
+    const int b = cm.tile_inst[t];
+    const InstDev I = cm.inst[b];
+    if (!I.enabled) continue;  // uniform in the block
+    const int lt = t - I.tile0;
+    const int i0 = (lt % I.ntx) * kTX, j0 = (lt / I.ntx) * kTY;
+    const int nx = I.nx, ny = I.ny, P = I.pitch;
+    const long long base = I.base;
+    // 1) f and 1/(f+eps) on the tile plus a one-cell halo
+    for (int q = threadIdx.x; q < HX * HY; q += blockDim.x) {
+      const int hx = q % HX, hy = q / HX;
+      const int i = i0 + hx - 1, j = j0 + hy - 1;
+      double fv = 0.0, iv = 0.0;
+      if (i >= 0 && i < nx && j >= 0 && j < ny) {
+        fv = fl.f[base + (long long)j * P + i];
+        iv = 1.0 / (fv + kEps);
+      }
+      fS[hy][hx] = fv;
+      iS[hy][hx] = iv;
+    }
+    __syncthreads();
+    // 2) vertex values (Solver.cc:299-422): corners copy, interior bilinear, boundary edges
+    //    linear, then Dirichlet overrides with XMIN < XMAX < YMIN < YMAX precedence.
+    for (int q = threadIdx.x; q < VX * VY; q += blockDim.x) {
+      const int vx = q % VX, vy = q / VX;
+      const int Iv = i0 + vx, Jv = j0 + vy;
+      if (Iv > nx || Jv > ny) continue;
+      double val;
+      if (Jv == ny && I.bc[YMAX] == DIRICHLET) val = cm.dirv[I.dir[YMAX] + Iv];
+      else if (Jv == 0 && I.bc[YMIN] == DIRICHLET) val = cm.dirv[I.dir[YMIN] + Iv];
+      else if (Iv == nx && I.bc[XMAX] == DIRICHLET) val = cm.dirv[I.dir[XMAX] + Jv];
+      else if (Iv == 0 && I.bc[XMIN] == DIRICHLET) val = cm.dirv[I.dir[XMIN] + Jv];
+      else {
+        // cells around vertex (Iv, Jv) are (Iv-1|Iv, Jv-1|Jv); clamp to the domain at edges
+        const int ci0 = Iv > 0 ? Iv - 1 : 0, ci1 = Iv < nx ? Iv : nx - 1;
+        const int cj0 = Jv > 0 ? Jv - 1 : 0, cj1 = Jv < ny ? Jv : ny - 1;
+        const double f00 = fS[cj0 - j0 + 1][ci0 - i0 + 1], f10 = fS[cj0 - j0 + 1][ci1 - i0 + 1];
+        const double f01 = fS[cj1 - j0 + 1][ci0 - i0 + 1], f11 = fS[cj1 - j0 + 1][ci1 - i0 + 1];
+        const bool xin = Iv > 0 && Iv < nx, yin = Jv > 0 && Jv < ny;
+        if (xin && yin) {
+          const double wL = cm.wx[2 * (I.xe + Iv)], wR = cm.wx[2 * (I.xe + Iv) + 1];
+          const double wB = cm.wy[2 * (I.ye + Jv)], wT = cm.wy[2 * (I.ye + Jv) + 1];
+          val = wB * (wL * f00 + wR * f10) + wT * (wL * f01 + wR * f11);
+        } else if (yin) {  // vertical boundary edge: linear in y
+          const double wB = cm.wy[2 * (I.ye + Jv)], wT = cm.wy[2 * (I.ye + Jv) + 1];
+          val = wB * f00 + wT * f01;
+        } else if (xin) {  // horizontal boundary edge: linear in x
+          const double wL = cm.wx[2 * (I.xe + Iv)], wR = cm.wx[2 * (I.xe + Iv) + 1];
+          val = wL * f00 + wR * f10;
+        } else {
+          val = f00;  // corner: the single adjacent cell
+        }
+      }
+      vS[vy][vx] = val;
+    }
+    __syncthreads();
+    // 3a) x-faces (vertex column Iv between cells Iv-1 and Iv)
+    for (int q = threadIdx.x; q < kTY * VX; q += blockDim.x) {
+      const int vx = q % VX, ry = q / VX;
+      const int Iv = i0 + vx, j = j0 + ry;
+      double aL = 0.0, aR = 0.0, bm = 0.0;
+      if (j < ny && Iv <= nx) {
+        const double vLo = vS[ry][vx], vHi = vS[ry + 1][vx];  // vertices (Iv, j), (Iv, j+1)
+        if (Iv > 0 && Iv < nx) {
+          const long long K = base + (long long)j * P + Iv, L = K - 1;
+          // K's XNEG edge: A=(Iv, j+1), B=(Iv, j); L's XPOS edge: A=(Iv, j), B=(Iv, j+1)
+          const double aK = geo.aAx[K] * vHi + geo.aBx[K] * vLo;
+          const double aLs = geo.aAx[L] * vLo + geo.aBx[L] * vHi;
+          inner_face(aK, geo.Sx[K], iS[ry + 1][vx + 1], aLs, geo.Sx[L], iS[ry + 1][vx], &aR, &aL);
+        } else if (Iv == 0 && I.bc[XMIN] == DIRICHLET) {
+          const long long K = base + (long long)j * P;
+          dirichlet_face(geo.aAx[K] * vHi + geo.aBx[K] * vLo, geo.Sx[K], iS[ry + 1][vx + 1], &aR, &bm);
+        } else if (Iv == nx && I.bc[XMAX] == DIRICHLET) {
+          const long long K = base + (long long)j * P + nx - 1;  // XPOS edge: A=(nx, j), B=(nx, j+1)
+          dirichlet_face(geo.aAx[K] * vLo + geo.aBx[K] * vHi, geo.Sx[K], iS[ry + 1][vx], &aL, &bm);
+        }
+      }
+      xL[ry][vx] = aL;
+      xR[ry][vx] = aR;
+      xB[ry][vx] = bm;
+    }
+    // 3b) y-faces (vertex row Jv between cells Jv-1 and Jv)
+    for (int q = threadIdx.x; q < VY * kTX; q += blockDim.x) {
+      const int cx = q % kTX, vy = q / kTX;
+      const int i = i0 + cx, Jv = j0 + vy;
+      double aB = 0.0, aT = 0.0, bm = 0.0;
+      if (i < nx && Jv <= ny) {
+        const double vLe = vS[vy][cx], vRi = vS[vy][cx + 1];  // vertices (i, Jv), (i+1, Jv)
+        if (Jv > 0 && Jv < ny) {
+          const long long K = base + (long long)Jv * P + i, L = K - P;
+          // K's YNEG edge: A=(i, Jv), B=(i+1, Jv); L's YPOS edge: A=(i+1, Jv), B=(i, Jv)
+          const double aK = geo.aAy[K] * vLe + geo.aBy[K] * vRi;
+          const double aLs = geo.aAy[L] * vRi + geo.aBy[L] * vLe;
+          inner_face(aK, geo.Sy[K], iS[vy + 1][cx + 1], aLs, geo.Sy[L], iS[vy][cx + 1], &aT, &aB);
+        } else if (Jv == 0 && I.bc[YMIN] == DIRICHLET) {
+          const long long K = base + i;
+          dirichlet_face(geo.aAy[K] * vLe + geo.aBy[K] * vRi, geo.Sy[K], iS[vy + 1][cx + 1], &aT, &bm);
+        } else if (Jv == ny && I.bc[YMAX] == DIRICHLET) {
+          const long long K = base + (long long)(ny - 1) * P + i;  // YPOS edge: A=(i+1,ny), B=(i,ny)
+          dirichlet_face(geo.aAy[K] * vRi + geo.aBy[K] * vLe, geo.Sy[K], iS[vy][cx + 1], &aB, &bm);
+        }
+      }
+      yB[vy][cx] = aB;
+      yT[vy][cx] = aT;
+      yR[vy][cx] = bm;
+    }
+    __syncthreads();
+    // 4) per cell: diagonal in the reference's triplet order, RHS, scaling, scatter
+    for (int q = threadIdx.x; q < kTX * kTY; q += blockDim.x) {
+      const int cx = q % kTX, cy = q / kTX;
+      const int i = i0 + cx, j = j0 + cy;
+      if (i >= nx || j >= ny) continue;
+      const long long K = base + (long long)j * P + i;
+      const double Aw = xR[cy][cx], Ae = xL[cy][cx + 1], As = yT[cy][cx], An = yB[cy + 1][cx];
+      const bool wIn = i > 0, eIn = i < nx - 1, sIn = j > 0, nIn = j < ny - 1;
+      double D = 0.0, Rv = 0.0, dir = 0.0;
+      if (wIn) D += Aw;
+      if (eIn) D += Ae;
+      if (sIn) D += As;
+      if (nIn) D += An;
+      if (!wIn && I.bc[XMIN] == DIRICHLET) { D += Aw; dir += Aw; Rv += xB[cy][cx]; }
+      if (!eIn && I.bc[XMAX] == DIRICHLET) { D += Ae; dir += Ae; Rv += xB[cy][cx + 1]; }
+      if (!sIn && I.bc[YMIN] == DIRICHLET) { D += As; dir += As; Rv += yR[cy][cx]; }
+      if (!nIn && I.bc[YMAX] == DIRICHLET) { D += An; dir += An; Rv += yR[cy + 1][cx]; }
+      const double sd = geo.sdiag[K];
+      D += sd;
+      const double fK = fS[cy + 1][cx + 1];
+      Rv += geo.ukk[K] * fK;
+      const double inv = 1.0 / D;
+      fl.invD[K] = inv;
+      fl.R[K] = Rv;
+      fl.colsum[K] = sd + dir;
+      fl.y64[cm.st[b].ycur][K] = D * fK;
+      if (wIn) AsmOut<C>::put(co, 1, K - 1, Aw * inv);  // row K-1, east entry
+      if (eIn) AsmOut<C>::put(co, 0, K + 1, Ae * inv);  // row K+1, west entry
+      if (sIn) AsmOut<C>::put(co, 3, K - P, As * inv);  // row K-P, north entry
+      if (nIn) AsmOut<C>::put(co, 2, K + P, An * inv);  // row K+P, south entry
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------------------ streaming helpers
+// Locates chunk c: instance b and the first cell index K0 of this thread's 4-cell group.
+struct Slot {
+  int b;
+  long long K;
+  bool valid;
+};
+__device__ __forceinline__ Slot slot_of(const Common& cm, int c, const InstDev& I) {
+  Slot s;
+  s.b = cm.chunk_inst[c];
+  s.K = I.base + (long long)(c - I.chunk0) * kChunk + 4 * threadIdx.x;
+  s.valid = s.K < I.base + (long long)I.ny * I.pitch;
+  return s;
+}
+
+// FP64 coefficient of row entry from the (hi, lo) split or the FP64 array
+template <typename C>
+struct Coef64;
+template <>
+struct Coef64<double> {
+  __device__ static Q4<double> row(const Coef<double>& c, int which, long long K) {
+    const double* a = which == 0 ? c.cw : which == 1 ? c.ce : which == 2 ? c.cs : c.cn;
+    return ld4(a + K);
+  }
+};
+template <>
+struct Coef64<float> {
+  __device__ static Q4<double> row(const Coef<float>& c, int which, long long K) {
+    const float* a = which == 0 ? c.cw : which == 1 ? c.ce : which == 2 ? c.cs : c.cn;
+    const float* l = which == 0 ? c.lw : which == 1 ? c.le : which == 2 ? c.ls : c.ln;
+    const Q4<float> h = ld4(a + K), lo = ld4(l + K);
+    Q4<double> o;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) o.a[k] = (double)h.a[k] + (double)lo.a[k];
+    return o;
+  }
+};
+
+// y = A~ x for a 4-cell group given the centre values, the west value of cell 0, the east value
+// of cell 3 and the rows below/above.
+template <typename T, typename CT>
+__device__ __forceinline__ Q4<T> stencil(const Q4<T>& c, T w0, T e3, const Q4<T>& dn, const Q4<T>& up,
+                                         const Q4<CT>& cw, const Q4<CT>& ce, const Q4<CT>& cs,
+                                         const Q4<CT>& cn) {
+  Q4<T> o;
+  const T wv[4] = {w0, c.a[0], c.a[1], c.a[2]};
+  const T ev[4] = {c.a[1], c.a[2], c.a[3], e3};
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    o.a[k] = c.a[k] - ((T)cw.a[k] * wv[k] + (T)ce.a[k] * ev[k] + (T)cs.a[k] * dn.a[k] + (T)cn.a[k] * up.a[k]);
+  return o;
+}
+
+// ------------------------------------------------------------------------------ FP64 residual
+// r = R - A~ (y + x) in FP64; writes y + x to the other y buffer and r (T precision).
+// Partials: ||r||^2, ||R||^2.
+template <typename T, typename C>
+__global__ void __launch_bounds__(kThreads) k_resid(Common cm, Fields fl, Coef<C> co, Kry<T> kr,
+                                                     double tol, double inner_tol, int max_refine) {
+  count_launch(cm.ctl);
+  for (int c = blockIdx.x; c < cm.nchunks; c += gridDim.x) {
+    const int b = cm.chunk_inst[c];
+    InstState& st = cm.st[b];
+    if (!st.outer_active) continue;
+    const InstDev I = cm.inst[b];
+    const Slot s = slot_of(cm, c, I);
+    const double* yin = fl.y64[st.ycur];
+    double* yout = fl.y64[st.ycur ^ 1];
+    const bool hx = st.has_x != 0;
+    double q[2] = {0.0, 0.0};
+    if (s.valid) {
+      const long long K = s.K, P = I.pitch;
+      auto Y4 = [&](long long k) {
+        Q4<double> y = ld4(yin + k);
+        if (hx) {
+          const Q4<T> x = ld4(kr.x + k);
+#pragma unroll
+          for (int m = 0; m < 4; ++m) y.a[m] += (double)x.a[m];
+        }
+        return y;
+      };
+      auto Y1 = [&](long long k) { return yin[k] + (hx ? (double)kr.x[k] : 0.0); };
+      const Q4<double> yc = Y4(K), yd = Y4(K - P), yu = Y4(K + P);
+      const double w0 = Y1(K - 1), e3 = Y1(K + 4);
+      const Q4<double> cw = Coef64<C>::row(co, 0, K), ce = Coef64<C>::row(co, 1, K);
+      const Q4<double> cs = Coef64<C>::row(co, 2, K), cn = Coef64<C>::row(co, 3, K);
+      const Q4<double> Ay = stencil<double, double>(yc, w0, e3, yd, yu, cw, ce, cs, cn);
+      const Q4<double> R = ld4(fl.R + K);
+      Q4<T> r;
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        const double rv = R.a[m] - Ay.a[m];
+        r.a[m] = (T)rv;
+        q[0] += rv * rv;
+        q[1] += R.a[m] * R.a[m];
+      }
+      st4(yout + K, yc);
+      st4(kr.r + K, r);
+    }
+    double tot[2], mine[2];
+    block_sum<2, double>(q, mine);
+    if (chunk_finish<2>(st, PH_RESID, I.chunk0, I.nchunks, c, cm.part, mine, tot) && threadIdx.x == 0) {
+      st.ycur ^= 1;
+      st.has_x = 0;
+      if (st.refines == 0) st.bb = tot[1];
+      st.refines += 1;
+      st.rr64 = tot[0];
+      st.rel = st.bb > 0 ? sqrt(tot[0] / st.bb) : 0.0;
+      if (!(st.rel > tol)) {
+        st.outer_active = 0;
+        st.status = ST_OK;
+        atomicSub(&cm.ctl->n_outer, 1);
+      } else if (st.refines >= max_refine) {
+        st.outer_active = 0;
+        st.status = ST_NOT_CONVERGED;
+        atomicSub(&cm.ctl->n_outer, 1);
+      } else {
+        st.inner_active = 1;
+        st.fresh = 1;
+        st.restart = 1;
+        st.iters = 0;
+        st.rr = tot[0];
+        const double a = inner_tol * inner_tol * tot[0], bnd = 0.0625 * tol * tol * st.bb;
+        st.rr_target = a > bnd ? a : bnd;
+        atomicAdd(&cm.ctl->n_inner, 1);
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------ BiCGSTAB
+// k1: p = r + beta (p_old - omega v_old)  (p = r on a restart, which also sets r^ = r);
+//     v = A~ p;  partial (r^, v).
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_bicg1(Common cm, Coef<T> co, Kry<T> kr) {
+  count_launch(cm.ctl);
+  for (int c = blockIdx.x; c < cm.nchunks; c += gridDim.x) {
+    const int b = cm.chunk_inst[c];
+    InstState& st = cm.st[b];
+    if (!st.inner_active) continue;
+    const InstDev I = cm.inst[b];
+    const Slot s = slot_of(cm, c, I);
+    const int pc = st.pcur;
+    const bool rs = st.restart != 0;
+    const T beta = (T)st.beta, omega = (T)st.omega;
+    const T* po = kr.p[pc];
+    const T* vo = kr.v[pc];
+    T* pn = kr.p[pc ^ 1];
+    T* vn = kr.v[pc ^ 1];
+    T q[1] = {(T)0};
+    if (s.valid) {
+      const long long K = s.K, P = I.pitch;
+      auto P4 = [&](long long k) {
+        Q4<T> r = ld4(kr.r + k);
+        if (!rs) {
+          const Q4<T> a = ld4(po + k), v = ld4(vo + k);
+#pragma unroll
+          for (int m = 0; m < 4; ++m) r.a[m] = r.a[m] + beta * (a.a[m] - omega * v.a[m]);
+        }
+        return r;
+      };
+      auto P1 = [&](long long k) { return rs ? kr.r[k] : kr.r[k] + beta * (po[k] - omega * vo[k]); };
+      const Q4<T> pcv = P4(K), pd = P4(K - P), pu = P4(K + P);
+      const T w0 = P1(K - 1), e3 = P1(K + 4);
+      const Q4<T> v = stencil<T, T>(pcv, w0, e3, pd, pu, ld4(co.cw + K), ld4(co.ce + K),
+                                    ld4(co.cs + K), ld4(co.cn + K));
+      st4(pn + K, pcv);
+      st4(vn + K, v);
+      Q4<T> rh;
+      if (rs) {
+        rh = ld4(kr.r + K);
+        st4(kr.rh + K, rh);
+      } else {
+        rh = ld4(kr.rh + K);
+      }
+#pragma unroll
+      for (int m = 0; m < 4; ++m) q[0] += rh.a[m] * v.a[m];
+    }
+    double tot[1], mine[1];
+    block_sum<1, T>(q, mine);
+    if (chunk_finish<1>(st, PH_K1, I.chunk0, I.nchunks, c, cm.part, mine, tot) && threadIdx.x == 0) {
+      if (st.restart) {
+        st.rho = st.rr;  // (r^, r) with r^ = r
+        st.restart = 0;
+      }
+      st.pcur ^= 1;
+      const double den = tot[0];
+      if (den != 0.0 && isfinite(den) && st.rho != 0.0) {
+        st.alpha = st.rho / den;
+      } else {
+        st.alpha = 0.0;  // breakdown: this iteration degenerates to a minimal-residual step
+        st.restart = 1;
+      }
+    }
+  }
+}
+
+// k2: s = r - alpha v;  t = A~ s;  partials (t, s), (t, t).
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_bicg2(Common cm, Coef<T> co, Kry<T> kr) {
+  count_launch(cm.ctl);
+  for (int c = blockIdx.x; c < cm.nchunks; c += gridDim.x) {
+    const int b = cm.chunk_inst[c];
+    InstState& st = cm.st[b];
+    if (!st.inner_active) continue;
+    const InstDev I = cm.inst[b];
+    const Slot s = slot_of(cm, c, I);
+    const T alpha = (T)st.alpha;
+    const T* vv = kr.v[st.pcur];
+    T q[2] = {(T)0, (T)0};
+    if (s.valid) {
+      const long long K = s.K, P = I.pitch;
+      auto S4 = [&](long long k) {
+        Q4<T> r = ld4(kr.r + k);
+        const Q4<T> v = ld4(vv + k);
+#pragma unroll
+        for (int m = 0; m < 4; ++m) r.a[m] -= alpha * v.a[m];
+        return r;
+      };
+      auto S1 = [&](long long k) { return kr.r[k] - alpha * vv[k]; };
+      const Q4<T> sc = S4(K), sd = S4(K - P), su = S4(K + P);
+      const T w0 = S1(K - 1), e3 = S1(K + 4);
+      const Q4<T> t = stencil<T, T>(sc, w0, e3, sd, su, ld4(co.cw + K), ld4(co.ce + K),
+                                    ld4(co.cs + K), ld4(co.cn + K));
+      st4(kr.t + K, t);
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        q[0] += t.a[m] * sc.a[m];
+        q[1] += t.a[m] * t.a[m];
+      }
+    }
+    double tot[2], mine[2];
+    block_sum<2, T>(q, mine);
+    if (chunk_finish<2>(st, PH_K2, I.chunk0, I.nchunks, c, cm.part, mine, tot) && threadIdx.x == 0) {
+      if (tot[1] > 0.0 && isfinite(tot[0])) {
+        st.omega = tot[0] / tot[1];
+      } else {
+        st.omega = 0.0;
+      }
+      if (st.omega == 0.0) st.restart = 1;
+    }
+  }
+}
+
+// k3: x += alpha p + omega s (x starts at 0 on the first iteration of a solve);
+//     r = s - omega t;  partials (r^, r), (r, r); convergence test.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_bicg3(Common cm, Kry<T> kr, int max_iters) {
+  count_launch(cm.ctl);
+  for (int c = blockIdx.x; c < cm.nchunks; c += gridDim.x) {
+    const int b = cm.chunk_inst[c];
+    InstState& st = cm.st[b];
+    if (!st.inner_active) continue;
+    const InstDev I = cm.inst[b];
+    const Slot s = slot_of(cm, c, I);
+    const T alpha = (T)st.alpha, omega = (T)st.omega;
+    const bool fresh = st.fresh != 0;
+    const T* pp = kr.p[st.pcur];
+    const T* vv = kr.v[st.pcur];
+    T q[2] = {(T)0, (T)0};
+    if (s.valid) {
+      const long long K = s.K;
+      const Q4<T> r = ld4(kr.r + K), v = ld4(vv + K), p = ld4(pp + K), t = ld4(kr.t + K);
+      const Q4<T> rh = ld4(kr.rh + K);
+      Q4<T> x = fresh ? Q4<T>{{(T)0, (T)0, (T)0, (T)0}} : ld4(kr.x + K);
+      Q4<T> rn;
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        const T sv = r.a[m] - alpha * v.a[m];
+        x.a[m] += alpha * p.a[m] + omega * sv;
+        rn.a[m] = sv - omega * t.a[m];
+        q[0] += rh.a[m] * rn.a[m];
+        q[1] += rn.a[m] * rn.a[m];
+      }
+      st4(kr.x + K, x);
+      st4(kr.r + K, rn);
+    }
+    double tot[2], mine[2];
+    block_sum<2, T>(q, mine);
+    if (chunk_finish<2>(st, PH_K3, I.chunk0, I.nchunks, c, cm.part, mine, tot) && threadIdx.x == 0) {
+      st.fresh = 0;
+      st.has_x = 1;
+      st.iters += 1;
+      st.iters_total += 1;
+      const double rhoN = tot[0];
+      st.rr = tot[1];
+      if (!(tot[1] > st.rr_target) || st.iters >= max_iters || !isfinite(tot[1])) {
+        st.inner_active = 0;
+        atomicSub(&cm.ctl->n_inner, 1);
+      } else {
+        const double beta = (rhoN / st.rho) * (st.alpha / st.omega);
+        st.rho = rhoN;
+        if (!isfinite(beta) || rhoN == 0.0) {
+          st.restart = 1;
+          st.beta = 0.0;
+        } else {
+          st.beta = beta;
+        }
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------ polish + checks
+// y' = R + (I - A~) max(y, 0) >= 0 (R >= 0, fractions >= 0), f = y' / D; partials: sum colsum*f,
+// sum R, clamped count, and -min f (as a max via the sum slot of a separate reduction).
+template <typename C>
+__global__ void __launch_bounds__(kThreads) k_polish(Common cm, Fields fl, Coef<C> co) {
+  count_launch(cm.ctl);
+  __shared__ double smin[kThreads / 32];
+  for (int c = blockIdx.x; c < cm.nchunks; c += gridDim.x) {
+    const int b = cm.chunk_inst[c];
+    InstState& st = cm.st[b];
+    const InstDev I = cm.inst[b];
+    if (!I.enabled) continue;
+    const Slot s = slot_of(cm, c, I);
+    const double* y = fl.y64[st.ycur];
+    double q[3] = {0.0, 0.0, 0.0};
+    double mn = 1.0e300;
+    if (s.valid) {
+      const long long K = s.K, P = I.pitch;
+      auto Yp4 = [&](long long k) {
+        Q4<double> v = ld4(y + k);
+#pragma unroll
+        for (int m = 0; m < 4; ++m) v.a[m] = fmax(v.a[m], 0.0);
+        return v;
+      };
+      const Q4<double> yc = ld4(y + K);
+      Q4<double> ycp;
+#pragma unroll
+      for (int m = 0; m < 4; ++m) ycp.a[m] = fmax(yc.a[m], 0.0);
+      const Q4<double> yd = Yp4(K - P), yu = Yp4(K + P);
+      const double w0 = fmax(y[K - 1], 0.0), e3 = fmax(y[K + 4], 0.0);
+      const Q4<double> cw = Coef64<C>::row(co, 0, K), ce = Coef64<C>::row(co, 1, K);
+      const Q4<double> cs = Coef64<C>::row(co, 2, K), cn = Coef64<C>::row(co, 3, K);
+      const Q4<double> R = ld4(fl.R + K), inv = ld4(fl.invD + K), cols = ld4(fl.colsum + K);
+      const double wv[4] = {w0, ycp.a[0], ycp.a[1], ycp.a[2]};
+      const double ev[4] = {ycp.a[1], ycp.a[2], ycp.a[3], e3};
+      Q4<double> fo;
+      const int row_i0 = (int)((K - I.base) % I.pitch);
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        const double yp = R.a[m] + (cw.a[m] * wv[m] + ce.a[m] * ev[m] + cs.a[m] * yd.a[m] + cn.a[m] * yu.a[m]);
+        const double fv = yp * inv.a[m];
+        fo.a[m] = fv;
+        q[0] += cols.a[m] * fv;
+        q[1] += R.a[m];
+        const bool real = row_i0 + m < I.nx;
+        if (real) {
+          q[2] += yc.a[m] < 0.0 ? 1.0 : 0.0;
+          mn = fmin(mn, fv);
+        }
+      }
+      st4(fl.f + K, fo);
+    }
+    // block min (separate from the sums)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    if ((threadIdx.x & 31) == 0) smin[threadIdx.x >> 5] = mn;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int w = 1; w < (int)(blockDim.x >> 5); ++w) mn = fmin(mn, smin[w]);
+      smin[0] = mn;
+    }
+    __syncthreads();
+    double tot[3], mine[3];
+    block_sum<3, double>(q, mine);
+    // the chunk's minimum travels in part slot 3 (read back below by the last block)
+    if (threadIdx.x == 0) cm.part[(size_t)c * 4 + 3] = smin[0];
+    if (chunk_finish<3>(st, PH_POLISH, I.chunk0, I.nchunks, c, cm.part, mine, tot) && threadIdx.x == 0) {
+      double gmin = 1.0e300;
+      for (int k = 0; k < I.nchunks; ++k) gmin = fmin(gmin, __ldcg(&cm.part[(size_t)(I.chunk0 + k) * 4 + 3]));
+      st.min_f = gmin;
+      st.clamped = (long long)tot[2];
+      st.mass_drift = tot[1] != 0.0 ? fabs(tot[0] - tot[1]) / fabs(tot[1]) : 0.0;
+      st.steps += 1;
+      if (!(gmin >= 0.0)) st.status = ST_NEGATIVE;
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace sg

@@ -1,0 +1,66 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import __graft_entry__  # noqa: E402
+
+__graft_entry__.load_package()
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built CUDA library")
+    config.addinivalue_line("markers", "slow: long-running")
+
+
+@pytest.fixture(scope="session")
+def oracle():
+    import oracle as orc  # the checker (tests only)
+
+    orc.build()
+    return orc
+
+
+@pytest.fixture(scope="session")
+def capi():
+    """The CUDA library binding; GPU tests fail loudly if it cannot be loaded."""
+    from sayram2d_gb300 import build, capi as c
+
+    build.build()
+    c.load()
+    return c
+
+
+def load_small():
+    """The reference-generated fixtures of the small cases: (npz, case names)."""
+    import numpy as np
+
+    z = np.load(os.path.join(GOLDEN, "ref_small.npz"))
+    names = sorted({k.split("/")[0] for k in z.files})
+    return z, names
+
+
+def problem_from(z, name):
+    """Rebuilds a cases.Problem from its stored inputs."""
+    from sayram2d_gb300 import cases
+
+    g = lambda k: z[f"{name}/{k}"]
+    meta = g("meta")
+    nx, ny, dt = int(meta[0]), int(meta[1]), float(meta[2])
+    bc = [int(v) for v in meta[3:7]]
+    dirs = [g(f"dir{s}") if bc[s] == cases.DIRICHLET else None for s in range(4)]
+    return cases.Problem(nx, ny, g("x_edges"), g("y_edges"), dt, bc, g("G"), g("Dxx"), g("Dxy"),
+                         g("Dyy"), g("inv_tau"), g("f0"), dirs, name=name)
+
+
+def c0_problem():
+    from sayram2d_gb300 import cases
+
+    rp = cases.read_ini(os.path.join(ROOT, "sayram-2d_gb300", "configs", "c0.ini"))
+    return rp, cases.problem_from_params(rp)

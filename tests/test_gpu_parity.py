@@ -1,0 +1,173 @@
+"""GPU parity: the CUDA path through the C-ABI against the reference-generated fixtures and the
+oracle. Tolerances: the plain FP64 drop-in must match the reference solution to a relative L2
+error <= 1e-10 and stay non-negative; the FP32+FP64-refinement path to <= 1e-8; the assembled
+matrix entry-wise to 1e-12 of its row scale (the GPU evaluates the same formulas with fused
+multiply-adds)."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, c0_problem, load_small, problem_from
+from sayram2d_gb300 import cases
+
+pytestmark = pytest.mark.gpu
+
+Z, NAMES = load_small()
+TOL64, TOL32 = 1e-10, 1e-8
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_assembly_matches_reference(capi, name):
+    p = problem_from(Z, name)
+    for prec in (capi.FP64, capi.FP32_REFINE):
+        s = capi.Solver(p, precision=prec)
+        M5, R = s.export_system(0)
+        s.close()
+        ref, Rref = Z[f"{name}/M5"], Z[f"{name}/R"]
+        scale = np.abs(ref).sum(axis=0)  # row scale
+        tol = 1e-12 if prec == capi.FP64 else 1e-12
+        assert (np.abs(M5 - ref) <= tol * scale[None, :]).all(), (name, prec, np.abs(M5 - ref).max())
+        assert np.allclose(R, Rref, rtol=1e-13, atol=1e-300), name
+
+
+@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("prec", [0, 1])
+def test_steps_match_reference(capi, name, prec):
+    p = problem_from(Z, name)
+    s = capi.Solver(p, precision=prec)
+    tol = TOL64 if prec == capi.FP64 else TOL32
+    s.update()
+    f1 = s.f()
+    assert rel(f1, Z[f"{name}/f1"]) <= tol, (name, rel(f1, Z[f"{name}/f1"]))
+    for _ in range(9):
+        s.update()
+    f10 = s.f()
+    st = s.get_stats()
+    s.close()
+    assert rel(f10, Z[f"{name}/f10"]) <= tol, (name, rel(f10, Z[f"{name}/f10"]), st)
+    assert f10.min() >= 0.0 and st["min_f"] >= 0.0
+    assert st["steps"] == 10 and abs(st["t"] - 10 * p.dt) < 1e-12
+    assert st["rel_residual"] <= (1e-12 if prec == capi.FP64 else 1e-10)
+    assert st["mass_drift"] <= 1e-8
+
+
+def test_config0_full_run_fp64(capi):
+    """Config 0: 90 x 90, dt = 1e-3, 1000 steps, against the reference's own result."""
+    z = np.load(os.path.join(GOLDEN, "ref_c0_90x90.npz"))
+    rp, p = c0_problem()
+    s = capi.Solver(p, precision=capi.FP64)
+    s.step(rp.nsteps)
+    f = s.f()
+    st = s.get_stats()
+    s.close()
+    assert rel(f, z[f"f{rp.nsteps}"]) <= TOL64, rel(f, z[f"f{rp.nsteps}"])
+    assert f.min() >= 0.0
+    assert st["steps"] == rp.nsteps
+
+
+def test_config0_full_run_mixed(capi):
+    z = np.load(os.path.join(GOLDEN, "ref_c0_90x90.npz"))
+    rp, p = c0_problem()
+    s = capi.Solver(p, precision=capi.FP32_REFINE)
+    s.step(rp.nsteps)
+    f = s.f()
+    s.close()
+    assert rel(f, z[f"f{rp.nsteps}"]) <= TOL32
+    assert f.min() >= 0.0
+
+
+def test_batch_equals_alone(capi):
+    """Each instance advanced inside an uneven batch equals the same instance advanced alone."""
+    probs = [problem_from(Z, n) for n in NAMES] + cases.batch_problems(6, seed=5, dt=1e-2, lo=40, hi=90)
+    for prec, tol in ((capi.FP64, 1e-12), (capi.FP32_REFINE, 1e-8)):
+        b = capi.Batch(probs, precision=prec)
+        b.step(5)
+        got = [b.f(k) for k in range(len(probs))]
+        b.close()
+        for k, p in enumerate(probs):
+            s = capi.Solver(p, precision=prec)
+            s.step(5)
+            alone = s.f()
+            s.close()
+            assert rel(got[k], alone) <= tol, (prec, k, rel(got[k], alone))
+
+
+def test_batch_vs_oracle(capi, oracle):
+    probs = cases.batch_problems(5, seed=11, dt=1e-2, lo=64, hi=100)
+    b = capi.Batch(probs, precision=capi.FP32_REFINE)
+    b.step(3)
+    for k, p in enumerate(probs):
+        ref = oracle.step(p, None, 3)
+        f = b.f(k)
+        assert rel(f, ref) <= TOL32 and f.min() >= 0.0
+        st = b.stats(k)
+        assert st["mass_drift"] <= 1e-8 and st["rel_residual"] <= 1e-10
+    b.close()
+
+
+def test_step_host_roundtrip(capi):
+    probs = cases.batch_problems(4, seed=2, dt=1e-2, lo=30, hi=70)
+    b = capi.Batch(probs, precision=capi.FP64)
+    fin = np.concatenate([p.f0.ravel() for p in probs])
+    fout = np.empty_like(fin)
+    b.step_host(2, fin.ctypes.data, fout.ctypes.data)
+    off = 0
+    for k, p in enumerate(probs):
+        n = p.nx * p.ny
+        assert np.array_equal(fout[off:off + n].reshape(p.nx, p.ny), b.f(k))
+        off += n
+    c = capi.Batch(probs, precision=capi.FP64)
+    c.step(2)
+    for k in range(len(probs)):
+        assert rel(b.f(k), c.f(k)) <= 1e-13
+    b.close()
+    c.close()
+
+
+def test_set_f_get_f_and_dirichlet(capi, oracle):
+    p = cases.synthetic_problem(20, 15, 1e-2, seed=3)
+    s = capi.Solver(p)
+    g = np.random.default_rng(0).uniform(0, 1, (20, 15))
+    s.set_f(g)
+    assert np.array_equal(s.f(), g)
+    newv = np.linspace(0.0, 0.5, 21)
+    s.set_dirichlet(cases.YMIN, newv)
+    p2 = cases.synthetic_problem(20, 15, 1e-2, seed=3)
+    p2.dirichlet[cases.YMIN] = newv
+    p2.f0 = g
+    s.update()
+    assert rel(s.f(), oracle.step(p2, g, 1)) <= TOL64
+    with pytest.raises(RuntimeError, match="not Dirichlet"):
+        s.set_dirichlet(cases.XMAX, np.zeros(16))
+    s.close()
+
+
+def test_not_converged_is_reported_not_hidden(capi):
+    """A forced non-convergence (one Krylov iteration, two residual checks) returns
+    NOT_CONVERGED but the state still advances and stays non-negative."""
+    p = cases.synthetic_problem(64, 64, 1e-2, seed=4)
+    s = capi.Solver(p, precision=capi.FP64, max_iters=1, max_refine=2)
+    rc = s.step(1, allow_not_converged=True)
+    assert rc == capi.ERR_NOT_CONVERGED
+    st = s.get_stats()
+    assert st["status"] == capi.ERR_NOT_CONVERGED and st["steps"] == 1
+    assert s.f().min() >= 0.0
+    s.close()
+
+
+def test_large_grid_properties(capi, oracle):
+    """512 x 512, dt = 1e-2: two steps against SuperLU, plus conservation and positivity."""
+    p = cases.synthetic_problem(512, 512, 1e-2, seed=5)
+    s = capi.Solver(p, precision=capi.FP64)
+    s.step(2)
+    f = s.f()
+    st = s.get_stats()
+    s.close()
+    ref = oracle.step(p, None, 2, solver="splu")
+    assert rel(f, ref) <= TOL64, rel(f, ref)
+    assert f.min() >= 0.0 and st["mass_drift"] <= 1e-9

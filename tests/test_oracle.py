@@ -1,0 +1,133 @@
+"""The oracle (CPU restatement of Sayram-2D's Solver.cc) against the reference's own outputs and
+against the structural facts of the PPFV matrix. CPU only."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, c0_problem, load_small, problem_from
+from sayram2d_gb300 import cases
+
+
+Z, NAMES = load_small()
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_assembly_bit_exact_vs_reference(oracle, name):
+    """M and R of the first assembly equal the reference Solver's M_ and R_ bit for bit."""
+    p = problem_from(Z, name)
+    M5, R = oracle.assemble(p, p.f0)
+    assert np.array_equal(M5, Z[f"{name}/M5"])
+    assert np.array_equal(R, Z[f"{name}/R"])
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_steps_vs_reference(oracle, name):
+    p = problem_from(Z, name)
+    for n in (1, 10):
+        f = oracle.step(p, None, n)
+        ref = Z[f"{name}/f{n}"]
+        assert np.allclose(f, ref, rtol=1e-14, atol=0), name
+        assert f.min() >= 0.0
+
+
+def test_config0_prefix_vs_reference(oracle):
+    z = np.load(os.path.join(GOLDEN, "ref_c0_90x90.npz"))
+    _, p = c0_problem()
+    f = oracle.step(p, None, 100)
+    err = np.linalg.norm(f - z["f100"]) / np.linalg.norm(z["f100"])
+    assert err <= 1e-13
+
+
+def test_ini_semantics(tmp_path):
+    """nsteps rounds down to a multiple of nplots and dt = T/nsteps (Parameters.cc:58-60)."""
+    ini = tmp_path / "p.ini"
+    ini.write_text("[basic]\nrun_id=x\nnalpha0=8\nnE=6\nalpha0min=5\nalpha0max=90\nEmin=0.2\nEmax=5\n"
+                   "T=1.0\nnsteps=1005\n[diagnostics]\nnplots=10\n")
+    rp = cases.read_ini(str(ini))
+    assert rp.nsteps == 1000 and rp.save_every_step == 100
+    assert rp.dt == 1.0 / 1000
+    rp0, _ = c0_problem()
+    assert (rp0.nalpha0, rp0.nE, rp0.nsteps) == (90, 90, 1000) and abs(rp0.dt - 1e-3) < 1e-18
+
+
+def test_face_coefficients_closed_form(oracle):
+    """a_sigma_A / a_sigma_B of the general formula (Solver.cc:68-97) reduce on a rectangle to
+    Lxx*dy/dx -/+ Lxy (x faces) and Lyy*dx/dy +/- Lxy (y faces)."""
+    rng = np.random.default_rng(0)
+    xe = np.cumsum(np.r_[0.1, rng.uniform(0.01, 0.2, 6)])
+    ye = np.cumsum(np.r_[-1.0, rng.uniform(0.05, 0.3, 5)])
+    p = cases.synthetic_problem(6, 5, 1e-2, seed=1, x_edges=xe, y_edges=ye)
+    f = p.f0
+    for (i, j) in [(0, 0), (2, 3), (5, 4), (3, 1)]:
+        dx, dy = xe[i + 1] - xe[i], ye[j + 1] - ye[j]
+        G = p.G[i, j]
+        Lxx, Lxy, Lyy = p.Dxx[i, j] * G, p.Dxy[i, j] * G, p.Dyy[i, j] * G
+        for inbr in range(4):
+            aa, ab, _ = oracle.face_coeffs(p, f, i, j, inbr)
+            if inbr in (0, 2):
+                ea, eb = Lxx * dy / dx - Lxy, Lxx * dy / dx + Lxy
+            else:
+                ea, eb = Lyy * dx / dy + Lxy, Lyy * dx / dy - Lxy
+            scale = abs(Lxx * dy / dx) + abs(Lyy * dx / dy) + abs(Lxy)
+            assert abs(aa - ea) <= 1e-13 * scale and abs(ab - eb) <= 1e-13 * scale
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_m_matrix_structure(oracle, name):
+    """diag > 0, off-diagonals <= 0, column sums = UKK(1+dt/tau) + Dirichlet face terms >= UKK."""
+    p = problem_from(Z, name)
+    M5, R = oracle.assemble(p, p.f0)
+    assert (M5[0] > 0).all()
+    assert (M5[1:] <= 0).all()
+    cs = oracle.column_sums(p.nx, p.ny, M5)
+    dx = np.diff(p.x_edges)[:, None]
+    dy = np.diff(p.y_edges)[None, :]
+    ukk = p.G * (dx * dy / p.dt)
+    s = oracle.field_to_sys(ukk * (1 + p.dt * p.inv_tau))
+    extra = cs - s
+    assert (extra >= -1e-12 * np.abs(M5[0])).all()
+    # cells away from Dirichlet boundaries: inner faces cancel column-wise
+    K = np.arange(p.nx * p.ny)
+    i, j = K % p.nx, K // p.nx
+    edge = np.zeros_like(K, dtype=bool)
+    if p.bc[0] == cases.DIRICHLET: edge |= i == 0
+    if p.bc[1] == cases.DIRICHLET: edge |= i == p.nx - 1
+    if p.bc[2] == cases.DIRICHLET: edge |= j == 0
+    if p.bc[3] == cases.DIRICHLET: edge |= j == p.ny - 1
+    assert np.allclose(extra[~edge], 0, atol=1e-12 * np.abs(M5[0]).max())
+    assert (R >= 0).all()
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_direct_solvers_agree_and_conserve(oracle, name):
+    p = problem_from(Z, name)
+    M5, R = oracle.assemble(p, p.f0)
+    xb = oracle.solve(p.nx, p.ny, M5, R, "banded")
+    xs = oracle.solve(p.nx, p.ny, M5, R, "splu")
+    assert np.linalg.norm(xb - xs) <= 1e-12 * np.linalg.norm(xs)
+    assert xb.min() >= 0
+    cs = oracle.column_sums(p.nx, p.ny, M5)
+    assert abs(cs @ xb - R.sum()) <= 1e-12 * R.sum()
+
+
+def test_problem_validation():
+    p = cases.synthetic_problem(5, 4, 1e-2, seed=0)
+    p.x_edges = p.x_edges[::-1].copy()
+    with pytest.raises(ValueError, match="strictly increasing"):
+        p.validate()
+    p = cases.synthetic_problem(5, 4, 1e-2, seed=0)
+    p.dirichlet[0] = None
+    with pytest.raises(ValueError, match="missing value"):
+        p.validate()
+
+
+def test_generators_deterministic():
+    a = cases.synthetic_problem(12, 9, 1e-2, seed=42)
+    b = cases.synthetic_problem(12, 9, 1e-2, seed=42)
+    for k in ("G", "Dxx", "Dxy", "Dyy", "f0"):
+        assert np.array_equal(getattr(a, k), getattr(b, k))
+    assert np.all(np.abs(a.Dxy) <= 0.9 * np.sqrt(a.Dxx * a.Dyy) * (1 + 1e-12))
+    assert a.Dxx.min() > 0 and a.Dxx.max() <= 1e-2
+    sizes = cases.batch_sizes(64, seed=3)
+    assert all(64 <= x <= 256 and 64 <= y <= 256 for x, y in sizes)
