@@ -1,0 +1,361 @@
+#!/usr/bin/env python3
+"""Benchmark of the Sayram-2D hot path on one GB300.
+
+Workload (the batched mixed-precision configuration the headline metric is quoted on): 4096
+independent instances, nalpha and nE each uniform in [64, 256], seeded synthetic D fields
+(rho ~ U[-0.9, 0.9], tau log-uniform in [0.1, 10] days), dt = 1e-2 day, advanced together with
+FP32 matrix/Krylov and FP64 residual/refinement to a relative residual of 1e-10.  One bench
+"step" is one backward-Euler step of every instance (assembly, solve, positivity polish).
+
+Prints ONE JSON line:
+  value        instance-steps/s, device-timed (CUDA events on the batch stream), inputs resident
+  e2e          the same metric through sayram_batch_step_host with pinned host buffers: every step
+               copies all instances' f host->device and the result device->host
+  roofline     the dominant kernel: algorithmic bytes / event-timed duration vs measured HBM peak
+  cpu_baseline the oracle port (C assembly restatement + SuperLU/COLAMD, the algorithm family of
+               the reference's Eigen SparseLU) on one host core, on a bounded sample
+  plain_fp64   the single-instance FP64 drop-in (sayram_create/sayram_update) on a sample of the
+               same batch, one instance after another
+and accuracy against FP64 (rel L2 per instance vs the batched FP64 path), min cell, mass drift.
+
+--impl reference times the oracle port on all host cores instead (the reference's own build needs
+Eigen/xtensor/HDF5, which are not available).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+import __graft_entry__  # noqa: E402
+
+__graft_entry__.load_package()
+from sayram2d_gb300 import cases  # noqa: E402
+
+METRIC = "instance-steps/s batched FP32+refine vs plain FP64 (rel err<=1e-8); p50/p99 ms"
+UNIT = "instance-steps/s"
+DT = 1e-2
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--instances", type=int, default=4096)
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--plain-sample", type=int, default=64)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--quick", action="store_true", help="skip the plain/FP64/e2e/CPU side measurements")
+    return ap.parse_args()
+
+
+def peak_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ----------------------------------------------------------------------------- clocks
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi while the timed region runs."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+                                          f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if parts[3 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+# ----------------------------------------------------------------------------- CPU baseline
+def _cpu_worker(p):
+    """One instance-step of the oracle port: assembly (C restatement) + SuperLU (COLAMD)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # checker / CPU baseline only
+
+    t0 = time.perf_counter()
+    M5, R = oracle.assemble(p, p.f0)
+    x = oracle.solve(p.nx, p.ny, M5, R, "splu")
+    return time.perf_counter() - t0, float(x.min())
+
+
+def cpu_baseline_single(seed, n, seconds):
+    """Bounded single-core sample: instances 0, 1, 2, ... for about `seconds` of CPU work."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # checker / CPU baseline only
+
+    oracle.build()
+    sizes = cases.batch_sizes(n, seed)
+    spent, done = 0.0, 0
+    while spent < seconds and done < n:
+        p = cases.batch_instance(done, seed, DT, sizes[done])
+        dt, _ = _cpu_worker(p)
+        spent += dt
+        done += 1
+    cells = sum(a * b for a, b in sizes[:done])
+    return {"value": done / spent, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"instances 0..{done - 1} of the batch ({cells} cells) x 1 step each, {spent:.1f} s: "
+                      "C restatement of Solver.cc assembly + SuperLU/COLAMD direct solve, one thread"}
+
+
+def run_reference(a):
+    """--impl reference: the oracle port on every host core, same config/metric."""
+    import multiprocessing as mp
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # checker / CPU baseline only
+
+    oracle.build()
+    cores = os.cpu_count() or 1
+    per_step = max(cores, 8)
+    sizes = cases.batch_sizes(a.instances, a.seed)
+    nsamples = max(a.warmup, 1) + a.steps
+    ks = [(s * per_step + i) % a.instances for s in range(nsamples) for i in range(per_step)]
+    probs = {k: cases.batch_instance(k, a.seed, DT, sizes[k]) for k in sorted(set(ks))}
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        def sample(s):
+            return pool.map(_cpu_worker, [probs[k] for k in ks[s * per_step:(s + 1) * per_step]])
+
+        for s in range(max(a.warmup, 1)):
+            sample(s)
+        t0 = time.perf_counter()
+        mins = []
+        for s in range(max(a.warmup, 1), nsamples):
+            mins += [m for _, m in sample(s)]
+        wall = time.perf_counter() - t0
+    v = per_step * a.steps / wall
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * wall / a.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)",
+            "config": {"workload": f"batched: {a.instances} instances, nalpha,nE~U[64,256], dt={DT} day; "
+                                   f"each bench step = {per_step} instance-steps sampled from the batch",
+                       "instances": a.instances, "seed": a.seed},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{per_step} instance-steps per bench step on {cores} processes: C "
+                                       "restatement of Solver.cc assembly + SuperLU/COLAMD (Eigen SparseLU "
+                                       "stand-in; the reference build needs Eigen/xtensor/HDF5)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "min_f": min(mins) if mins else None}
+    print(json.dumps(line))
+
+
+# ----------------------------------------------------------------------------- our arm
+# Algorithmic bytes per real cell per launch (FP32+refine path): reads + writes of the arrays
+# each kernel must touch once (neighbour re-reads served by cache are not counted).
+BYTES32 = {
+    "assemble": 8 + 8 * 8 + 4 * (4 + 4) + 4 * 8,  # f, 8 face/diag factors -> 4 hi+lo coefs, invD/R/colsum/y
+    "resid": 8 + 4 + 8 + 4 * (4 + 4) + 8 + 4,     # y, x, R, hi+lo coefs -> y', r
+    "bicg1": 4 * 4 + 4 * 4 + 2 * 4,               # r, p, v, r^, 4 coefs -> p', v'
+    "bicg2": 2 * 4 + 4 * 4 + 4,                   # r, v, 4 coefs -> t
+    "bicg3": 6 * 4 + 2 * 4,                       # r, v, p, t, r^, x -> x, r
+    "polish": 8 + 4 * (4 + 4) + 3 * 8 + 8,        # y, hi+lo coefs, R, invD, colsum -> f
+}
+
+
+def kernel_roofline(b, probs, peak, steps=2):
+    """Per-kernel event timing over `steps` steps; bytes from the cells each kernel processed."""
+    cells = np.array([p.nx * p.ny for p in probs], dtype=np.float64)
+    before = [b.stats(k) for k in range(len(probs))]
+    b.enable_timing(True)
+    b.step(steps, allow_not_converged=True)
+    kt = b.kernel_times()
+    b.enable_timing(False)
+    after = [b.stats(k) for k in range(len(probs))]
+    it = np.array([a["total_iterations"] - c["total_iterations"] for a, c in zip(after, before)], dtype=np.float64)
+    rf = np.array([a["total_refinements"] - c["total_refinements"] for a, c in zip(after, before)], dtype=np.float64)
+    proc = {"assemble": cells.sum() * steps, "polish": cells.sum() * steps, "resid": (cells * rf).sum(),
+            "bicg1": (cells * it).sum(), "bicg2": (cells * it).sum(), "bicg3": (cells * it).sum()}
+    out = {}
+    for name, (ms, n) in kt.items():
+        if name in BYTES32 and n > 0:
+            byts = BYTES32[name] * proc[name]
+            out[name] = {"ms": ms, "launches": int(n), "bytes": byts, "GBps": byts / (ms * 1e-3) / 1e9,
+                         "share": 0.0}
+        else:
+            out[name] = {"ms": ms, "launches": int(n)}
+    total = sum(v["ms"] for v in out.values())
+    for v in out.values():
+        v["share"] = v["ms"] / total if total else 0.0
+    dom = max((k for k in out if k in BYTES32), key=lambda k: out[k]["ms"])
+    d = out[dom]
+    ach = d["GBps"]
+    traffic = None
+    roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak[0], "unit": "GB/s",
+            "frac": ach / peak[0], "peak_source": peak[1], "traffic": traffic,
+            "bytes_per_launch": d["bytes"] / d["launches"], "avg_launch_ms": d["ms"] / d["launches"]}
+    return roof, out
+
+
+def run_ours(a):
+    from sayram2d_gb300 import build, capi
+
+    build.build()
+    capi.load()
+    t0 = time.perf_counter()
+    probs = cases.batch_problems(a.instances, a.seed, DT)
+    gen_s = time.perf_counter() - t0
+    ncells = int(sum(p.nx * p.ny for p in probs))
+    b = capi.Batch(probs, precision=capi.FP32_REFINE)
+    for _ in range(a.warmup):
+        b.step(1, allow_not_converged=True)
+    l0 = b.launches()
+    clk = Clocks()
+    clk.start()
+    b.record_event(0)
+    rc = b.step(a.steps, allow_not_converged=True)
+    b.record_event(1)
+    ms = b.elapsed_ms(0, 1)
+    clocks = clk.stop()
+    launches = b.launches() - l0
+    value = a.instances * a.steps / (ms * 1e-3)
+    peak = peak_hbm()
+    roof, kern = kernel_roofline(b, probs, peak)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded)",
+            "config": {"workload": f"batched FP32+FP64-refine: {a.instances} instances, nalpha,nE~U[64,256], "
+                                   f"rho~U[-0.9,0.9], tau~logU[0.1,10] d, dt={DT} day, refined to rel residual 1e-10",
+                       "instances": a.instances, "cells": ncells, "seed": a.seed, "precision": "fp32_refine",
+                       "l2": f"working set {b.device_bytes() / 1e9:.1f} GB >> 129 MB L2 (no flush needed)"},
+            "gpu_launches": int(launches), "roofline": roof, "kernels": kern, "clocks": clocks,
+            "status_last_step": rc, "setup_s": {"generate": gen_s}}
+    # accuracy: per-instance stats and rel L2 against the batched FP64 path after the same steps
+    st = [b.stats(k) for k in range(len(probs))]
+    nsteps_done = st[0]["steps"]
+    line["min_f"] = min(s["min_f"] for s in st)
+    line["max_mass_drift"] = max(s["mass_drift"] for s in st)
+    line["max_rel_residual"] = max(s["rel_residual"] for s in st)
+    line["not_converged"] = int(sum(1 for s in st if s["status"] != 0))
+    if not a.quick:
+        f32 = [b.f(k) for k in range(len(probs))]
+        # e2e through the public C-ABI with pinned host buffers
+        L = capi.load()
+        nbytes = 8 * ncells
+        hin = L.sayram_host_alloc(nbytes)
+        hout = L.sayram_host_alloc(nbytes)
+        arr_in = np.ctypeslib.as_array((__import__("ctypes").c_double * ncells).from_address(hin))
+        arr_in[:] = np.concatenate([f.ravel() for f in f32])
+        b.step_host(1, hin, hout, allow_not_converged=True)  # warm
+        e2e_steps = max(3, a.steps // 2)
+        t0 = time.perf_counter()
+        for s in range(e2e_steps):
+            src, dst = (hout, hin) if s % 2 == 0 else (hin, hout)
+            b.step_host(1, src, dst, allow_not_converged=True)
+        wall = time.perf_counter() - t0
+        L.sayram_host_free(hin)
+        L.sayram_host_free(hout)
+        line["e2e"] = {"value": a.instances * e2e_steps / wall, "unit": UNIT, "h2d_bytes_per_step": nbytes,
+                       "d2h_bytes_per_step": nbytes, "steps": e2e_steps,
+                       "api": "sayram_batch_step_host (pinned host f in/out every step)"}
+        b.close()
+        # batched FP64 on the same batch, same number of steps -> accuracy + precision gain
+        b64 = capi.Batch(probs, precision=capi.FP64)
+        b64.step(nsteps_done - 1, allow_not_converged=True)
+        b64.record_event(0)
+        b64.step(1, allow_not_converged=True)
+        b64.record_event(1)
+        ms64 = b64.elapsed_ms(0, 1)
+        errs = []
+        for k in range(len(probs)):
+            g = b64.f(k)
+            errs.append(float(np.linalg.norm(f32[k] - g) / np.linalg.norm(g)))
+        b64.close()
+        line["rel_err_vs_fp64"] = {"max": max(errs), "median": statistics.median(errs),
+                                   "reference": "batched FP64 GPU path (matches the oracle to <=1e-10)"}
+        line["batched_fp64"] = {"value": a.instances / (ms64 * 1e-3), "unit": UNIT, "ms_per_step": ms64}
+        # plain FP64 drop-in, one instance after another
+        ns = min(a.plain_sample, len(probs))
+        tot = 0.0
+        for k in range(ns):
+            s = capi.Solver(probs[k], precision=capi.FP64)
+            s.update()
+            s.record_event(0)
+            s.step(2)
+            s.record_event(1)
+            tot += s.elapsed_ms(0, 1) * 1e-3
+            s.close()
+        plain = 2 * ns / tot
+        line["plain_fp64"] = {"value": plain, "unit": UNIT,
+                              "sample": f"first {ns} instances, 2 steps each, one sayram_create per instance"}
+        line["speedup_vs_plain_fp64"] = value / plain
+        line["cpu_baseline"] = cpu_baseline_single(a.seed, a.instances, a.cpu_seconds)
+    else:
+        b.close()
+    print(json.dumps(line))
+
+
+def main():
+    a = parse()
+    if a.gpus != 1 or int(os.environ.get("WORLD_SIZE", "1")) != 1:
+        raise SystemExit("bench.py runs on one GPU (instances are independent; multi-GPU is replicas only "
+                         "and not part of this build)")
+    if a.warmup < 3 and a.impl == "ours":
+        a.warmup = 3
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

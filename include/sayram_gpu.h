@@ -97,6 +97,8 @@ typedef struct sayram_stats {
   double min_f;           /* minimum cell value after the positivity polish */
   long long clamped;      /* cells the polish lifted from a negative Krylov value */
   double mass_drift;      /* |1^T M f - 1^T R| / 1^T R after the last step */
+  long long total_iterations;  /* inner Krylov iterations since creation */
+  long long total_refinements; /* FP64 residual evaluations since creation */
 } sayram_stats;
 
 /* ---- library -------------------------------------------------------------------------- */
@@ -159,6 +161,10 @@ int sayram_batch_export_system(sayram_batch b, int idx, double* M5, double* R);
 size_t sayram_batch_device_bytes(sayram_batch b);
 /* The CUDA stream the batch launches on (a cudaStream_t, as void*), for event timing. */
 void* sayram_batch_stream(sayram_batch b);
+/* CUDA events on the batch's stream: record event slot (0..7); elapsed time between two recorded
+ * slots (waits for the later one). */
+int sayram_batch_record_event(sayram_batch b, int slot);
+int sayram_batch_elapsed_ms(sayram_batch b, int slot0, int slot1, double* ms);
 /* Per-kernel timing: when enabled, every launch is bracketed by CUDA events on the batch's
  * stream (steps then run without graphs). sayram_batch_kernel_times fills up to cap entries of
  * names/total milliseconds/launch counts and returns the number of kernels. */

@@ -50,6 +50,7 @@ class sayram_stats(ctypes.Structure):
         ("refinements", ctypes.c_int), ("iterations", ctypes.c_int),
         ("rel_residual", ctypes.c_double), ("min_f", ctypes.c_double),
         ("clamped", ctypes.c_longlong), ("mass_drift", ctypes.c_double),
+        ("total_iterations", ctypes.c_longlong), ("total_refinements", ctypes.c_longlong),
     ]
 
     def as_dict(self):
@@ -86,6 +87,8 @@ SIGNATURES = {
     "sayram_batch_export_system": (ctypes.c_int, [_P, ctypes.c_int, _dp, _dp]),
     "sayram_batch_device_bytes": (ctypes.c_size_t, [_P]),
     "sayram_batch_stream": (ctypes.c_void_p, [_P]),
+    "sayram_batch_record_event": (ctypes.c_int, [_P, ctypes.c_int]),
+    "sayram_batch_elapsed_ms": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, _dp]),
     "sayram_batch_enable_timing": (ctypes.c_int, [_P, ctypes.c_int]),
     "sayram_batch_kernel_times": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_char_p), _dp, ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
     "sayram_batch_launches": (ctypes.c_longlong, [_P]),
@@ -245,6 +248,14 @@ class Batch:
     def stream(self) -> int:
         return int(self._L.sayram_batch_stream(self.h) or 0)
 
+    def record_event(self, slot: int) -> None:
+        check(self._L.sayram_batch_record_event(self.h, slot), "sayram_batch_record_event")
+
+    def elapsed_ms(self, slot0: int, slot1: int) -> float:
+        ms = ctypes.c_double()
+        check(self._L.sayram_batch_elapsed_ms(self.h, slot0, slot1, ctypes.byref(ms)), "sayram_batch_elapsed_ms")
+        return ms.value
+
     def enable_timing(self, on: bool = True) -> None:
         check(self._L.sayram_batch_enable_timing(self.h, 1 if on else 0), "sayram_batch_enable_timing")
 
@@ -275,6 +286,15 @@ class Solver(Batch):
 
     def f(self, idx: int = 0) -> np.ndarray:  # Solver::f, Solver.h:24
         return super().f(0)
+
+    def set_f(self, f) -> None:  # replaces the state (alpha-major)
+        super().set_f(0, f)
+
+    def set_dirichlet(self, side: int, v) -> None:
+        super().set_dirichlet(0, side, v)
+
+    def set_coeffs(self, G, Dxx, Dxy, Dyy, inv_tau) -> None:
+        super().set_coeffs(0, G, Dxx, Dxy, Dyy, inv_tau)
 
     def get_stats(self) -> dict:
         return self.stats(0)

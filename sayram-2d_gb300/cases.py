@@ -325,15 +325,18 @@ def batch_sizes(n_instances: int, seed: int, lo: int = 64, hi: int = 256):
     return [(int(a), int(e)) for a, e in rng.integers(lo, hi + 1, size=(n_instances, 2))]
 
 
+def batch_instance(k: int, seed: int, dt: float, size) -> Problem:
+    """Instance k of a batch: its own seeded D fields, rho ~ U[-0.9, 0.9], tau log-uniform in
+    [0.1, 10] days (independent of the other instances, so any one can be generated alone)."""
+    rng = np.random.default_rng([seed, k, 17])
+    tau = float(10.0 ** rng.uniform(-1.0, 1.0))
+    rho = float(rng.uniform(-0.9, 0.9))
+    a, e = size
+    return synthetic_problem(int(a), int(e), dt, seed=seed * 7919 + k, tau=tau, rho=rho)
+
+
 def batch_problems(n_instances: int, seed: int, dt: float, lo: int = 64, hi: int = 256,
                    sizes: Optional[Sequence] = None) -> List[Problem]:
-    """Independent seeded instances: sizes uniform in [lo, hi]^2, rho ~ U[-0.9, 0.9],
-    tau log-uniform in [0.1, 10] days, each with its own D fields."""
-    rng = np.random.default_rng(seed + 1_000_003)
+    """Independent seeded instances: sizes uniform in [lo, hi]^2 (see batch_instance)."""
     sizes = sizes if sizes is not None else batch_sizes(n_instances, seed, lo, hi)
-    out = []
-    for k, (a, e) in enumerate(sizes):
-        tau = float(10.0 ** rng.uniform(-1.0, 1.0))
-        rho = float(rng.uniform(-0.9, 0.9))
-        out.append(synthetic_problem(a, e, dt, seed=seed * 7919 + k, tau=tau, rho=rho))
-    return out
+    return [batch_instance(k, seed, dt, sizes[k]) for k in range(n_instances)]

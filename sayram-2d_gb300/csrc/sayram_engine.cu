@@ -86,6 +86,7 @@ struct sayram_batch_s {
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
   std::vector<cudaEvent_t> evpool;
   size_t evused = 0;
+  cudaEvent_t slots[8] = {};
 
   ~sayram_batch_s() { release(); }
 
@@ -97,6 +98,8 @@ struct sayram_batch_s {
     h_ctl = nullptr;
     for (auto e : evpool) cudaEventDestroy(e);
     evpool.clear();
+    for (auto& e : slots)
+      if (e) cudaEventDestroy(e), e = nullptr;
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
   }
@@ -603,6 +606,8 @@ int sayram_batch_stats(sayram_batch b, int idx, sayram_stats* out) {
   out->min_f = s.min_f;
   out->clamped = s.clamped;
   out->mass_drift = s.mass_drift;
+  out->total_iterations = s.cum_iters;
+  out->total_refinements = s.cum_refines;
   return SAYRAM_OK;
 }
 
@@ -653,6 +658,24 @@ int sayram_batch_export_system(sayram_batch b, int idx, double* M5, double* R) {
 
 size_t sayram_batch_device_bytes(sayram_batch b) { return b ? b->bytes : 0; }
 void* sayram_batch_stream(sayram_batch b) { return b ? (void*)b->stream : nullptr; }
+
+int sayram_batch_record_event(sayram_batch b, int slot) {
+  if (!b || slot < 0 || slot >= 8) return fail(SAYRAM_ERR_ARG, "bad handle or slot");
+  SG_CUDA(cudaSetDevice(b->dev));
+  if (!b->slots[slot]) SG_CUDA(cudaEventCreate(&b->slots[slot]));
+  SG_CUDA(cudaEventRecord(b->slots[slot], b->stream));
+  return SAYRAM_OK;
+}
+
+int sayram_batch_elapsed_ms(sayram_batch b, int slot0, int slot1, double* ms) {
+  if (!b || !ms || slot0 < 0 || slot0 >= 8 || slot1 < 0 || slot1 >= 8 || !b->slots[slot0] || !b->slots[slot1])
+    return fail(SAYRAM_ERR_ARG, "bad handle or unrecorded slot");
+  SG_CUDA(cudaEventSynchronize(b->slots[slot1]));
+  float f = 0.f;
+  SG_CUDA(cudaEventElapsedTime(&f, b->slots[slot0], b->slots[slot1]));
+  *ms = f;
+  return SAYRAM_OK;
+}
 
 int sayram_batch_enable_timing(sayram_batch b, int enable) {
   if (!b) return fail(SAYRAM_ERR_ARG, "null handle");

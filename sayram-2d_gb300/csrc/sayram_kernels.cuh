@@ -57,6 +57,7 @@ struct InstState {
   double rr, rr_target, bb, rr64;
   double rel, mass_drift, min_f, pad_d;
   long long clamped, steps;
+  long long cum_iters, cum_refines;  // totals since creation (work accounting)
   int ycur, pcur, outer_active, inner_active;
   int restart, fresh, has_x, iters;
   int iters_total, refines, status, pad_i;

@@ -465,6 +465,7 @@ __global__ void __launch_bounds__(kThreads) k_resid(Common cm, Fields fl, Coef<C
       st.has_x = 0;
       if (st.refines == 0) st.bb = tot[1];
       st.refines += 1;
+      st.cum_refines += 1;
       st.rr64 = tot[0];
       st.rel = st.bb > 0 ? sqrt(tot[0] / st.bb) : 0.0;
       if (!(st.rel > tol)) {
@@ -643,6 +644,7 @@ __global__ void __launch_bounds__(kThreads) k_bicg3(Common cm, Kry<T> kr, int ma
       st.has_x = 1;
       st.iters += 1;
       st.iters_total += 1;
+      st.cum_iters += 1;
       const double rhoN = tot[0];
       st.rr = tot[1];
       if (!(tot[1] > st.rr_target) || st.iters >= max_iters || !isfinite(tot[1])) {
