@@ -78,7 +78,7 @@ typedef struct sayram_problem {
 typedef struct sayram_options {
   int precision;    /* SAYRAM_FP64 (default) or SAYRAM_FP32_REFINE */
   double tol;       /* target ||R - M f|| / ||R|| in the Jacobi-scaled system (FP64 residual);
-                       default 1e-12 (FP64) / 1e-10 (FP32_REFINE) */
+                       default 1e-12 (FP64) / 1e-11 (FP32_REFINE) */
   double inner_tol; /* residual reduction asked of each inner Krylov solve; default 0 (FP64:
                        solve to tol at once) / 1e-4 (FP32_REFINE) */
   int max_iters;    /* inner BiCGSTAB iterations per solve; default 500 */

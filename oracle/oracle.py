@@ -68,6 +68,8 @@ def lib():
             L.orc_vertex_f.argtypes = [P, _dp, _dp]
             L.orc_face_coeffs.argtypes = [P, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp]
             L.orc_assemble.argtypes = [P, _dp, _dp, _dp]
+            L.orc_assemble_bound.argtypes = [P, _dp, _dp, _dp, _dp]
+            L.orc_assemble_bound.restype = ctypes.c_int
             L.orc_solve.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]
             L.orc_step.argtypes = [P, _dp, ctypes.c_int]
             for fn in (L.orc_vertex_f, L.orc_face_coeffs, L.orc_assemble, L.orc_solve, L.orc_step):
@@ -130,6 +132,17 @@ def assemble(prob, f):
     R = np.empty(N)
     _check(lib().orc_assemble(ctypes.byref(P.s), _ptr(f), _ptr(M5), _ptr(R)), "assemble")
     return M5, R
+
+
+def assemble_bound(prob, f):
+    """(M5, R, B5): B5 is each entry's forward-error scale (its formula on term magnitudes)."""
+    P = _Packed(prob)
+    f = np.ascontiguousarray(f, dtype=np.float64)
+    N = prob.nx * prob.ny
+    M5, B5 = np.empty((5, N)), np.empty((5, N))
+    R = np.empty(N)
+    _check(lib().orc_assemble_bound(ctypes.byref(P.s), _ptr(f), _ptr(M5), _ptr(R), _ptr(B5)), "assemble_bound")
+    return M5, R, B5
 
 
 def to_csc(nx, ny, M5):

@@ -216,15 +216,39 @@ static void a_sigma(const orc_ws* w, int i, int j, int inbr, double* aa, double*
 
 static int rinbr(int inbr) { return (inbr + 2) & 3; } /* Mesh.h:115 {2,3,0,1} */
 
+/* vertex values at the A / B end of the edge of cell (i,j) in direction inbr (Mesh.cc:80-151) */
+static double vfA_(const orc_ws* w, int i, int j, int inbr) {
+  const int ny = w->p->ny;
+  switch (inbr) {
+    case ORC_IM: return VF(i, j + 1);
+    case ORC_JP: return VF(i + 1, j + 1);
+    case ORC_IP: return VF(i + 1, j);
+    default: return VF(i, j);
+  }
+}
+static double vfB_(const orc_ws* w, int i, int j, int inbr) {
+  const int ny = w->p->ny;
+  switch (inbr) {
+    case ORC_IM: return VF(i, j);
+    case ORC_JP: return VF(i, j + 1);
+    case ORC_IP: return VF(i + 1, j + 1);
+    default: return VF(i + 1, j);
+  }
+}
+
 typedef struct {
   double* M5;
   double* R;
   long N;
   int nx;
+  double* B5; /* optional: forward-error scale of every entry (same formulas on |terms|) */
 } orc_sys;
 
 /* add value v to diagonal d (0 = M(K,K), 1 = W, 2 = E, 3 = S, 4 = N) of row r */
 static void add_entry(orc_sys* s, long r, int d, double v) { s->M5[(long)d * s->N + r] += v; }
+static void add_bound(orc_sys* s, long r, int d, double v) {
+  if (s->B5) s->B5[(long)d * s->N + r] += v;
+}
 
 /* Solver::apply_inner_face_pair, Solver.cc:99-141 */
 static void inner_face_pair(const orc_ws* w, const double* f, orc_sys* s, int i, int j, int inbr) {
@@ -248,6 +272,26 @@ static void inner_face_pair(const orc_ws* w, const double* f, orc_sys* s, int i,
   const double AK = muK * (aaK + abK) + Bp / (F(i, j) + ORC_EPS);
   const double AL = muL * (aaL + abL) + Bm / (F(li, lj) + ORC_EPS);
   const long K = (long)j * nx + i, L = (long)lj * nx + li;
+  if (s->B5) { /* every sum replaced by the sum of magnitudes of its terms */
+    const int ny_ = w->p->ny;
+    double tA, tB, tK, tL;
+    (void)ny_;
+    tA = tB = tK = tL = 0.0;
+    double a0, a1, a2;
+    a_sigma(w, i, j, inbr, &a0, &a1, &a2);
+    (void)a2;
+    tK = fabs(a0) * fabs(vfA_(w, i, j, inbr)) + fabs(a1) * fabs(vfB_(w, i, j, inbr));
+    a_sigma(w, li, lj, rinbr(inbr), &a0, &a1, &a2);
+    tL = fabs(a0) * fabs(vfA_(w, li, lj, rinbr(inbr))) + fabs(a1) * fabs(vfB_(w, li, lj, rinbr(inbr)));
+    tA = muK * (fabs(aaK) + fabs(abK)) + (muL * tL + muK * tK) / (F(i, j) + ORC_EPS);
+    tB = muL * (fabs(aaL) + fabs(abL)) + (muL * tL + muK * tK) / (F(li, lj) + ORC_EPS);
+    const int dKL_ = (inbr == ORC_IM) ? 1 : (inbr == ORC_IP) ? 2 : (inbr == ORC_JM) ? 3 : 4;
+    const int dLK_ = (dKL_ == 1) ? 2 : (dKL_ == 2) ? 1 : (dKL_ == 3) ? 4 : 3;
+    add_bound(s, K, 0, tA);
+    add_bound(s, K, dKL_, tB);
+    add_bound(s, L, 0, tB);
+    add_bound(s, L, dLK_, tA);
+  }
   /* K's neighbour L lies west (inbr = im) or south (inbr = jm) of K */
   const int dKL = (inbr == ORC_IM) ? 1 : (inbr == ORC_IP) ? 2 : (inbr == ORC_JM) ? 3 : 4;
   const int dLK = (dKL == 1) ? 2 : (dKL == 2) ? 1 : (dKL == 3) ? 4 : 3;
@@ -269,15 +313,18 @@ static void dirichlet_face(const orc_ws* w, const double* f, orc_sys* s, int i, 
   const double AK = aa + ab + Bp / (F(i, j) + ORC_EPS);
   const long K = (long)j * nx + i;
   add_entry(s, K, 0, AK);
+  add_bound(s, K, 0, fabs(aa) + fabs(ab) +
+            (fabs(aa) * fabs(vfA_(w, i, j, inbr)) + fabs(ab) * fabs(vfB_(w, i, j, inbr))) / (F(i, j) + ORC_EPS));
   s->R[K] += Bm;
 }
 
-static void assemble_ws(const orc_ws* w, const double* f, double* M5, double* R) {
+static void assemble_ws(const orc_ws* w, const double* f, double* M5, double* R, double* B5) {
   const orc_problem* p = w->p;
   const int nx = p->nx, ny = p->ny;
   const long N = (long)nx * ny;
-  orc_sys s = {M5, R, N, nx};
+  orc_sys s = {M5, R, N, nx, B5};
   memset(M5, 0, sizeof(double) * 5 * (size_t)N);
+  if (B5) memset(B5, 0, sizeof(double) * 5 * (size_t)N);
   memset(R, 0, sizeof(double) * (size_t)N);
   /* 1) interior faces: west faces, then south faces (Solver.cc:172-182) */
   for (int i = 1; i < nx; ++i)
@@ -301,6 +348,7 @@ static void assemble_ws(const orc_ws* w, const double* f, double* M5, double* R)
       const size_t c = (size_t)i * ny + j;
       const double UKK = p->G[c] * (w->dxc[i] * w->dyc[j] / p->dt);
       add_entry(&s, K, 0, UKK * (1 + p->dt * p->inv_tau[c]));
+      add_bound(&s, K, 0, UKK * (1 + p->dt * p->inv_tau[c]));
       R[K] += UKK * F(i, j);
     }
   }
@@ -339,7 +387,20 @@ int orc_assemble(const orc_problem* p, const double* f, double* M5, double* R) {
   orc_ws w;
   if (ws_init(&w, p)) { ws_free(&w); return -3; }
   vertex_f(&w, f);
-  assemble_ws(&w, f, M5, R);
+  assemble_ws(&w, f, M5, R, NULL);
+  ws_free(&w);
+  return 0;
+}
+
+/* As orc_assemble, plus B5: for every entry the same expression evaluated on the magnitudes of
+   its terms (sums of |products|), the scale of its floating-point rounding error. */
+int orc_assemble_bound(const orc_problem* p, const double* f, double* M5, double* R, double* B5) {
+  int rc = check_problem(p);
+  if (rc) return rc;
+  orc_ws w;
+  if (ws_init(&w, p)) { ws_free(&w); return -3; }
+  vertex_f(&w, f);
+  assemble_ws(&w, f, M5, R, B5);
   ws_free(&w);
   return 0;
 }
@@ -378,7 +439,7 @@ int orc_step(const orc_problem* p, double* f, int nsteps) {
   if (ws_init(&w, p) || !M5 || !R || !x) { ws_free(&w); free(M5); free(R); free(x); return -3; }
   for (int s = 0; s < nsteps && rc == 0; ++s) {
     vertex_f(&w, f);
-    assemble_ws(&w, f, M5, R);
+    assemble_ws(&w, f, M5, R, NULL);
     rc = orc_solve(nx, ny, M5, R, x);
     for (int i = 0; i < nx; ++i)
       for (int j = 0; j < ny; ++j) F(i, j) = x[(long)j * nx + i];

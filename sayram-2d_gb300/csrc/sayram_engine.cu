@@ -201,7 +201,7 @@ int sayram_batch_s::build(const sayram_problem* probs, int count, const sayram_o
   if (o) opt = *o;
   if (opt.precision != SAYRAM_FP64 && opt.precision != SAYRAM_FP32_REFINE)
     return fail(SAYRAM_ERR_ARG, "unknown precision");
-  if (!(opt.tol > 0)) opt.tol = opt.precision == SAYRAM_FP64 ? 1e-12 : 1e-10;
+  if (!(opt.tol > 0)) opt.tol = opt.precision == SAYRAM_FP64 ? 1e-12 : 1e-11;
   if (opt.inner_tol < 0) opt.inner_tol = 0;
   if (opt.max_iters < 1) opt.max_iters = 1;
   if (opt.max_refine < 2) opt.max_refine = 2;

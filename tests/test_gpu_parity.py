@@ -4,9 +4,10 @@ error <= 1e-10 and stay non-negative; the FP32+FP64-refinement path to <= 1e-8.
 
 Matrix entries: the GPU evaluates the reference's formulas with fused multiply-adds and a
 reciprocal of (f + eps). Where f is about eps, B+/(f + eps) magnifies the rounding of a nearly
-cancelling a_sigma = aA*fA + aB*fB; the reference compiled with FMA contraction (the default of
-its own clang build) moves such entries by ~2e-13 of the row scale in the loss-cone fixture. So
-every entry must lie within 1e-10 of its row scale and at least 99% of them within 1e-14."""
+cancelling a_sigma = aA*fA + aB*fB (the reference compiled with FMA contraction, the default of
+its own clang build, moves such entries too). Each entry is therefore held to 1e-12 of its
+forward-error scale: the same formula evaluated on the magnitudes of its terms (oracle
+assemble_bound), about 4500 units in the last place of that scale."""
 import os
 
 import numpy as np
@@ -26,17 +27,17 @@ def rel(a, b):
 
 
 @pytest.mark.parametrize("name", NAMES)
-def test_assembly_matches_reference(capi, name):
+def test_assembly_matches_reference(capi, oracle, name):
     p = problem_from(Z, name)
+    ref, Rref = Z[f"{name}/M5"], Z[f"{name}/R"]
+    M5o, _, bound = oracle.assemble_bound(p, p.f0)
+    assert np.array_equal(M5o, ref)
     for prec in (capi.FP64, capi.FP32_REFINE):
         s = capi.Solver(p, precision=prec)
         M5, R = s.export_system(0)
         s.close()
-        ref, Rref = Z[f"{name}/M5"], Z[f"{name}/R"]
-        scale = np.abs(ref).sum(axis=0)  # row scale
-        err = np.abs(M5 - ref) / scale[None, :]
-        assert err.max() <= 1e-10, (name, prec, err.max())
-        assert (err <= 1e-14).mean() >= 0.99, (name, prec, (err <= 1e-14).mean())
+        err = np.abs(M5 - ref)
+        assert (err <= 1e-12 * bound).all(), (name, prec, (err / np.maximum(bound, 1e-300)).max())
         assert np.allclose(R, Rref, rtol=1e-13, atol=1e-300), name
 
 

@@ -131,3 +131,12 @@ def test_generators_deterministic():
     assert a.Dxx.min() > 0 and a.Dxx.max() <= 1e-2
     sizes = cases.batch_sizes(64, seed=3)
     assert all(64 <= x <= 256 and 64 <= y <= 256 for x, y in sizes)
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_forward_error_scale(oracle, name):
+    """The per-entry error scale covers every entry's magnitude (it sums |terms|)."""
+    p = problem_from(Z, name)
+    M5, R, B5 = oracle.assemble_bound(p, p.f0)
+    assert np.array_equal(M5, Z[f"{name}/M5"])
+    assert (B5 >= np.abs(M5) * (1 - 1e-12)).all()
