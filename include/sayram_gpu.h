@@ -175,6 +175,31 @@ int sayram_batch_kernel_times(sayram_batch b, const char** names, double* total_
 long long sayram_batch_launches(sayram_batch b);
 void sayram_batch_destroy(sayram_batch b);
 
+/* ---- stepping without allocating -------------------------------------------------------
+ * sayram_step_noalloc: nsteps FP64 backward-Euler steps of ONE instance that allocate no memory.
+ * No counterpart in the reference. It is for callers that cannot call cudaMalloc: programs whose
+ * own memory manager owns the GPU's memory (for example a larger model that embeds this step and
+ * reserves the device through its own pool), and programs that must not allocate once running
+ * (a memory budget fixed at start, where an allocation failure mid-run is not acceptable).
+ *
+ * Every array pointer in *p (edges, G, Dxx, Dxy, Dyy, inv_tau, Dirichlet values) and f_in/f_out
+ * is a DEVICE pointer, with the same layouts as for sayram_create; p->f0 is ignored and the state
+ * comes from f_in (alpha-major). f_out may equal f_in. stream is a cudaStream_t (NULL = legacy
+ * default stream); the call returns once that stream has finished the work. opt may be NULL and
+ * must select SAYRAM_FP64. stats (may be NULL) receives this call's statistics.
+ *
+ * Working memory is one fixed device array of 16,384,000 bytes defined in this library; every
+ * GPU that loads the library holds it until the process exits. A grid fits when
+ * round_up((ny+2) * round_up(nx,4), 32) + 64 <= 73728 cells and nx, ny <= 4096 (256 x 256
+ * fits); larger grids return SAYRAM_ERR_ARG with a message saying so.
+ * The first call on a device looks up the array's device address (cudaGetSymbolAddress) and
+ * keeps it for later calls; make that first call before any stream capture begins.
+ * All calls share the array: each call clears it at its start and the array keeps the last
+ * call's contents afterwards. Calls that overlap on the GPU (several host threads or streams at
+ * once) race on it and must be serialized by the caller. */
+int sayram_step_noalloc(const sayram_problem* p, const sayram_options* opt, int nsteps,
+                        const double* f_in, double* f_out, void* stream, sayram_stats* stats);
+
 /* Bytes of device memory an instance of nx*ny cells needs (admission control). */
 size_t sayram_instance_bytes(int nx, int ny, int precision);
 

@@ -94,6 +94,9 @@ SIGNATURES = {
     "sayram_batch_launches": (ctypes.c_longlong, [_P]),
     "sayram_batch_destroy": (None, [_P]),
     "sayram_instance_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "sayram_step_noalloc": (ctypes.c_int, [ctypes.POINTER(sayram_problem), ctypes.POINTER(sayram_options),
+                                           ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.POINTER(sayram_stats)]),
 }
 
 _lib = None

@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -738,3 +739,287 @@ int sayram_get_stats(sayram_solver s, sayram_stats* out) { return sayram_batch_s
 void sayram_destroy(sayram_solver s) { sayram_batch_destroy(s); }
 
 }  // extern "C"
+
+// ================================================================================== no allocation
+// sayram_step_noalloc: the FP64 single-instance step for callers that cannot allocate device
+// memory (see the header). Its working arrays live in one file-scope device array that the CUDA
+// runtime creates when the module loads; this path calls no cudaMalloc / cudaFree /
+// cudaMallocHost and no allocating library routine.
+namespace {
+
+constexpr long long kNoAllocCells = 73728;  // padded cells: round_up((ny+2)*round_up(nx,4), 32) + 64
+constexpr int kNoAllocMaxSide = 4096;       // nx, ny limit (host tables are on the stack)
+constexpr int kNoAllocMaxChunks = (int)(kNoAllocCells / sg::kChunk) + 2;
+constexpr int kNoAllocMaxTiles = 8192;
+constexpr size_t kNoAllocTableBytes = 1u << 20;
+constexpr size_t kNoAllocBytes = kNoAllocTableBytes + (size_t)kNoAllocCells * 26 * sizeof(double);
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+std::mutex g_noalloc_mu;
+unsigned char* g_noalloc_base[128] = {};  // device address of g_noalloc_scratch, per device
+
+// Per-cell face factors from separate coefficient arrays (alpha-major); same arithmetic as
+// k_setup, which reads one packed staging buffer instead.
+__global__ void k_setup_fields(sg::Common cm, sg::Geo geo, const double* G, const double* Dxx,
+                               const double* Dxy, const double* Dyy, const double* itau,
+                               const double* xe, const double* ye) {
+  const sg::InstDev I = cm.inst[0];
+  const long long ncell = (long long)I.nx * I.ny;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < ncell;
+       c += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(c / I.ny), j = (int)(c % I.ny);
+    const long long K = I.base + (long long)j * I.pitch + i;
+    const double xl = xe[i], xr = xe[i + 1];
+    const double yb = ye[j], yt = ye[j + 1];
+    const double dx = __dadd_rn(xr, -xl), dy = __dadd_rn(yt, -yb);
+    const double Kx = __dmul_rn(0.5, __dadd_rn(xl, xr)), Ky = __dmul_rn(0.5, __dadd_rn(yb, yt));
+    const double g = G[c];
+    const double L[4] = {__dmul_rn(Dxx[c], g), __dmul_rn(Dxy[c], g), __dmul_rn(Dxy[c], g),
+                         __dmul_rn(Dyy[c], g)};
+    double aa, ab;
+    sg::face_pair(Kx, Ky, xl, yt, xl, yb, -1.0, 0.0, L, &aa, &ab);
+    geo.aAx[K] = aa;
+    geo.aBx[K] = ab;
+    geo.Sx[K] = __dadd_rn(aa, ab);
+    sg::face_pair(Kx, Ky, xl, yb, xr, yb, 0.0, -1.0, L, &aa, &ab);
+    geo.aAy[K] = aa;
+    geo.aBy[K] = ab;
+    geo.Sy[K] = __dadd_rn(aa, ab);
+    const double ukk = __dmul_rn(g, __ddiv_rn(__dmul_rn(dx, dy), I.dt));
+    geo.ukk[K] = ukk;
+    geo.sdiag[K] = __dmul_rn(ukk, __dadd_rn(1.0, __dmul_rn(I.dt, itau[c])));
+  }
+}
+
+// Carves the scratch array into the typed regions of one instance.
+struct NoAllocLayout {
+  unsigned char* cur;
+  unsigned char* end;
+  template <typename T>
+  T* take(long long count) {
+    const size_t nb = ((size_t)count * sizeof(T) + 255) & ~(size_t)255;
+    if (cur + nb > end) return nullptr;
+    T* p = reinterpret_cast<T*>(cur);
+    cur += nb;
+    return p;
+  }
+};
+
+int noalloc_device_base(int dev, unsigned char** out) {
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (dev < 0 || dev >= 128) return fail(SAYRAM_ERR_ARG, "device ordinal out of range");
+  if (!g_noalloc_base[dev]) {
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || !ptr)
+      return fail(SAYRAM_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+    g_noalloc_base[dev] = (unsigned char*)ptr;
+  }
+  *out = g_noalloc_base[dev];
+  return SAYRAM_OK;
+}
+
+}  // namespace
+
+extern "C" int sayram_step_noalloc(const sayram_problem* pd, const sayram_options* opt, int nsteps,
+                                   const double* f_in, double* f_out, void* stream_ptr,
+                                   sayram_stats* stats_out) {
+  using namespace sg;
+  if (!pd || !f_in || !f_out || nsteps < 0) return fail(SAYRAM_ERR_ARG, "null problem/buffer or negative nsteps");
+  const int nx = pd->nx, ny = pd->ny;
+  if (nx < 1 || ny < 1) return fail(SAYRAM_ERR_ARG, "Grid2D: x_edges/y_edges must have size >= 2.");
+  const long long pitch = round_up(nx, 4);
+  const long long padded = round_up((long long)(ny + 2) * pitch, 32) + 64;
+  if (nx > kNoAllocMaxSide || ny > kNoAllocMaxSide || padded > kNoAllocCells)
+    return fail(SAYRAM_ERR_ARG, "sayram_step_noalloc: grid " + std::to_string(nx) + "x" + std::to_string(ny) +
+                                    " exceeds the fixed scratch (needs round_up((ny+2)*round_up(nx,4),32)+64 <= " +
+                                    std::to_string(kNoAllocCells) + " cells and nx, ny <= " +
+                                    std::to_string(kNoAllocMaxSide) + "; 256x256 fits)");
+  if (!pd->x_edges || !pd->y_edges || !pd->G || !pd->Dxx || !pd->Dxy || !pd->Dyy || !pd->inv_tau)
+    return fail(SAYRAM_ERR_ARG, "missing device array in the problem");
+  if (!(pd->dt > 0) || !std::isfinite(pd->dt)) return fail(SAYRAM_ERR_ARG, "dt must be positive");
+  for (int s = 0; s < 4; ++s) {
+    if (pd->bc[s] != SAYRAM_DIRICHLET && pd->bc[s] != SAYRAM_ZEROFLUX) return fail(SAYRAM_ERR_ARG, "unknown boundary type");
+    if (pd->bc[s] == SAYRAM_DIRICHLET && !pd->dirichlet[s]) return fail(SAYRAM_ERR_ARG, "Dirichlet BC: missing value.");
+  }
+  sayram_options o;
+  sayram_default_options(&o);
+  if (opt) o = *opt;
+  if (o.precision != SAYRAM_FP64) return fail(SAYRAM_ERR_ARG, "sayram_step_noalloc runs the FP64 path only");
+  if (!(o.tol > 0)) o.tol = 1e-12;
+  if (o.inner_tol < 0) o.inner_tol = 0.0;
+  if (o.max_iters < 1) o.max_iters = 1;
+  if (o.max_refine < 2) o.max_refine = 2;
+  int dev = 0;
+  SG_CUDA(cudaGetDevice(&dev));
+  unsigned char* base = nullptr;
+  int rc = noalloc_device_base(dev, &base);
+  if (rc) return rc;
+  cudaStream_t stream = (cudaStream_t)stream_ptr;
+  int nsm = 0;
+  SG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+
+  // ---- host tables (stack), the same layout rules as sayram_batch_create for one instance
+  InstDev I;
+  std::memset(&I, 0, sizeof(I));
+  I.nx = nx;
+  I.ny = ny;
+  I.pitch = (int)pitch;
+  I.enabled = 1;
+  for (int s = 0; s < 4; ++s) I.bc[s] = pd->bc[s];
+  I.base = pitch;
+  I.hoff = 0;
+  I.chunk0 = 0;
+  I.nchunks = (int)((round_up((long long)ny * pitch, 4) + kChunk - 1) / kChunk);
+  I.tile0 = 0;
+  I.ntx = (nx + kTX - 1) / kTX;
+  I.nty = (ny + kTY - 1) / kTY;
+  if (I.nchunks > kNoAllocMaxChunks || I.ntx * I.nty > kNoAllocMaxTiles)
+    return fail(SAYRAM_ERR_ARG, "sayram_step_noalloc: grid exceeds the fixed work tables");
+  I.xe = 0;
+  I.ye = 0;
+  int doff = 0;
+  for (int s = 0; s < 4; ++s) {
+    I.dir[s] = pd->bc[s] == SAYRAM_DIRICHLET ? doff : -1;
+    if (pd->bc[s] == SAYRAM_DIRICHLET) doff += (s <= 1) ? ny + 1 : nx + 1;
+  }
+  I.dt = pd->dt;
+  static thread_local double hxe[kNoAllocMaxSide + 1], hye[kNoAllocMaxSide + 1];
+  static thread_local double hwx[2 * (kNoAllocMaxSide + 1)], hwy[2 * (kNoAllocMaxSide + 1)];
+  static thread_local int hchunk[kNoAllocMaxChunks], htile[kNoAllocMaxTiles];
+
+  // ---- carve the scratch array
+  NoAllocLayout lay{base, base + kNoAllocBytes};
+  InstDev* d_inst = lay.take<InstDev>(1);
+  InstState* d_st = lay.take<InstState>(1);
+  Ctl* d_ctl = lay.take<Ctl>(1);
+  int* d_chunk = lay.take<int>(kNoAllocMaxChunks);
+  int* d_tile = lay.take<int>(kNoAllocMaxTiles);
+  double* d_wx = lay.take<double>(2 * (nx + 1));
+  double* d_wy = lay.take<double>(2 * (ny + 1));
+  double* d_dirv = lay.take<double>(doff > 0 ? doff : 1);
+  double* d_part = lay.take<double>(4LL * kNoAllocMaxChunks);
+  unsigned char* tables_end = lay.cur;
+  if (!d_part || tables_end > base + kNoAllocTableBytes) return fail(SAYRAM_ERR_ARG, "tables exceed the scratch");
+  lay.cur = base + kNoAllocTableBytes;
+  Geo geo{};
+  Fields fl{};
+  Coef<double> co{};
+  Kry<double> kr{};
+  double** cellarrs[26] = {&geo.aAx, &geo.aBx, &geo.Sx, &geo.aAy, &geo.aBy, &geo.Sy, &geo.ukk, &geo.sdiag,
+                           &fl.f, &fl.invD, &fl.R, &fl.colsum, &fl.y64[0], &fl.y64[1],
+                           &co.cw, &co.ce, &co.cs, &co.cn,
+                           &kr.r, &kr.rh, &kr.t, &kr.x, &kr.p[0], &kr.p[1], &kr.v[0], &kr.v[1]};
+  for (auto a : cellarrs) {
+    *a = lay.take<double>(kNoAllocCells);
+    if (!*a) return fail(SAYRAM_ERR_ARG, "cell arrays exceed the scratch");
+  }
+  unsigned char* used_end = lay.cur;
+
+  // ---- every call starts from zero: padding, pad rows, state and counters must be 0
+  SG_CUDA(cudaMemsetAsync(base, 0, (size_t)(used_end - base), stream));
+  SG_CUDA(cudaMemcpyAsync(hxe, pd->x_edges, sizeof(double) * (nx + 1), cudaMemcpyDeviceToHost, stream));
+  SG_CUDA(cudaMemcpyAsync(hye, pd->y_edges, sizeof(double) * (ny + 1), cudaMemcpyDeviceToHost, stream));
+  SG_CUDA(cudaStreamSynchronize(stream));
+  for (int i = 0; i < nx; ++i)
+    if (!(hxe[i + 1] > hxe[i])) return fail(SAYRAM_ERR_ARG, "Grid2D: x_edges must be strictly increasing at i=" + std::to_string(i));
+  for (int j = 0; j < ny; ++j)
+    if (!(hye[j + 1] > hye[j])) return fail(SAYRAM_ERR_ARG, "Grid2D: y_edges must be strictly increasing at j=" + std::to_string(j));
+  for (int k = 0; k < 2 * (kNoAllocMaxSide + 1) && k < 2 * (nx + 1); ++k) hwx[k] = 0.0;
+  for (int k = 0; k < 2 * (kNoAllocMaxSide + 1) && k < 2 * (ny + 1); ++k) hwy[k] = 0.0;
+  for (int i = 1; i < nx; ++i) {  // bilinear weights of Solver.cc:333-336
+    const double xv = hxe[i], xl = 0.5 * (hxe[i - 1] + hxe[i]), xr = 0.5 * (hxe[i] + hxe[i + 1]);
+    hwx[2 * i] = (xr - xv) / (xr - xl);
+    hwx[2 * i + 1] = (xv - xl) / (xr - xl);
+  }
+  for (int j = 1; j < ny; ++j) {
+    const double yv = hye[j], yb = 0.5 * (hye[j - 1] + hye[j]), yt = 0.5 * (hye[j] + hye[j + 1]);
+    hwy[2 * j] = (yt - yv) / (yt - yb);
+    hwy[2 * j + 1] = (yv - yb) / (yt - yb);
+  }
+  for (int k = 0; k < I.nchunks; ++k) hchunk[k] = 0;
+  for (int k = 0; k < I.ntx * I.nty; ++k) htile[k] = 0;
+  SG_CUDA(cudaMemcpyAsync(d_inst, &I, sizeof(I), cudaMemcpyHostToDevice, stream));
+  SG_CUDA(cudaMemcpyAsync(d_chunk, hchunk, sizeof(int) * I.nchunks, cudaMemcpyHostToDevice, stream));
+  SG_CUDA(cudaMemcpyAsync(d_tile, htile, sizeof(int) * I.ntx * I.nty, cudaMemcpyHostToDevice, stream));
+  SG_CUDA(cudaMemcpyAsync(d_wx, hwx, sizeof(double) * 2 * (nx + 1), cudaMemcpyHostToDevice, stream));
+  SG_CUDA(cudaMemcpyAsync(d_wy, hwy, sizeof(double) * 2 * (ny + 1), cudaMemcpyHostToDevice, stream));
+  for (int s = 0; s < 4; ++s)
+    if (I.dir[s] >= 0)
+      SG_CUDA(cudaMemcpyAsync(d_dirv + I.dir[s], pd->dirichlet[s], sizeof(double) * ((s <= 1) ? ny + 1 : nx + 1),
+                              cudaMemcpyDeviceToDevice, stream));
+  Common cm{};
+  cm.inst = d_inst;
+  cm.st = d_st;
+  cm.ctl = d_ctl;
+  cm.chunk_inst = d_chunk;
+  cm.nchunks = I.nchunks;
+  cm.tile_inst = d_tile;
+  cm.ntiles = I.ntx * I.nty;
+  cm.ninst = 1;
+  cm.wx = d_wx;
+  cm.wy = d_wy;
+  cm.dirv = d_dirv;
+  cm.part = d_part;
+  // the caller's edges are read directly by the setup kernel
+  const long long ncell = (long long)nx * ny;
+  const int sblocks = (int)std::min<long long>((ncell + 255) / 256, (long long)nsm * 8);
+  k_setup_fields<<<sblocks, 256, 0, stream>>>(cm, geo, pd->G, pd->Dxx, pd->Dxy, pd->Dyy, pd->inv_tau,
+                                             pd->x_edges, pd->y_edges);
+  SG_CUDA(cudaGetLastError());
+  const int gt = std::max(1, std::min(cm.ntiles, nsm * 8));
+  const int gs = std::max(1, std::min(cm.nchunks, nsm * 16));
+  k_field_in<<<gt, 256, 0, stream>>>(cm, fl.f, f_in);
+  SG_CUDA(cudaGetLastError());
+  Ctl hctl;
+  for (int s = 0; s < nsteps; ++s) {
+    SG_CUDA(cudaMemsetAsync(d_ctl, 0, 2 * sizeof(int), stream));
+    k_begin<<<1, 32, 0, stream>>>(cm);
+    k_assemble<double><<<gt, kAsmThreads, 0, stream>>>(cm, geo, fl, co);
+    for (int r = 0; r < o.max_refine; ++r) {
+      k_resid<double, double><<<gs, kThreads, 0, stream>>>(cm, fl, co, kr, o.tol, o.inner_tol, o.max_refine);
+      SG_CUDA(cudaGetLastError());
+      if (r == o.max_refine - 1) break;
+      SG_CUDA(cudaMemcpyAsync(&hctl, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, stream));
+      SG_CUDA(cudaStreamSynchronize(stream));
+      if (hctl.n_outer == 0) break;
+      for (int it = 0; it < o.max_iters; ++it) {
+        k_bicg1<double><<<gs, kThreads, 0, stream>>>(cm, co, kr);
+        k_bicg2<double><<<gs, kThreads, 0, stream>>>(cm, co, kr);
+        k_bicg3<double><<<gs, kThreads, 0, stream>>>(cm, kr, o.max_iters);
+        SG_CUDA(cudaGetLastError());
+        if (it < 4 || (it & 3) == 3) {
+          SG_CUDA(cudaMemcpyAsync(&hctl, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, stream));
+          SG_CUDA(cudaStreamSynchronize(stream));
+          if (hctl.n_inner == 0) break;
+        }
+      }
+    }
+    k_polish<double><<<gs, kThreads, 0, stream>>>(cm, fl, co);
+    SG_CUDA(cudaGetLastError());
+  }
+  k_field_out<<<gt, 256, 0, stream>>>(cm, f_out, fl.f);
+  SG_CUDA(cudaGetLastError());
+  InstState hs;
+  SG_CUDA(cudaMemcpyAsync(&hs, d_st, sizeof(hs), cudaMemcpyDeviceToHost, stream));
+  SG_CUDA(cudaStreamSynchronize(stream));
+  if (stats_out) {
+    stats_out->steps = hs.steps;
+    stats_out->t = (double)hs.steps * pd->dt;
+    stats_out->status = hs.steps == 0 ? SAYRAM_OK
+                        : hs.status == ST_NEGATIVE ? SAYRAM_ERR_NEGATIVE
+                        : hs.status == ST_NOT_CONVERGED ? SAYRAM_ERR_NOT_CONVERGED : SAYRAM_OK;
+    stats_out->refinements = hs.refines;
+    stats_out->iterations = hs.iters_total;
+    stats_out->rel_residual = hs.rel;
+    stats_out->min_f = hs.min_f;
+    stats_out->clamped = hs.clamped;
+    stats_out->mass_drift = hs.mass_drift;
+    stats_out->total_iterations = hs.cum_iters;
+    stats_out->total_refinements = hs.cum_refines;
+  }
+  if (hs.steps > 0 && hs.status == ST_NEGATIVE) return fail(SAYRAM_ERR_NEGATIVE, "a negative cell survived the positivity polish");
+  if (hs.steps > 0 && hs.status == ST_NOT_CONVERGED) return fail(SAYRAM_ERR_NOT_CONVERGED, "a step ended above the residual target");
+  return SAYRAM_OK;
+}
