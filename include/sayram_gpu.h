@@ -57,6 +57,10 @@ extern "C" {
 /* ---- precision modes --------------------------------------------------------------------- */
 #define SAYRAM_FP64 0        /* FP64 everywhere (the plain drop-in) */
 #define SAYRAM_FP32_REFINE 1 /* FP32 matrix/Krylov, FP64 residual + refinement + checks */
+#define SAYRAM_FP32_REFINE_DW 2 /* FP32 matrix/Krylov; the residual, refinement, assembly and
+                                   checks in double-word arithmetic (pairs of FP32, ~48-bit
+                                   significand) on the FP32 pipes -- GB300's FP64 rate is 1/69 of
+                                   its FP32 rate */
 
 /* One instance: grid, time step, coefficients, initial state and boundary conditions. All
  * arrays are read during the call that receives the struct and are not retained. */
@@ -76,11 +80,11 @@ typedef struct sayram_problem {
 } sayram_problem;
 
 typedef struct sayram_options {
-  int precision;    /* SAYRAM_FP64 (default) or SAYRAM_FP32_REFINE */
+  int precision;    /* SAYRAM_FP64 (default), SAYRAM_FP32_REFINE or SAYRAM_FP32_REFINE_DW */
   double tol;       /* target ||R - M f|| / ||R|| in the Jacobi-scaled system (FP64 residual);
-                       default 1e-12 (FP64) / 1e-11 (FP32_REFINE) */
+                       default 1e-12 (FP64) / 1e-11 (FP32_REFINE, FP32_REFINE_DW) */
   double inner_tol; /* residual reduction asked of each inner Krylov solve; default 0 (FP64:
-                       solve to tol at once) / 1e-4 (FP32_REFINE) */
+                       solve to tol at once) / 1e-4 (FP32 modes) */
   int max_iters;    /* inner BiCGSTAB iterations per solve; default 500 */
   int max_refine;   /* FP64 residual evaluations (outer refinements) per step; default 6 */
   int device;       /* CUDA device ordinal; default 0 */

@@ -22,7 +22,7 @@ from . import build as _build
 _dp = ctypes.POINTER(ctypes.c_double)
 
 OK, ERR_ARG, ERR_OOM, ERR_NOT_CONVERGED, ERR_NEGATIVE, ERR_TIMEOUT, ERR_CUDA, ERR_BUDGET, ERR_STATE = range(9)
-FP64, FP32_REFINE = 0, 1
+FP64, FP32_REFINE, FP32_REFINE_DW = 0, 1, 2
 
 
 class sayram_problem(ctypes.Structure):

@@ -1,0 +1,114 @@
+// dword.cuh -- double-word arithmetic: a value is an unevaluated sum hi + lo of two FP32 numbers
+// with |lo| <= ulp(hi)/2, giving a ~48-bit significand computed entirely on the FP32 pipes.
+//
+// GB300's FP64 pipe runs at 1/69 of its FP32 rate (measured 503 GFMA/s vs 34.9 TFMA/s) and its
+// FP64<->FP32 conversions run at the FP64 rate, so FP64-class accuracy is cheaper in double-word
+// form. The building blocks are the published error-free transformations and double-word
+// algorithms:
+//   2Sum (Knuth, TAOCP vol. 2), Fast2Sum (Dekker 1971), Fast2Mult with FMA,
+//   AccurateDWPlusDW (Alg. 6), DWPlusFP (Alg. 4), DWTimesFP3 (Alg. 9) and DWTimesDW3 (Alg. 12) of
+//   M. Joldes, J.-M. Muller, V. Popescu, "Tight and rigorous error bounds for basic building
+//   blocks of double-word arithmetic", ACM TOMS 44(2), 2017 -- relative errors <= 3u^2, 2u^2,
+//   2u^2, 4u^2 with u = 2^-24;
+//   the reciprocal is one Newton-Raphson step r = t + t(1 - y t) from the FP32 reciprocal t.
+// Values below ~2^-100 lose low-part bits to FP32 underflow; the solver only needs them to
+// absolute accuracy.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+
+namespace sg {
+
+struct dw {
+  float hi, lo;
+};
+
+#define SG_HD __host__ __device__ __forceinline__
+
+SG_HD dw dw_make(float h, float l) { return dw{h, l}; }
+
+// Fast2Sum: exact s + t = a + b when |a| >= |b| (or a's exponent is at least b's)
+SG_HD dw fast2sum(float a, float b) {
+  const float s = a + b;
+  const float z = s - a;
+  return dw{s, b - z};
+}
+
+// 2Sum: exact s + t = a + b for any a, b
+SG_HD dw two_sum(float a, float b) {
+  const float s = a + b;
+  const float ap = s - b;
+  const float bp = s - ap;
+  const float da = a - ap;
+  const float db = b - bp;
+  return dw{s, da + db};
+}
+
+// Fast2Mult: exact p + e = a * b (FMA)
+SG_HD dw two_prod(float a, float b) {
+  const float p = a * b;
+  return dw{p, fmaf(a, b, -p)};
+}
+
+// AccurateDWPlusDW
+SG_HD dw dw_add(dw x, dw y) {
+  const dw s = two_sum(x.hi, y.hi);
+  const dw t = two_sum(x.lo, y.lo);
+  const float c = s.lo + t.hi;
+  const dw v = fast2sum(s.hi, c);
+  const float w = t.lo + v.lo;
+  return fast2sum(v.hi, w);
+}
+
+SG_HD dw dw_neg(dw x) { return dw{-x.hi, -x.lo}; }
+SG_HD dw dw_sub(dw x, dw y) { return dw_add(x, dw_neg(y)); }
+
+// DWPlusFP
+SG_HD dw dw_add_f(dw x, float y) {
+  const dw s = two_sum(x.hi, y);
+  const float v = x.lo + s.lo;
+  return fast2sum(s.hi, v);
+}
+
+// DWTimesFP3
+SG_HD dw dw_mul_f(dw x, float y) {
+  const dw c = two_prod(x.hi, y);
+  const float cl3 = fmaf(x.lo, y, c.lo);
+  return fast2sum(c.hi, cl3);
+}
+
+// DWTimesDW3
+SG_HD dw dw_mul(dw x, dw y) {
+  const dw c = two_prod(x.hi, y.hi);
+  const float tl0 = x.lo * y.lo;
+  const float tl1 = fmaf(x.hi, y.lo, tl0);
+  const float cl2 = fmaf(x.lo, y.hi, tl1);
+  const float cl3 = c.lo + cl2;
+  return fast2sum(c.hi, cl3);
+}
+
+// 1/y: FP32 reciprocal t, then r = t + t*(1 - y*t) with y*t formed in double-word
+SG_HD dw dw_rcp(dw y) {
+  const float t = 1.0f / y.hi;
+  const dw p = dw_mul_f(y, t);               // y*t ~ 1
+  const float e = (1.0f - p.hi) - p.lo;      // 1 - p.hi is exact (Sterbenz)
+  return fast2sum(t, t * e);
+}
+
+SG_HD dw dw_div(dw x, dw y) { return dw_mul(x, dw_rcp(y)); }
+
+SG_HD dw dw_abs(dw x) { return x.hi < 0.0f || (x.hi == 0.0f && x.lo < 0.0f) ? dw_neg(x) : x; }
+SG_HD dw dw_max0(dw x) { return x.hi > 0.0f ? x : dw{0.0f, 0.0f}; }
+SG_HD bool dw_gt0(dw x) { return x.hi > 0.0f; }
+
+// conversions (FP64 pipe: only at set-up and at the API boundary)
+SG_HD dw dw_from_double(double v) {
+  const float h = (float)v;
+  return dw{h, (float)(v - (double)h)};
+}
+SG_HD double dw_to_double(dw x) { return (double)x.hi + (double)x.lo; }
+
+#undef SG_HD
+
+}  // namespace sg

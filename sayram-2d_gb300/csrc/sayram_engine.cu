@@ -57,7 +57,8 @@ struct sayram_batch_s {
   long long nreal = 0;      // real cells (packed alpha-major size)
   int nchunks = 0, ntiles = 0;
   size_t bytes = 0;
-  bool mixed = false;
+  bool mixed = false;  // FP32 Krylov with (hi, lo) coefficients
+  bool dwm = false;    // double-word wide arithmetic (otherwise IEEE FP64)
 
   // device memory
   std::vector<void*> allocs;
@@ -171,8 +172,23 @@ struct sayram_batch_s {
   int run_steps(int nsteps);
   int read_ctl();
   int finish_status();
-  template <typename T, typename C>
+  template <typename T, typename C, typename A>
   int step_once(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, const sg::Kry<T>& kr);
+  // wide (8-byte) table entries: a double, or a (hi, lo) float pair in double-word mode
+  double wide(double v) const {
+    if (!dwm) return v;
+    const float h = (float)v, l = (float)(v - (double)h);
+    double out;
+    float pr[2] = {h, l};
+    std::memcpy(&out, pr, sizeof(out));
+    return out;
+  }
+  double unwide(double w) const {
+    if (!dwm) return w;
+    float pr[2];
+    std::memcpy(pr, &w, sizeof(pr));
+    return (double)pr[0] + (double)pr[1];
+  }
 };
 
 static int validate_problem(const sayram_problem& p) {
@@ -200,13 +216,14 @@ static int validate_problem(const sayram_problem& p) {
 int sayram_batch_s::build(const sayram_problem* probs, int count, const sayram_options* o) {
   sayram_default_options(&opt);
   if (o) opt = *o;
-  if (opt.precision != SAYRAM_FP64 && opt.precision != SAYRAM_FP32_REFINE)
+  if (opt.precision != SAYRAM_FP64 && opt.precision != SAYRAM_FP32_REFINE && opt.precision != SAYRAM_FP32_REFINE_DW)
     return fail(SAYRAM_ERR_ARG, "unknown precision");
   if (!(opt.tol > 0)) opt.tol = opt.precision == SAYRAM_FP64 ? 1e-12 : 1e-11;
   if (opt.inner_tol < 0) opt.inner_tol = 0;
   if (opt.max_iters < 1) opt.max_iters = 1;
   if (opt.max_refine < 2) opt.max_refine = 2;
-  mixed = opt.precision == SAYRAM_FP32_REFINE;
+  mixed = opt.precision != SAYRAM_FP64;
+  dwm = opt.precision == SAYRAM_FP32_REFINE_DW;
   for (int b = 0; b < count; ++b) {
     int rc = validate_problem(probs[b]);
     if (rc) return fail(rc, "instance " + std::to_string(b) + ": " + g_err);
@@ -317,19 +334,19 @@ int sayram_batch_s::build(const sayram_problem* probs, int count, const sayram_o
     for (int i = 1; i < p.nx; ++i) {
       const double xv = p.x_edges[i];
       const double xl = 0.5 * (p.x_edges[i - 1] + p.x_edges[i]), xr = 0.5 * (p.x_edges[i] + p.x_edges[i + 1]);
-      wx[2 * (I.xe + i)] = (xr - xv) / (xr - xl);
-      wx[2 * (I.xe + i) + 1] = (xv - xl) / (xr - xl);
+      wx[2 * (I.xe + i)] = wide((xr - xv) / (xr - xl));
+      wx[2 * (I.xe + i) + 1] = wide((xv - xl) / (xr - xl));
     }
     for (int j = 1; j < p.ny; ++j) {
       const double yv = p.y_edges[j];
       const double yb = 0.5 * (p.y_edges[j - 1] + p.y_edges[j]), yt = 0.5 * (p.y_edges[j] + p.y_edges[j + 1]);
-      wy[2 * (I.ye + j)] = (yt - yv) / (yt - yb);
-      wy[2 * (I.ye + j) + 1] = (yv - yb) / (yt - yb);
+      wy[2 * (I.ye + j)] = wide((yt - yv) / (yt - yb));
+      wy[2 * (I.ye + j) + 1] = wide((yv - yb) / (yt - yb));
     }
     for (int s = 0; s < 4; ++s)
       if (I.dir[s] >= 0) {
         const int m = (s <= 1) ? p.ny + 1 : p.nx + 1;
-        for (int k = 0; k < m; ++k) dirv[I.dir[s] + k] = p.dirichlet[s][k];
+        for (int k = 0; k < m; ++k) dirv[I.dir[s] + k] = wide(p.dirichlet[s][k]);
       }
     stage[b].nx = p.nx;
     stage[b].ny = p.ny;
@@ -377,7 +394,10 @@ int sayram_batch_s::upload_instance(int b, const sayram_problem& p, bool coeffs,
   if (coeffs && (mask & 31) != 31) return fail(SAYRAM_ERR_ARG, "all coefficient fields are required");
   const int threads = 256;
   const int blocks = (int)std::min<long long>((nc + threads - 1) / threads, (long long)nsm * 8);
-  sg::k_setup<<<blocks, threads, 0, stream>>>(cm, geo, fl.f, d_stage, d_xe, d_ye, b, mask);
+  if (dwm)
+    sg::k_setup<sg::DWA><<<blocks, threads, 0, stream>>>(cm, geo, fl.f, d_stage, d_xe, d_ye, b, mask);
+  else
+    sg::k_setup<sg::F64A><<<blocks, threads, 0, stream>>>(cm, geo, fl.f, d_stage, d_xe, d_ye, b, mask);
   SG_CUDA(cudaGetLastError());
   // the staging buffer is reused by the next upload: keep the stream ordered
   SG_CUDA(cudaStreamSynchronize(stream));
@@ -390,16 +410,16 @@ int sayram_batch_s::read_ctl() {
   return SAYRAM_OK;
 }
 
-template <typename T, typename C>
+template <typename T, typename C, typename A>
 int sayram_batch_s::step_once(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, const sg::Kry<T>& kr) {
   using namespace sg;
   const int gs = grid_stream(), gt = grid_tiles();
   SG_CUDA(cudaMemsetAsync(d_ctl, 0, 2 * sizeof(int), stream));
   launch("begin", [&] { k_begin<<<(n + 255) / 256, 256, 0, stream>>>(cm); });
-  launch("assemble", [&] { k_assemble<C><<<gt, kAsmThreads, 0, stream>>>(cm, geo, fl, cfull); });
+  launch("assemble", [&] { k_assemble<C, A><<<gt, kAsmThreads, 0, stream>>>(cm, geo, fl, cfull); });
   for (int o = 0; o < opt.max_refine; ++o) {
     launch("resid", [&] {
-      k_resid<T, C><<<gs, kThreads, 0, stream>>>(cm, fl, cfull, kr, opt.tol, opt.inner_tol, opt.max_refine);
+      k_resid<T, C, A><<<gs, kThreads, 0, stream>>>(cm, fl, cfull, kr, opt.tol, opt.inner_tol, opt.max_refine);
     });
     SG_CUDA(cudaGetLastError());
     if (o == opt.max_refine - 1) break;
@@ -418,7 +438,7 @@ int sayram_batch_s::step_once(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, c
       }
     }
   }
-  launch("polish", [&] { k_polish<C><<<gs, kThreads, 0, stream>>>(cm, fl, cfull); });
+  launch("polish", [&] { k_polish<C, A><<<gs, kThreads, 0, stream>>>(cm, fl, cfull); });
   SG_CUDA(cudaGetLastError());
   return SAYRAM_OK;
 }
@@ -427,7 +447,9 @@ int sayram_batch_s::run_steps(int nsteps) {
   if (nsteps < 0) return fail(SAYRAM_ERR_ARG, "nsteps must be >= 0");
   SG_CUDA(cudaSetDevice(dev));
   for (int s = 0; s < nsteps; ++s) {
-    int rc = mixed ? step_once<float, float>(c32, c32, k32) : step_once<double, double>(c64, c64, k64);
+    int rc = dwm ? step_once<float, float, sg::DWA>(c32, c32, k32)
+             : mixed ? step_once<float, float, sg::F64A>(c32, c32, k32)
+                     : step_once<double, double, sg::F64A>(c64, c64, k64);
     if (rc) return rc;
   }
   SG_CUDA(cudaStreamSynchronize(stream));
@@ -489,7 +511,7 @@ int sayram_batch_create(const sayram_problem* probs, int n, const sayram_options
   sayram_options o;
   sayram_default_options(&o);
   if (opt) o = *opt;
-  if (o.inner_tol < 0) o.inner_tol = (o.precision == SAYRAM_FP32_REFINE) ? 1e-4 : 0.0;
+  if (o.inner_tol < 0) o.inner_tol = (o.precision != SAYRAM_FP64) ? 1e-4 : 0.0;
   int rc = b->build(probs, n, &o);
   if (rc) {
     std::string msg = g_err;
@@ -514,14 +536,20 @@ int sayram_batch_step_host(sayram_batch b, int nsteps, const double* f_in, doubl
   if (f_in) {
     SG_CUDA(cudaMemcpyAsync(b->d_stage, f_in, sizeof(double) * b->nreal, cudaMemcpyHostToDevice, b->stream));
     b->launch("field_in", [&] {
-      sg::k_field_in<<<b->grid_tiles(), 256, 0, b->stream>>>(b->cm, b->fl.f, b->d_stage);
+      if (b->dwm)
+        sg::k_field_in<sg::DWA><<<b->grid_tiles(), 256, 0, b->stream>>>(b->cm, b->fl.f, b->d_stage);
+      else
+        sg::k_field_in<sg::F64A><<<b->grid_tiles(), 256, 0, b->stream>>>(b->cm, b->fl.f, b->d_stage);
     });
   }
   int rc = b->run_steps(nsteps);
   if (rc != SAYRAM_OK && rc != SAYRAM_ERR_NOT_CONVERGED && rc != SAYRAM_ERR_NEGATIVE) return rc;
   if (f_out) {
     b->launch("field_out", [&] {
-      sg::k_field_out<<<b->grid_tiles(), 256, 0, b->stream>>>(b->cm, b->d_stage, b->fl.f);
+      if (b->dwm)
+        sg::k_field_out<sg::DWA><<<b->grid_tiles(), 256, 0, b->stream>>>(b->cm, b->d_stage, b->fl.f);
+      else
+        sg::k_field_out<sg::F64A><<<b->grid_tiles(), 256, 0, b->stream>>>(b->cm, b->d_stage, b->fl.f);
     });
     SG_CUDA(cudaMemcpyAsync(f_out, b->d_stage, sizeof(double) * b->nreal, cudaMemcpyDeviceToHost, b->stream));
     SG_CUDA(cudaStreamSynchronize(b->stream));
@@ -539,7 +567,7 @@ int sayram_batch_get_f(sayram_batch b, int idx, double* f_out) {
   SG_CUDA(cudaMemcpyAsync(rows.data(), b->fl.f + I.base, sizeof(double) * rows.size(), cudaMemcpyDeviceToHost, b->stream));
   SG_CUDA(cudaStreamSynchronize(b->stream));
   for (int i = 0; i < I.nx; ++i)
-    for (int j = 0; j < I.ny; ++j) f_out[(size_t)i * I.ny + j] = rows[(size_t)j * I.pitch + i];
+    for (int j = 0; j < I.ny; ++j) f_out[(size_t)i * I.ny + j] = b->unwide(rows[(size_t)j * I.pitch + i]);
   return SAYRAM_OK;
 }
 
@@ -549,7 +577,7 @@ int sayram_batch_set_f(sayram_batch b, int idx, const double* f) {
   const InstDev& I = b->hinst[idx];
   std::vector<double> rows((size_t)I.ny * I.pitch, 0.0);
   for (int i = 0; i < I.nx; ++i)
-    for (int j = 0; j < I.ny; ++j) rows[(size_t)j * I.pitch + i] = f[(size_t)i * I.ny + j];
+    for (int j = 0; j < I.ny; ++j) rows[(size_t)j * I.pitch + i] = b->wide(f[(size_t)i * I.ny + j]);
   SG_CUDA(cudaMemcpyAsync(b->fl.f + I.base, rows.data(), sizeof(double) * rows.size(), cudaMemcpyHostToDevice, b->stream));
   SG_CUDA(cudaStreamSynchronize(b->stream));
   return SAYRAM_OK;
@@ -563,7 +591,9 @@ int sayram_batch_set_dirichlet(sayram_batch b, int idx, int side, const double* 
   const int m = (side <= 1) ? I.ny + 1 : I.nx + 1;
   if (n != m) return fail(SAYRAM_ERR_ARG, "expected " + std::to_string(m) + " vertex values");
   SG_CUDA(cudaSetDevice(b->dev));
-  SG_CUDA(cudaMemcpyAsync(b->d_dirv + I.dir[side], v, sizeof(double) * m, cudaMemcpyHostToDevice, b->stream));
+  std::vector<double> wv(m);
+  for (int k = 0; k < m; ++k) wv[k] = b->wide(v[k]);
+  SG_CUDA(cudaMemcpyAsync(b->d_dirv + I.dir[side], wv.data(), sizeof(double) * m, cudaMemcpyHostToDevice, b->stream));
   SG_CUDA(cudaStreamSynchronize(b->stream));
   return SAYRAM_OK;
 }
@@ -616,10 +646,12 @@ int sayram_batch_export_system(sayram_batch b, int idx, double* M5, double* R) {
   if (!b || !M5 || !R || idx < 0 || idx >= b->n) return fail(SAYRAM_ERR_ARG, "bad handle, index or buffer");
   SG_CUDA(cudaSetDevice(b->dev));
   const InstDev& I = b->hinst[idx];
-  if (b->mixed)
-    sg::k_assemble<float><<<b->grid_tiles(), sg::kAsmThreads, 0, b->stream>>>(b->cm, b->geo, b->fl, b->c32);
+  if (b->dwm)
+    sg::k_assemble<float, sg::DWA><<<b->grid_tiles(), sg::kAsmThreads, 0, b->stream>>>(b->cm, b->geo, b->fl, b->c32);
+  else if (b->mixed)
+    sg::k_assemble<float, sg::F64A><<<b->grid_tiles(), sg::kAsmThreads, 0, b->stream>>>(b->cm, b->geo, b->fl, b->c32);
   else
-    sg::k_assemble<double><<<b->grid_tiles(), sg::kAsmThreads, 0, b->stream>>>(b->cm, b->geo, b->fl, b->c64);
+    sg::k_assemble<double, sg::F64A><<<b->grid_tiles(), sg::kAsmThreads, 0, b->stream>>>(b->cm, b->geo, b->fl, b->c64);
   SG_CUDA(cudaGetLastError());
   const size_t rows = (size_t)I.ny * I.pitch;
   std::vector<double> invD(rows), Rr(rows), c[4];
@@ -643,7 +675,7 @@ int sayram_batch_export_system(sayram_batch b, int idx, double* M5, double* R) {
   SG_CUDA(cudaStreamSynchronize(b->stream));
   const int nx = I.nx, ny = I.ny, P = I.pitch;
   const size_t N = (size_t)nx * ny;
-  auto Dof = [&](int i, int j) { return 1.0 / invD[(size_t)j * P + i]; };
+  auto Dof = [&](int i, int j) { return 1.0 / b->unwide(invD[(size_t)j * P + i]); };
   for (int j = 0; j < ny; ++j)
     for (int i = 0; i < nx; ++i) {
       const size_t K = (size_t)j * nx + i, q = (size_t)j * P + i;
@@ -652,7 +684,7 @@ int sayram_batch_export_system(sayram_batch b, int idx, double* M5, double* R) {
       M5[2 * N + K] = i < nx - 1 ? -c[1][q] * Dof(i + 1, j) : 0.0;
       M5[3 * N + K] = j > 0 ? -c[2][q] * Dof(i, j - 1) : 0.0;
       M5[4 * N + K] = j < ny - 1 ? -c[3][q] * Dof(i, j + 1) : 0.0;
-      R[K] = Rr[q];
+      R[K] = b->unwide(Rr[q]);
     }
   return SAYRAM_OK;
 }
@@ -711,7 +743,7 @@ void sayram_batch_destroy(sayram_batch b) { delete b; }
 size_t sayram_instance_bytes(int nx, int ny, int precision) {
   const long long pitch = round_up(nx, 4);
   const long long cells = round_up((long long)(ny + 2) * pitch, 32);
-  const long long per = 14 * 8 + (precision == SAYRAM_FP32_REFINE ? 8 * 4 + 8 * 4 : 4 * 8 + 8 * 8) + 8;
+  const long long per = 14 * 8 + (precision != SAYRAM_FP64 ? 8 * 4 + 8 * 4 : 4 * 8 + 8 * 8) + 8;
   return (size_t)(cells * per + 4096);
 }
 
@@ -970,15 +1002,15 @@ extern "C" int sayram_step_noalloc(const sayram_problem* pd, const sayram_option
   SG_CUDA(cudaGetLastError());
   const int gt = std::max(1, std::min(cm.ntiles, nsm * 8));
   const int gs = std::max(1, std::min(cm.nchunks, nsm * 16));
-  k_field_in<<<gt, 256, 0, stream>>>(cm, fl.f, f_in);
+  k_field_in<F64A><<<gt, 256, 0, stream>>>(cm, fl.f, f_in);
   SG_CUDA(cudaGetLastError());
   Ctl hctl;
   for (int s = 0; s < nsteps; ++s) {
     SG_CUDA(cudaMemsetAsync(d_ctl, 0, 2 * sizeof(int), stream));
     k_begin<<<1, 32, 0, stream>>>(cm);
-    k_assemble<double><<<gt, kAsmThreads, 0, stream>>>(cm, geo, fl, co);
+    k_assemble<double, F64A><<<gt, kAsmThreads, 0, stream>>>(cm, geo, fl, co);
     for (int r = 0; r < o.max_refine; ++r) {
-      k_resid<double, double><<<gs, kThreads, 0, stream>>>(cm, fl, co, kr, o.tol, o.inner_tol, o.max_refine);
+      k_resid<double, double, F64A><<<gs, kThreads, 0, stream>>>(cm, fl, co, kr, o.tol, o.inner_tol, o.max_refine);
       SG_CUDA(cudaGetLastError());
       if (r == o.max_refine - 1) break;
       SG_CUDA(cudaMemcpyAsync(&hctl, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, stream));
@@ -996,10 +1028,10 @@ extern "C" int sayram_step_noalloc(const sayram_problem* pd, const sayram_option
         }
       }
     }
-    k_polish<double><<<gs, kThreads, 0, stream>>>(cm, fl, co);
+    k_polish<double, F64A><<<gs, kThreads, 0, stream>>>(cm, fl, co);
     SG_CUDA(cudaGetLastError());
   }
-  k_field_out<<<gt, 256, 0, stream>>>(cm, f_out, fl.f);
+  k_field_out<F64A><<<gt, 256, 0, stream>>>(cm, f_out, fl.f);
   SG_CUDA(cudaGetLastError());
   InstState hs;
   SG_CUDA(cudaMemcpyAsync(&hs, d_st, sizeof(hs), cudaMemcpyDeviceToHost, stream));

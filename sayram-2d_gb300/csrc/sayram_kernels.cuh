@@ -60,7 +60,8 @@ struct InstState {
   long long cum_iters, cum_refines;  // totals since creation (work accounting)
   int ycur, pcur, outer_active, inner_active;
   int restart, fresh, has_x, iters;
-  int iters_total, refines, status, pad_i;
+  int iters_total, refines, status;
+  unsigned int rmax_bits;  // bits of max |R| over the instance (non-negative float; atomicMax order)
   unsigned int cnt[PH_COUNT];
 };
 
@@ -116,6 +117,28 @@ __device__ __forceinline__ void block_sum(T (&v)[NQ], double (&out)[NQ]) {
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
       double x = lane < nw ? sm[q][lane] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+      out[q] = x;
+    }
+  }
+  __syncthreads();
+}
+
+// Sum over the block of per-warp totals held in lane 0 of each warp (result in thread 0).
+template <int NQ>
+__device__ __forceinline__ void block_sum_lane0(const double (&w)[NQ], double (&out)[NQ]) {
+  __shared__ double sm0[NQ][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) sm0[q][warp] = w[q];
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      double x = lane < nw ? sm0[q][lane] : 0.0;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
       out[q] = x;

@@ -3,12 +3,19 @@
 //   k_setup      once per instance: coefficients -> per-cell face factors, UKK, loss diagonal
 //   k_begin      per step: resets the per-instance solver state
 //   k_assemble   fused vertex interpolation + PPFV face fluxes + diagonal/RHS + Jacobi scaling
-//   k_resid      FP64 true residual r = R - A~ y (adds the last Krylov correction first)
+//   k_resid      outer residual r = R - A~ y (adds the last Krylov correction first)
 //   k_bicg1/2/3  one BiCGSTAB iteration in T precision (FP64 or FP32) with fused SpMV + dots
 //   k_polish     positivity polish y' = R + (I - A~) y+, f = y'/D, min / clamp / mass checks
-//   k_field_*    alpha-major <-> padded system order copies for get_f / set_f
+//   k_field_*    alpha-major FP64 <-> padded system order copies for get_f / set_f
+//
+// The assembly, residual, polish and state are written once over an arithmetic policy A:
+//   F64A  IEEE binary64 (the FP64 drop-in and the FP32 + FP64-residual mode)
+//   DWA   double-word pairs of FP32 (dword.cuh): FP64-class accuracy on the FP32 pipes
+// Per-cell "wide" arrays (f, 1/D, R, column sums, y, the face factors, the weights and Dirichlet
+// values) hold 8 bytes per entry in both: one double, or one (hi, lo) float pair.
 #pragma once
 
+#include "dword.cuh"
 #include "sayram_kernels.cuh"
 
 namespace sg {
@@ -44,7 +51,7 @@ struct Fields {
   double* invD;    // 1 / diag(M)
   double* R;       // right-hand side
   double* colsum;  // 1^T M per column (conservation check)
-  double* y64[2];  // FP64 scaled solution y = D f (ping-pong)
+  double* y64[2];  // scaled solution y = D f (ping-pong)
 };
 
 template <typename T>
@@ -52,6 +59,117 @@ struct Kry {
   T *r, *rh, *t, *x;
   T *p[2], *v[2];
 };
+
+// ------------------------------------------------------------------------------ arithmetic
+struct F64A {
+  using V = double;
+  __device__ static V ld(const double* p, long long i) { return p[i]; }
+  __device__ static void st(double* p, long long i, V v) { p[i] = v; }
+  __device__ static Q4<V> ld4(const double* p) { return sg::ld4(p); }
+  __device__ static void st4(double* p, const Q4<V>& q) { sg::st4(p, q); }
+  __device__ static V add(V a, V b) { return a + b; }
+  __device__ static V sub(V a, V b) { return a - b; }
+  __device__ static V mul(V a, V b) { return a * b; }
+  __device__ static V fma(V a, V b, V c) { return a * b + c; }
+  __device__ static V addf(V a, float b) { return a + (double)b; }
+  __device__ static V rcp(V a) { return 1.0 / a; }
+  __device__ static V div(V a, V b) { return a / b; }
+  __device__ static V abs(V a) { return fabs(a); }
+  __device__ static V max0(V a) { return fmax(a, 0.0); }
+  __device__ static V k(double c) { return c; }
+  __device__ static bool lt0(V a) { return a < 0.0; }
+  __device__ static float f32(V a) { return (float)a; }
+  __device__ static float sq32(V a) { return (float)(a * a); }
+  __device__ static double to_d(V a) { return a; }
+  __device__ static V from_d(double a) { return a; }
+  __device__ static void split(V a, float& hi, float& lo) {
+    hi = __double2float_rn(a);
+    lo = __double2float_rn(a - (double)hi);
+  }
+  __device__ static V hilo(float hi, float lo) { return (double)hi + (double)lo; }
+  // r * s for a power-of-two s, in the Krylov precision T
+  template <typename T>
+  __device__ static T scaled(V a, float s) { return (T)(a * (double)s); }
+  // y + x*s for the FP32/FP64 Krylov correction x in scaled units
+  template <typename T>
+  __device__ static V add_scaled(V y, T x, float s) { return y + (double)x * (double)s; }
+  using Acc = double;  // per-thread accumulator of scaled squares
+  __device__ static Acc sq_scaled(V a, float s) { const double t = a * (double)s; return t * t; }
+  __device__ static double warp_total(Acc a) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    return a;
+  }
+  __device__ static double warp_total_v(V a) { return warp_total(a); }
+};
+
+struct DWA {
+  using V = dw;
+  __device__ static V ld(const double* p, long long i) {
+    const float2 q = reinterpret_cast<const float2*>(p)[i];
+    return dw{q.x, q.y};
+  }
+  __device__ static void st(double* p, long long i, V v) { reinterpret_cast<float2*>(p)[i] = make_float2(v.hi, v.lo); }
+  __device__ static Q4<V> ld4(const double* p) {
+    const float4 a = reinterpret_cast<const float4*>(p)[0];
+    const float4 b = reinterpret_cast<const float4*>(p)[1];
+    return Q4<V>{{dw{a.x, a.y}, dw{a.z, a.w}, dw{b.x, b.y}, dw{b.z, b.w}}};
+  }
+  __device__ static void st4(double* p, const Q4<V>& q) {
+    reinterpret_cast<float4*>(p)[0] = make_float4(q.a[0].hi, q.a[0].lo, q.a[1].hi, q.a[1].lo);
+    reinterpret_cast<float4*>(p)[1] = make_float4(q.a[2].hi, q.a[2].lo, q.a[3].hi, q.a[3].lo);
+  }
+  __device__ static V add(V a, V b) { return dw_add(a, b); }
+  __device__ static V sub(V a, V b) { return dw_sub(a, b); }
+  __device__ static V mul(V a, V b) { return dw_mul(a, b); }
+  __device__ static V fma(V a, V b, V c) { return dw_add(dw_mul(a, b), c); }
+  __device__ static V addf(V a, float b) { return dw_add_f(a, b); }
+  __device__ static V rcp(V a) { return dw_rcp(a); }
+  __device__ static V div(V a, V b) { return dw_div(a, b); }
+  __device__ static V abs(V a) { return dw_abs(a); }
+  __device__ static V max0(V a) { return dw_max0(a); }
+  __device__ static V k(double c) { return dw_from_double(c); }
+  __device__ static bool lt0(V a) { return a.hi < 0.0f; }
+  __device__ static float f32(V a) { return a.hi; }
+  __device__ static float sq32(V a) { return a.hi * a.hi; }
+  __device__ static double to_d(V a) { return dw_to_double(a); }
+  __device__ static V from_d(double a) { return dw_from_double(a); }
+  __device__ static void split(V a, float& hi, float& lo) {
+    hi = a.hi;
+    lo = a.lo;
+  }
+  __device__ static V hilo(float hi, float lo) { return dw{hi, lo}; }
+  template <typename T>
+  __device__ static T scaled(V a, float s) { return (T)(a.hi * s); }
+  template <typename T>
+  __device__ static V add_scaled(V y, T x, float s) { return dw_add_f(y, (float)x * s); }
+  using Acc = float;
+  __device__ static Acc sq_scaled(V a, float s) { const float t = a.hi * s; return t * t; }
+  __device__ static double warp_total(Acc a) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    return (double)a;
+  }
+  __device__ static double warp_total_v(V a) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const dw b{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)};
+      a = dw_add(a, b);
+    }
+    return dw_to_double(a);
+  }
+};
+
+// Power-of-two scale of an instance's refinement system: 2^-e with max|R| = m * 2^e, m in
+// [0.5, 1). Residuals are handed to the Krylov solver as r * scale, so its vectors and dot
+// products stay O(1) or below whatever the magnitude of f (no FP32 underflow).
+__device__ __forceinline__ float rhs_scale(unsigned int rmax_bits) {
+  const float m = __uint_as_float(rmax_bits);
+  if (!(m > 0.0f) || !isfinite(m)) return 1.0f;
+  int e;
+  frexpf(m, &e);
+  return ldexpf(1.0f, -e);
+}
 
 // ------------------------------------------------------------------------------ setup
 // Face factors of cell (i,j) from the reference's general formula (Solver.cc:68-97) evaluated on
@@ -73,8 +191,10 @@ __device__ __forceinline__ void face_pair(double Kx, double Ky, double Ax, doubl
                   __dadd_rn(__dmul_rn(vkb0, rvka0), __dmul_rn(vkb1, rvka1)));
 }
 
-// One instance: stage holds alpha-major G, Dxx, Dxy, Dyy, inv_tau, f0 (each nx*ny; a NULL
-// section is skipped by passing has mask bits). Writes the face factors (and f if bit 5 set).
+// One instance: stage holds alpha-major G, Dxx, Dxy, Dyy, inv_tau, f0 (each nx*ny). mask bits
+// 0-4 select the coefficient sections (all five together), bit 5 the initial state. Values are
+// computed in FP64 and stored in the policy's wide format.
+template <typename A>
 __global__ void k_setup(Common cm, Geo geo, double* f, const double* stage, const double* xe,
                         const double* ye, int b, int mask) {
   const InstDev I = cm.inst[b];
@@ -99,23 +219,24 @@ __global__ void k_setup(Common cm, Geo geo, double* f, const double* stage, cons
                            __dmul_rn(Dyy[c], g)};
       double aa, ab;
       face_pair(Kx, Ky, xl, yt, xl, yb, -1.0, 0.0, L, &aa, &ab);  // XNEG: A=(i,j+1) B=(i,j)
-      geo.aAx[K] = aa;
-      geo.aBx[K] = ab;
-      geo.Sx[K] = __dadd_rn(aa, ab);
+      A::st(geo.aAx, K, A::from_d(aa));
+      A::st(geo.aBx, K, A::from_d(ab));
+      A::st(geo.Sx, K, A::from_d(__dadd_rn(aa, ab)));
       face_pair(Kx, Ky, xl, yb, xr, yb, 0.0, -1.0, L, &aa, &ab);  // YNEG: A=(i,j) B=(i+1,j)
-      geo.aAy[K] = aa;
-      geo.aBy[K] = ab;
-      geo.Sy[K] = __dadd_rn(aa, ab);
+      A::st(geo.aAy, K, A::from_d(aa));
+      A::st(geo.aBy, K, A::from_d(ab));
+      A::st(geo.Sy, K, A::from_d(__dadd_rn(aa, ab)));
       // UKK = G * (dx*dy/dt); diagonal UKK*(1 + dt/tau) (Solver.cc:190-199, Mesh.h:61-63)
       const double ukk = __dmul_rn(g, __ddiv_rn(__dmul_rn(dx, dy), I.dt));
-      geo.ukk[K] = ukk;
-      geo.sdiag[K] = __dmul_rn(ukk, __dadd_rn(1.0, __dmul_rn(I.dt, itau[c])));
+      A::st(geo.ukk, K, A::from_d(ukk));
+      A::st(geo.sdiag, K, A::from_d(__dmul_rn(ukk, __dadd_rn(1.0, __dmul_rn(I.dt, itau[c])))));
     }
-    if (mask & 32) f[K] = f0[c];
+    if (mask & 32) A::st(f, K, A::from_d(f0[c]));
   }
 }
 
-// alpha-major (packed at hoff) -> padded system order, for every enabled instance (tile grid)
+// alpha-major FP64 (packed at hoff) -> padded system order in the wide format (tile grid)
+template <typename A>
 __global__ void k_field_in(Common cm, double* dst, const double* src) {
   count_launch(cm.ctl);
   for (int t = blockIdx.x; t < cm.ntiles; t += gridDim.x) {
@@ -125,11 +246,13 @@ __global__ void k_field_in(Common cm, double* dst, const double* src) {
     const int lt = t - I.tile0, i0 = (lt % I.ntx) * kTX, j0 = (lt / I.ntx) * kTY;
     for (int q = threadIdx.x; q < kTX * kTY; q += blockDim.x) {
       const int i = i0 + (q / kTY), j = j0 + (q % kTY);  // j fastest: reads contiguous in j
-      if (i < I.nx && j < I.ny) dst[I.base + (long long)j * I.pitch + i] = src[I.hoff + (long long)i * I.ny + j];
+      if (i < I.nx && j < I.ny)
+        A::st(dst, I.base + (long long)j * I.pitch + i, A::from_d(src[I.hoff + (long long)i * I.ny + j]));
     }
   }
 }
 
+template <typename A>
 __global__ void k_field_out(Common cm, double* dst, const double* src) {
   count_launch(cm.ctl);
   for (int t = blockIdx.x; t < cm.ntiles; t += gridDim.x) {
@@ -139,7 +262,8 @@ __global__ void k_field_out(Common cm, double* dst, const double* src) {
     const int lt = t - I.tile0, i0 = (lt % I.ntx) * kTX, j0 = (lt / I.ntx) * kTY;
     for (int q = threadIdx.x; q < kTX * kTY; q += blockDim.x) {
       const int i = i0 + (q / kTY), j = j0 + (q % kTY);
-      if (i < I.nx && j < I.ny) dst[I.hoff + (long long)i * I.ny + j] = src[I.base + (long long)j * I.pitch + i];
+      if (i < I.nx && j < I.ny)
+        dst[I.hoff + (long long)i * I.ny + j] = A::to_d(A::ld(src, I.base + (long long)j * I.pitch + i));
     }
   }
 }
@@ -159,25 +283,26 @@ __global__ void k_begin(Common cm) {
     s.iters_total = 0;
     s.refines = 0;
     s.clamped = 0;
+    s.rmax_bits = 0u;
     if (on) atomicAdd(&cm.ctl->n_outer, 1);
   }
 }
 
 // ------------------------------------------------------------------------------ assembly
-template <typename C>
+template <typename C, typename A>
 struct AsmOut;
-template <>
-struct AsmOut<double> {
-  __device__ static void put(const Coef<double>& c, int which, long long idx, double v) {
+template <typename A>
+struct AsmOut<double, A> {
+  __device__ static void put(const Coef<double>& c, int which, long long idx, typename A::V v) {
     double* a = which == 0 ? c.cw : which == 1 ? c.ce : which == 2 ? c.cs : c.cn;
-    a[idx] = v;
+    a[idx] = A::to_d(v);
   }
 };
-template <>
-struct AsmOut<float> {
-  __device__ static void put(const Coef<float>& c, int which, long long idx, double v) {
-    const float hi = __double2float_rn(v);
-    const float lo = __double2float_rn(v - (double)hi);
+template <typename A>
+struct AsmOut<float, A> {
+  __device__ static void put(const Coef<float>& c, int which, long long idx, typename A::V v) {
+    float hi, lo;
+    A::split(v, hi, lo);
     float* a = which == 0 ? c.cw : which == 1 ? c.ce : which == 2 ? c.cs : c.cn;
     float* l = which == 0 ? c.lw : which == 1 ? c.le : which == 2 ? c.ls : c.ln;
     a[idx] = hi;
@@ -187,36 +312,43 @@ struct AsmOut<float> {
 
 // Inner face (Solver.cc:99-141, calculate_mu Solver.h:63-67). K and L one-sided data:
 // a_sigma = aA*fA + aB*fB, S = aA + aB, inv = 1/(f + eps).
-__device__ __forceinline__ void inner_face(double aK, double SK, double invK, double aL, double SL,
-                                           double invL, double* AK, double* AL) {
-  const double absK = fabs(aK), absL = fabs(aL);
-  const double denom = absK + absL + 2 * kEps;
-  const double muK = (absL + kEps) / denom;
-  const double muL = 1 - muK;
-  const double B = muL * aL - muK * aK;
-  const double Bp = fmax(B, 0.0);   // (|B| + B) / 2
-  const double Bm = fmax(-B, 0.0);  // (|B| - B) / 2
-  *AK = muK * SK + Bp * invK;
-  *AL = muL * SL + Bm * invL;
+template <typename A>
+__device__ __forceinline__ void inner_face(typename A::V aK, typename A::V SK, typename A::V invK,
+                                           typename A::V aL, typename A::V SL, typename A::V invL,
+                                           typename A::V* AK, typename A::V* AL) {
+  using V = typename A::V;
+  const V absK = A::abs(aK), absL = A::abs(aL);
+  const V denom = A::add(A::add(absK, absL), A::k(2 * kEps));
+  const V muK = A::div(A::add(absL, A::k(kEps)), denom);
+  const V muL = A::sub(A::k(1.0), muK);
+  const V B = A::sub(A::mul(muL, aL), A::mul(muK, aK));
+  const V Bp = A::max0(B);             // (|B| + B) / 2
+  const V Bm = A::max0(A::sub(A::k(0.0), B));  // (|B| - B) / 2
+  *AK = A::fma(Bp, invK, A::mul(muK, SK));
+  *AL = A::fma(Bm, invL, A::mul(muL, SL));
 }
 
 // Dirichlet face (Solver.cc:143-164): B = -a_sigma; A = S + B+/(f+eps); R += B-.
-__device__ __forceinline__ void dirichlet_face(double aK, double SK, double invK, double* A, double* Bm) {
-  *A = SK + fmax(-aK, 0.0) * invK;
-  *Bm = fmax(aK, 0.0);
+template <typename A>
+__device__ __forceinline__ void dirichlet_face(typename A::V aK, typename A::V SK, typename A::V invK,
+                                               typename A::V* Aout, typename A::V* Bm) {
+  *Aout = A::fma(A::max0(A::sub(A::k(0.0), aK)), invK, SK);
+  *Bm = A::max0(aK);
 }
 
 // One tile of kTX x kTY cells per iteration; vertices and faces are computed once per tile
 // (plus a one-cell halo), in shared memory.
-template <typename C>
+template <typename C, typename A>
 __global__ void __launch_bounds__(kAsmThreads) k_assemble(Common cm, Geo geo, Fields fl, Coef<C> co) {
+  using V = typename A::V;
   count_launch(cm.ctl);
   constexpr int HX = kTX + 2, HY = kTY + 2, VX = kTX + 1, VY = kTY + 1;
-  __shared__ double fS[HY][HX];
-  __shared__ double iS[HY][HX];
-  __shared__ double vS[VY][VX];
-  __shared__ double xL[kTY][VX], xR[kTY][VX], xB[kTY][VX];  // x-faces: left/right outflow, R part
-  __shared__ double yB[VY][kTX], yT[VY][kTX], yR[VY][kTX];  // y-faces: below/above outflow, R part
+  __shared__ V fS[HY][HX];
+  __shared__ V iS[HY][HX];
+  __shared__ V vS[VY][VX];
+  __shared__ V xL[kTY][VX], xR[kTY][VX], xB[kTY][VX];  // x-faces: left/right outflow, R part
+  __shared__ V yB[VY][kTX], yT[VY][kTX], yR[VY][kTX];  // y-faces: below/above outflow, R part
+  const V zero = A::k(0.0);
   for (int t = blockIdx.x; t < cm.ntiles; t += gridDim.x) {
     const int b = cm.tile_inst[t];
     const InstDev I = cm.inst[b];
@@ -229,10 +361,10 @@ __global__ void __launch_bounds__(kAsmThreads) k_assemble(Common cm, Geo geo, Fi
     for (int q = threadIdx.x; q < HX * HY; q += blockDim.x) {
       const int hx = q % HX, hy = q / HX;
       const int i = i0 + hx - 1, j = j0 + hy - 1;
-      double fv = 0.0, iv = 0.0;
+      V fv = zero, iv = zero;
       if (i >= 0 && i < nx && j >= 0 && j < ny) {
-        fv = fl.f[base + (long long)j * P + i];
-        iv = 1.0 / (fv + kEps);
+        fv = A::ld(fl.f, base + (long long)j * P + i);
+        iv = A::rcp(A::add(fv, A::k(kEps)));
       }
       fS[hy][hx] = fv;
       iS[hy][hx] = iv;
@@ -244,28 +376,28 @@ __global__ void __launch_bounds__(kAsmThreads) k_assemble(Common cm, Geo geo, Fi
       const int vx = q % VX, vy = q / VX;
       const int Iv = i0 + vx, Jv = j0 + vy;
       if (Iv > nx || Jv > ny) continue;
-      double val;
-      if (Jv == ny && I.bc[YMAX] == DIRICHLET) val = cm.dirv[I.dir[YMAX] + Iv];
-      else if (Jv == 0 && I.bc[YMIN] == DIRICHLET) val = cm.dirv[I.dir[YMIN] + Iv];
-      else if (Iv == nx && I.bc[XMAX] == DIRICHLET) val = cm.dirv[I.dir[XMAX] + Jv];
-      else if (Iv == 0 && I.bc[XMIN] == DIRICHLET) val = cm.dirv[I.dir[XMIN] + Jv];
+      V val;
+      if (Jv == ny && I.bc[YMAX] == DIRICHLET) val = A::ld(cm.dirv, I.dir[YMAX] + Iv);
+      else if (Jv == 0 && I.bc[YMIN] == DIRICHLET) val = A::ld(cm.dirv, I.dir[YMIN] + Iv);
+      else if (Iv == nx && I.bc[XMAX] == DIRICHLET) val = A::ld(cm.dirv, I.dir[XMAX] + Jv);
+      else if (Iv == 0 && I.bc[XMIN] == DIRICHLET) val = A::ld(cm.dirv, I.dir[XMIN] + Jv);
       else {
         // cells around vertex (Iv, Jv) are (Iv-1|Iv, Jv-1|Jv); clamp to the domain at edges
         const int ci0 = Iv > 0 ? Iv - 1 : 0, ci1 = Iv < nx ? Iv : nx - 1;
         const int cj0 = Jv > 0 ? Jv - 1 : 0, cj1 = Jv < ny ? Jv : ny - 1;
-        const double f00 = fS[cj0 - j0 + 1][ci0 - i0 + 1], f10 = fS[cj0 - j0 + 1][ci1 - i0 + 1];
-        const double f01 = fS[cj1 - j0 + 1][ci0 - i0 + 1], f11 = fS[cj1 - j0 + 1][ci1 - i0 + 1];
+        const V f00 = fS[cj0 - j0 + 1][ci0 - i0 + 1], f10 = fS[cj0 - j0 + 1][ci1 - i0 + 1];
+        const V f01 = fS[cj1 - j0 + 1][ci0 - i0 + 1], f11 = fS[cj1 - j0 + 1][ci1 - i0 + 1];
         const bool xin = Iv > 0 && Iv < nx, yin = Jv > 0 && Jv < ny;
         if (xin && yin) {
-          const double wL = cm.wx[2 * (I.xe + Iv)], wR = cm.wx[2 * (I.xe + Iv) + 1];
-          const double wB = cm.wy[2 * (I.ye + Jv)], wT = cm.wy[2 * (I.ye + Jv) + 1];
-          val = wB * (wL * f00 + wR * f10) + wT * (wL * f01 + wR * f11);
+          const V wL = A::ld(cm.wx, 2 * (I.xe + Iv)), wR = A::ld(cm.wx, 2 * (I.xe + Iv) + 1);
+          const V wB = A::ld(cm.wy, 2 * (I.ye + Jv)), wT = A::ld(cm.wy, 2 * (I.ye + Jv) + 1);
+          val = A::fma(wB, A::fma(wL, f00, A::mul(wR, f10)), A::mul(wT, A::fma(wL, f01, A::mul(wR, f11))));
         } else if (yin) {  // vertical boundary edge: linear in y
-          const double wB = cm.wy[2 * (I.ye + Jv)], wT = cm.wy[2 * (I.ye + Jv) + 1];
-          val = wB * f00 + wT * f01;
+          const V wB = A::ld(cm.wy, 2 * (I.ye + Jv)), wT = A::ld(cm.wy, 2 * (I.ye + Jv) + 1);
+          val = A::fma(wB, f00, A::mul(wT, f01));
         } else if (xin) {  // horizontal boundary edge: linear in x
-          const double wL = cm.wx[2 * (I.xe + Iv)], wR = cm.wx[2 * (I.xe + Iv) + 1];
-          val = wL * f00 + wR * f10;
+          const V wL = A::ld(cm.wx, 2 * (I.xe + Iv)), wR = A::ld(cm.wx, 2 * (I.xe + Iv) + 1);
+          val = A::fma(wL, f00, A::mul(wR, f10));
         } else {
           val = f00;  // corner: the single adjacent cell
         }
@@ -277,21 +409,23 @@ __global__ void __launch_bounds__(kAsmThreads) k_assemble(Common cm, Geo geo, Fi
     for (int q = threadIdx.x; q < kTY * VX; q += blockDim.x) {
       const int vx = q % VX, ry = q / VX;
       const int Iv = i0 + vx, j = j0 + ry;
-      double aL = 0.0, aR = 0.0, bm = 0.0;
+      V aL = zero, aR = zero, bm = zero;
       if (j < ny && Iv <= nx) {
-        const double vLo = vS[ry][vx], vHi = vS[ry + 1][vx];  // vertices (Iv, j), (Iv, j+1)
+        const V vLo = vS[ry][vx], vHi = vS[ry + 1][vx];  // vertices (Iv, j), (Iv, j+1)
         if (Iv > 0 && Iv < nx) {
           const long long K = base + (long long)j * P + Iv, L = K - 1;
           // K's XNEG edge: A=(Iv, j+1), B=(Iv, j); L's XPOS edge: A=(Iv, j), B=(Iv, j+1)
-          const double aK = geo.aAx[K] * vHi + geo.aBx[K] * vLo;
-          const double aLs = geo.aAx[L] * vLo + geo.aBx[L] * vHi;
-          inner_face(aK, geo.Sx[K], iS[ry + 1][vx + 1], aLs, geo.Sx[L], iS[ry + 1][vx], &aR, &aL);
+          const V aK = A::fma(A::ld(geo.aAx, K), vHi, A::mul(A::ld(geo.aBx, K), vLo));
+          const V aLs = A::fma(A::ld(geo.aAx, L), vLo, A::mul(A::ld(geo.aBx, L), vHi));
+          inner_face<A>(aK, A::ld(geo.Sx, K), iS[ry + 1][vx + 1], aLs, A::ld(geo.Sx, L), iS[ry + 1][vx], &aR, &aL);
         } else if (Iv == 0 && I.bc[XMIN] == DIRICHLET) {
           const long long K = base + (long long)j * P;
-          dirichlet_face(geo.aAx[K] * vHi + geo.aBx[K] * vLo, geo.Sx[K], iS[ry + 1][vx + 1], &aR, &bm);
+          dirichlet_face<A>(A::fma(A::ld(geo.aAx, K), vHi, A::mul(A::ld(geo.aBx, K), vLo)), A::ld(geo.Sx, K),
+                            iS[ry + 1][vx + 1], &aR, &bm);
         } else if (Iv == nx && I.bc[XMAX] == DIRICHLET) {
           const long long K = base + (long long)j * P + nx - 1;  // XPOS edge: A=(nx, j), B=(nx, j+1)
-          dirichlet_face(geo.aAx[K] * vLo + geo.aBx[K] * vHi, geo.Sx[K], iS[ry + 1][vx], &aL, &bm);
+          dirichlet_face<A>(A::fma(A::ld(geo.aAx, K), vLo, A::mul(A::ld(geo.aBx, K), vHi)), A::ld(geo.Sx, K),
+                            iS[ry + 1][vx], &aL, &bm);
         }
       }
       xL[ry][vx] = aL;
@@ -302,21 +436,23 @@ __global__ void __launch_bounds__(kAsmThreads) k_assemble(Common cm, Geo geo, Fi
     for (int q = threadIdx.x; q < VY * kTX; q += blockDim.x) {
       const int cx = q % kTX, vy = q / kTX;
       const int i = i0 + cx, Jv = j0 + vy;
-      double aB = 0.0, aT = 0.0, bm = 0.0;
+      V aB = zero, aT = zero, bm = zero;
       if (i < nx && Jv <= ny) {
-        const double vLe = vS[vy][cx], vRi = vS[vy][cx + 1];  // vertices (i, Jv), (i+1, Jv)
+        const V vLe = vS[vy][cx], vRi = vS[vy][cx + 1];  // vertices (i, Jv), (i+1, Jv)
         if (Jv > 0 && Jv < ny) {
           const long long K = base + (long long)Jv * P + i, L = K - P;
           // K's YNEG edge: A=(i, Jv), B=(i+1, Jv); L's YPOS edge: A=(i+1, Jv), B=(i, Jv)
-          const double aK = geo.aAy[K] * vLe + geo.aBy[K] * vRi;
-          const double aLs = geo.aAy[L] * vRi + geo.aBy[L] * vLe;
-          inner_face(aK, geo.Sy[K], iS[vy + 1][cx + 1], aLs, geo.Sy[L], iS[vy][cx + 1], &aT, &aB);
+          const V aK = A::fma(A::ld(geo.aAy, K), vLe, A::mul(A::ld(geo.aBy, K), vRi));
+          const V aLs = A::fma(A::ld(geo.aAy, L), vRi, A::mul(A::ld(geo.aBy, L), vLe));
+          inner_face<A>(aK, A::ld(geo.Sy, K), iS[vy + 1][cx + 1], aLs, A::ld(geo.Sy, L), iS[vy][cx + 1], &aT, &aB);
         } else if (Jv == 0 && I.bc[YMIN] == DIRICHLET) {
           const long long K = base + i;
-          dirichlet_face(geo.aAy[K] * vLe + geo.aBy[K] * vRi, geo.Sy[K], iS[vy + 1][cx + 1], &aT, &bm);
+          dirichlet_face<A>(A::fma(A::ld(geo.aAy, K), vLe, A::mul(A::ld(geo.aBy, K), vRi)), A::ld(geo.Sy, K),
+                            iS[vy + 1][cx + 1], &aT, &bm);
         } else if (Jv == ny && I.bc[YMAX] == DIRICHLET) {
           const long long K = base + (long long)(ny - 1) * P + i;  // YPOS edge: A=(i+1,ny), B=(i,ny)
-          dirichlet_face(geo.aAy[K] * vRi + geo.aBy[K] * vLe, geo.Sy[K], iS[vy][cx + 1], &aB, &bm);
+          dirichlet_face<A>(A::fma(A::ld(geo.aAy, K), vRi, A::mul(A::ld(geo.aBy, K), vLe)), A::ld(geo.Sy, K),
+                            iS[vy][cx + 1], &aB, &bm);
         }
       }
       yB[vy][cx] = aB;
@@ -325,36 +461,41 @@ __global__ void __launch_bounds__(kAsmThreads) k_assemble(Common cm, Geo geo, Fi
     }
     __syncthreads();
     // 4) per cell: diagonal in the reference's triplet order, RHS, scaling, scatter
+    float rmax = 0.0f;
     for (int q = threadIdx.x; q < kTX * kTY; q += blockDim.x) {
       const int cx = q % kTX, cy = q / kTX;
       const int i = i0 + cx, j = j0 + cy;
       if (i >= nx || j >= ny) continue;
       const long long K = base + (long long)j * P + i;
-      const double Aw = xR[cy][cx], Ae = xL[cy][cx + 1], As = yT[cy][cx], An = yB[cy + 1][cx];
+      const V Aw = xR[cy][cx], Ae = xL[cy][cx + 1], As = yT[cy][cx], An = yB[cy + 1][cx];
       const bool wIn = i > 0, eIn = i < nx - 1, sIn = j > 0, nIn = j < ny - 1;
-      double D = 0.0, Rv = 0.0, dir = 0.0;
-      if (wIn) D += Aw;
-      if (eIn) D += Ae;
-      if (sIn) D += As;
-      if (nIn) D += An;
-      if (!wIn && I.bc[XMIN] == DIRICHLET) { D += Aw; dir += Aw; Rv += xB[cy][cx]; }
-      if (!eIn && I.bc[XMAX] == DIRICHLET) { D += Ae; dir += Ae; Rv += xB[cy][cx + 1]; }
-      if (!sIn && I.bc[YMIN] == DIRICHLET) { D += As; dir += As; Rv += yR[cy][cx]; }
-      if (!nIn && I.bc[YMAX] == DIRICHLET) { D += An; dir += An; Rv += yR[cy + 1][cx]; }
-      const double sd = geo.sdiag[K];
-      D += sd;
-      const double fK = fS[cy + 1][cx + 1];
-      Rv += geo.ukk[K] * fK;
-      const double inv = 1.0 / D;
-      fl.invD[K] = inv;
-      fl.R[K] = Rv;
-      fl.colsum[K] = sd + dir;
-      fl.y64[cm.st[b].ycur][K] = D * fK;
-      if (wIn) AsmOut<C>::put(co, 1, K - 1, Aw * inv);  // row K-1, east entry
-      if (eIn) AsmOut<C>::put(co, 0, K + 1, Ae * inv);  // row K+1, west entry
-      if (sIn) AsmOut<C>::put(co, 3, K - P, As * inv);  // row K-P, north entry
-      if (nIn) AsmOut<C>::put(co, 2, K + P, An * inv);  // row K+P, south entry
+      V D = zero, Rv = zero, dir = zero;
+      if (wIn) D = A::add(D, Aw);
+      if (eIn) D = A::add(D, Ae);
+      if (sIn) D = A::add(D, As);
+      if (nIn) D = A::add(D, An);
+      if (!wIn && I.bc[XMIN] == DIRICHLET) { D = A::add(D, Aw); dir = A::add(dir, Aw); Rv = A::add(Rv, xB[cy][cx]); }
+      if (!eIn && I.bc[XMAX] == DIRICHLET) { D = A::add(D, Ae); dir = A::add(dir, Ae); Rv = A::add(Rv, xB[cy][cx + 1]); }
+      if (!sIn && I.bc[YMIN] == DIRICHLET) { D = A::add(D, As); dir = A::add(dir, As); Rv = A::add(Rv, yR[cy][cx]); }
+      if (!nIn && I.bc[YMAX] == DIRICHLET) { D = A::add(D, An); dir = A::add(dir, An); Rv = A::add(Rv, yR[cy + 1][cx]); }
+      const V sd = A::ld(geo.sdiag, K);
+      D = A::add(D, sd);
+      const V fK = fS[cy + 1][cx + 1];
+      Rv = A::fma(A::ld(geo.ukk, K), fK, Rv);
+      rmax = fmaxf(rmax, fabsf(A::f32(Rv)));
+      const V inv = A::rcp(D);
+      A::st(fl.invD, K, inv);
+      A::st(fl.R, K, Rv);
+      A::st(fl.colsum, K, A::add(sd, dir));
+      A::st(fl.y64[cm.st[b].ycur], K, A::mul(D, fK));
+      if (wIn) AsmOut<C, A>::put(co, 1, K - 1, A::mul(Aw, inv));  // row K-1, east entry
+      if (eIn) AsmOut<C, A>::put(co, 0, K + 1, A::mul(Ae, inv));  // row K+1, west entry
+      if (sIn) AsmOut<C, A>::put(co, 3, K - P, A::mul(As, inv));  // row K-P, north entry
+      if (nIn) AsmOut<C, A>::put(co, 2, K + P, A::mul(An, inv));  // row K+P, south entry
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+    if ((threadIdx.x & 31) == 0 && rmax > 0.0f) atomicMax(&cm.st[b].rmax_bits, __float_as_uint(rmax));
     __syncthreads();
   }
 }
@@ -374,25 +515,29 @@ __device__ __forceinline__ Slot slot_of(const Common& cm, int c, const InstDev& 
   return s;
 }
 
-// FP64 coefficient of row entry from the (hi, lo) split or the FP64 array
-template <typename C>
-struct Coef64;
-template <>
-struct Coef64<double> {
-  __device__ static Q4<double> row(const Coef<double>& c, int which, long long K) {
+// Coefficients of a row in the wide arithmetic: from the FP64 arrays or the (hi, lo) split
+template <typename C, typename A>
+struct CoefW;
+template <typename A>
+struct CoefW<double, A> {
+  __device__ static Q4<typename A::V> row(const Coef<double>& c, int which, long long K) {
     const double* a = which == 0 ? c.cw : which == 1 ? c.ce : which == 2 ? c.cs : c.cn;
-    return ld4(a + K);
+    const Q4<double> q = ld4(a + K);
+    Q4<typename A::V> o;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) o.a[k] = A::from_d(q.a[k]);
+    return o;
   }
 };
-template <>
-struct Coef64<float> {
-  __device__ static Q4<double> row(const Coef<float>& c, int which, long long K) {
+template <typename A>
+struct CoefW<float, A> {
+  __device__ static Q4<typename A::V> row(const Coef<float>& c, int which, long long K) {
     const float* a = which == 0 ? c.cw : which == 1 ? c.ce : which == 2 ? c.cs : c.cn;
     const float* l = which == 0 ? c.lw : which == 1 ? c.le : which == 2 ? c.ls : c.ln;
     const Q4<float> h = ld4(a + K), lo = ld4(l + K);
-    Q4<double> o;
+    Q4<typename A::V> o;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) o.a[k] = (double)h.a[k] + (double)lo.a[k];
+    for (int k = 0; k < 4; ++k) o.a[k] = A::hilo(h.a[k], lo.a[k]);
     return o;
   }
 };
@@ -412,12 +557,32 @@ __device__ __forceinline__ Q4<T> stencil(const Q4<T>& c, T w0, T e3, const Q4<T>
   return o;
 }
 
-// ------------------------------------------------------------------------------ FP64 residual
-// r = R - A~ (y + x) in FP64; writes y + x to the other y buffer and r (T precision).
+// The same stencil in the wide arithmetic: A~ y = y - sum_nbr c * y_nbr
+template <typename A>
+__device__ __forceinline__ Q4<typename A::V> stencilW(const Q4<typename A::V>& c, typename A::V w0,
+                                                      typename A::V e3, const Q4<typename A::V>& dn,
+                                                      const Q4<typename A::V>& up,
+                                                      const Q4<typename A::V>& cw, const Q4<typename A::V>& ce,
+                                                      const Q4<typename A::V>& cs, const Q4<typename A::V>& cn) {
+  using V = typename A::V;
+  Q4<V> o;
+  const V wv[4] = {w0, c.a[0], c.a[1], c.a[2]};
+  const V ev[4] = {c.a[1], c.a[2], c.a[3], e3};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const V s = A::fma(cn.a[k], up.a[k], A::fma(cs.a[k], dn.a[k], A::fma(ce.a[k], ev[k], A::mul(cw.a[k], wv[k]))));
+    o.a[k] = A::sub(c.a[k], s);
+  }
+  return o;
+}
+
+// ------------------------------------------------------------------------------ outer residual
+// r = R - A~ (y + x) in the wide arithmetic; writes y + x to the other y buffer and r (T precision).
 // Partials: ||r||^2, ||R||^2.
-template <typename T, typename C>
+template <typename T, typename C, typename A>
 __global__ void __launch_bounds__(kThreads) k_resid(Common cm, Fields fl, Coef<C> co, Kry<T> kr,
                                                      double tol, double inner_tol, int max_refine) {
+  using V = typename A::V;
   count_launch(cm.ctl);
   for (int c = blockIdx.x; c < cm.nchunks; c += gridDim.x) {
     const int b = cm.chunk_inst[c];
@@ -428,39 +593,45 @@ __global__ void __launch_bounds__(kThreads) k_resid(Common cm, Fields fl, Coef<C
     const double* yin = fl.y64[st.ycur];
     double* yout = fl.y64[st.ycur ^ 1];
     const bool hx = st.has_x != 0;
-    double q[2] = {0.0, 0.0};
+    const float sc = rhs_scale(st.rmax_bits);  // r is handed over as r * sc
+    const float isc = 1.0f / sc;                // exact: sc is a power of two
+    typename A::Acc q0 = 0, q1 = 0;
     if (s.valid) {
       const long long K = s.K, P = I.pitch;
       auto Y4 = [&](long long k) {
-        Q4<double> y = ld4(yin + k);
+        Q4<V> y = A::ld4(yin + k);
         if (hx) {
           const Q4<T> x = ld4(kr.x + k);
 #pragma unroll
-          for (int m = 0; m < 4; ++m) y.a[m] += (double)x.a[m];
+          for (int m = 0; m < 4; ++m) y.a[m] = A::template add_scaled<T>(y.a[m], x.a[m], isc);
         }
         return y;
       };
-      auto Y1 = [&](long long k) { return yin[k] + (hx ? (double)kr.x[k] : 0.0); };
-      const Q4<double> yc = Y4(K), yd = Y4(K - P), yu = Y4(K + P);
-      const double w0 = Y1(K - 1), e3 = Y1(K + 4);
-      const Q4<double> cw = Coef64<C>::row(co, 0, K), ce = Coef64<C>::row(co, 1, K);
-      const Q4<double> cs = Coef64<C>::row(co, 2, K), cn = Coef64<C>::row(co, 3, K);
-      const Q4<double> Ay = stencil<double, double>(yc, w0, e3, yd, yu, cw, ce, cs, cn);
-      const Q4<double> R = ld4(fl.R + K);
+      auto Y1 = [&](long long k) {
+        return hx ? A::template add_scaled<T>(A::ld(yin, k), kr.x[k], isc) : A::ld(yin, k);
+      };
+      const Q4<V> yc = Y4(K), yd = Y4(K - P), yu = Y4(K + P);
+      const V w0 = Y1(K - 1), e3 = Y1(K + 4);
+      const Q4<V> cw = CoefW<C, A>::row(co, 0, K), ce = CoefW<C, A>::row(co, 1, K);
+      const Q4<V> cs = CoefW<C, A>::row(co, 2, K), cn = CoefW<C, A>::row(co, 3, K);
+      const Q4<V> Ay = stencilW<A>(yc, w0, e3, yd, yu, cw, ce, cs, cn);
+      const Q4<V> R = A::ld4(fl.R + K);
       Q4<T> r;
 #pragma unroll
       for (int m = 0; m < 4; ++m) {
-        const double rv = R.a[m] - Ay.a[m];
-        r.a[m] = (T)rv;
-        q[0] += rv * rv;
-        q[1] += R.a[m] * R.a[m];
+        const V rv = A::sub(R.a[m], Ay.a[m]);
+        r.a[m] = A::template scaled<T>(rv, sc);
+        q0 += A::sq_scaled(rv, sc);
+        q1 += A::sq_scaled(R.a[m], sc);
       }
-      st4(yout + K, yc);
+      A::st4(yout + K, yc);
       st4(kr.r + K, r);
     }
+    const double w[2] = {A::warp_total(q0), A::warp_total(q1)};
     double tot[2], mine[2];
-    block_sum<2, double>(q, mine);
+    block_sum_lane0<2>(w, mine);
     if (chunk_finish<2>(st, PH_RESID, I.chunk0, I.nchunks, c, cm.part, mine, tot) && threadIdx.x == 0) {
+      // tot holds ||r*sc||^2 and ||R*sc||^2
       st.ycur ^= 1;
       st.has_x = 0;
       if (st.refines == 0) st.bb = tot[1];
@@ -664,13 +835,15 @@ __global__ void __launch_bounds__(kThreads) k_bicg3(Common cm, Kry<T> kr, int ma
   }
 }
 
+
 // ------------------------------------------------------------------------------ polish + checks
 // y' = R + (I - A~) max(y, 0) >= 0 (R >= 0, fractions >= 0), f = y' / D; partials: sum colsum*f,
-// sum R, clamped count, and -min f (as a max via the sum slot of a separate reduction).
-template <typename C>
+// sum R, clamped count; the chunk minimum of f travels in part slot 3.
+template <typename C, typename A>
 __global__ void __launch_bounds__(kThreads) k_polish(Common cm, Fields fl, Coef<C> co) {
+  using V = typename A::V;
   count_launch(cm.ctl);
-  __shared__ double smin[kThreads / 32];
+  __shared__ float smin[kThreads / 32];
   for (int c = blockIdx.x; c < cm.nchunks; c += gridDim.x) {
     const int b = cm.chunk_inst[c];
     InstState& st = cm.st[b];
@@ -678,58 +851,62 @@ __global__ void __launch_bounds__(kThreads) k_polish(Common cm, Fields fl, Coef<
     if (!I.enabled) continue;
     const Slot s = slot_of(cm, c, I);
     const double* y = fl.y64[st.ycur];
-    double q[3] = {0.0, 0.0, 0.0};
-    double mn = 1.0e300;
+    V mass = A::k(0.0), rsum = A::k(0.0);
+    float clamp = 0.0f;
+    float mn = 3.0e38f;
     if (s.valid) {
       const long long K = s.K, P = I.pitch;
       auto Yp4 = [&](long long k) {
-        Q4<double> v = ld4(y + k);
+        Q4<V> v = A::ld4(y + k);
 #pragma unroll
-        for (int m = 0; m < 4; ++m) v.a[m] = fmax(v.a[m], 0.0);
+        for (int m = 0; m < 4; ++m) v.a[m] = A::max0(v.a[m]);
         return v;
       };
-      const Q4<double> yc = ld4(y + K);
-      Q4<double> ycp;
+      const Q4<V> yc = A::ld4(y + K);
+      Q4<V> ycp;
 #pragma unroll
-      for (int m = 0; m < 4; ++m) ycp.a[m] = fmax(yc.a[m], 0.0);
-      const Q4<double> yd = Yp4(K - P), yu = Yp4(K + P);
-      const double w0 = fmax(y[K - 1], 0.0), e3 = fmax(y[K + 4], 0.0);
-      const Q4<double> cw = Coef64<C>::row(co, 0, K), ce = Coef64<C>::row(co, 1, K);
-      const Q4<double> cs = Coef64<C>::row(co, 2, K), cn = Coef64<C>::row(co, 3, K);
-      const Q4<double> R = ld4(fl.R + K), inv = ld4(fl.invD + K), cols = ld4(fl.colsum + K);
-      const double wv[4] = {w0, ycp.a[0], ycp.a[1], ycp.a[2]};
-      const double ev[4] = {ycp.a[1], ycp.a[2], ycp.a[3], e3};
-      Q4<double> fo;
+      for (int m = 0; m < 4; ++m) ycp.a[m] = A::max0(yc.a[m]);
+      const Q4<V> yd = Yp4(K - P), yu = Yp4(K + P);
+      const V w0 = A::max0(A::ld(y, K - 1)), e3 = A::max0(A::ld(y, K + 4));
+      const Q4<V> cw = CoefW<C, A>::row(co, 0, K), ce = CoefW<C, A>::row(co, 1, K);
+      const Q4<V> cs = CoefW<C, A>::row(co, 2, K), cn = CoefW<C, A>::row(co, 3, K);
+      const Q4<V> R = A::ld4(fl.R + K), inv = A::ld4(fl.invD + K), cols = A::ld4(fl.colsum + K);
+      const V wv[4] = {w0, ycp.a[0], ycp.a[1], ycp.a[2]};
+      const V ev[4] = {ycp.a[1], ycp.a[2], ycp.a[3], e3};
+      Q4<V> fo;
       const int row_i0 = (int)((K - I.base) % I.pitch);
 #pragma unroll
       for (int m = 0; m < 4; ++m) {
-        const double yp = R.a[m] + (cw.a[m] * wv[m] + ce.a[m] * ev[m] + cs.a[m] * yd.a[m] + cn.a[m] * yu.a[m]);
-        const double fv = yp * inv.a[m];
+        const V yp = A::add(R.a[m], A::fma(cn.a[m], yu.a[m], A::fma(cs.a[m], yd.a[m],
+                                           A::fma(ce.a[m], ev[m], A::mul(cw.a[m], wv[m])))));
+        const V fv = A::mul(yp, inv.a[m]);
         fo.a[m] = fv;
-        q[0] += cols.a[m] * fv;
-        q[1] += R.a[m];
-        const bool real = row_i0 + m < I.nx;
-        if (real) {
-          q[2] += yc.a[m] < 0.0 ? 1.0 : 0.0;
-          mn = fmin(mn, fv);
+        mass = A::fma(cols.a[m], fv, mass);
+        rsum = A::add(rsum, R.a[m]);
+        if (row_i0 + m < I.nx) {
+          clamp += A::lt0(yc.a[m]) ? 1.0f : 0.0f;
+          mn = fminf(mn, A::f32(fv));
         }
       }
-      st4(fl.f + K, fo);
+      A::st4(fl.f + K, fo);
     }
-    // block min (separate from the sums)
+    // block minimum (separate from the sums)
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    for (int o = 16; o > 0; o >>= 1) mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
     if ((threadIdx.x & 31) == 0) smin[threadIdx.x >> 5] = mn;
     __syncthreads();
     if (threadIdx.x == 0) {
-      for (int w = 1; w < (int)(blockDim.x >> 5); ++w) mn = fmin(mn, smin[w]);
+      for (int w = 1; w < (int)(blockDim.x >> 5); ++w) mn = fminf(mn, smin[w]);
       smin[0] = mn;
     }
     __syncthreads();
+    float cl = clamp;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cl += __shfl_xor_sync(0xffffffffu, cl, o);
+    const double w[3] = {A::warp_total_v(mass), A::warp_total_v(rsum), (double)cl};
     double tot[3], mine[3];
-    block_sum<3, double>(q, mine);
-    // the chunk's minimum travels in part slot 3 (read back below by the last block)
-    if (threadIdx.x == 0) cm.part[(size_t)c * 4 + 3] = smin[0];
+    block_sum_lane0<3>(w, mine);
+    if (threadIdx.x == 0) cm.part[(size_t)c * 4 + 3] = (double)smin[0];
     if (chunk_finish<3>(st, PH_POLISH, I.chunk0, I.nchunks, c, cm.part, mine, tot) && threadIdx.x == 0) {
       double gmin = 1.0e300;
       for (int k = 0; k < I.nchunks; ++k) gmin = fmin(gmin, __ldcg(&cm.part[(size_t)(I.chunk0 + k) * 4 + 3]));

@@ -32,7 +32,7 @@ def test_assembly_matches_reference(capi, oracle, name):
     ref, Rref = Z[f"{name}/M5"], Z[f"{name}/R"]
     M5o, _, bound = oracle.assemble_bound(p, p.f0)
     assert np.array_equal(M5o, ref)
-    for prec in (capi.FP64, capi.FP32_REFINE):
+    for prec in (capi.FP64, capi.FP32_REFINE, capi.FP32_REFINE_DW):
         s = capi.Solver(p, precision=prec)
         M5, R = s.export_system(0)
         s.close()
@@ -42,7 +42,7 @@ def test_assembly_matches_reference(capi, oracle, name):
 
 
 @pytest.mark.parametrize("name", NAMES)
-@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("prec", [0, 1, 2])
 def test_steps_match_reference(capi, name, prec):
     p = problem_from(Z, name)
     s = capi.Solver(p, precision=prec)
@@ -76,10 +76,11 @@ def test_config0_full_run_fp64(capi):
     assert st["steps"] == rp.nsteps
 
 
-def test_config0_full_run_mixed(capi):
+@pytest.mark.parametrize("prec", [1, 2])
+def test_config0_full_run_mixed(capi, prec):
     z = np.load(os.path.join(GOLDEN, "ref_c0_90x90.npz"))
     rp, p = c0_problem()
-    s = capi.Solver(p, precision=capi.FP32_REFINE)
+    s = capi.Solver(p, precision=prec)
     s.step(rp.nsteps)
     f = s.f()
     s.close()
@@ -90,7 +91,7 @@ def test_config0_full_run_mixed(capi):
 def test_batch_equals_alone(capi):
     """Each instance advanced inside an uneven batch equals the same instance advanced alone."""
     probs = [problem_from(Z, n) for n in NAMES] + cases.batch_problems(6, seed=5, dt=1e-2, lo=40, hi=90)
-    for prec, tol in ((capi.FP64, 1e-12), (capi.FP32_REFINE, 1e-8)):
+    for prec, tol in ((capi.FP64, 1e-12), (capi.FP32_REFINE, 1e-8), (capi.FP32_REFINE_DW, 1e-8)):
         b = capi.Batch(probs, precision=prec)
         b.step(5)
         got = [b.f(k) for k in range(len(probs))]
@@ -103,9 +104,10 @@ def test_batch_equals_alone(capi):
             assert rel(got[k], alone) <= tol, (prec, k, rel(got[k], alone))
 
 
-def test_batch_vs_oracle(capi, oracle):
+@pytest.mark.parametrize("prec", [1, 2])
+def test_batch_vs_oracle(capi, oracle, prec):
     probs = cases.batch_problems(5, seed=11, dt=1e-2, lo=64, hi=100)
-    b = capi.Batch(probs, precision=capi.FP32_REFINE)
+    b = capi.Batch(probs, precision=prec)
     b.step(3)
     for k, p in enumerate(probs):
         ref = oracle.step(p, None, 3)
@@ -116,9 +118,10 @@ def test_batch_vs_oracle(capi, oracle):
     b.close()
 
 
-def test_step_host_roundtrip(capi):
+@pytest.mark.parametrize("prec", [0, 2])
+def test_step_host_roundtrip(capi, prec):
     probs = cases.batch_problems(4, seed=2, dt=1e-2, lo=30, hi=70)
-    b = capi.Batch(probs, precision=capi.FP64)
+    b = capi.Batch(probs, precision=prec)
     fin = np.concatenate([p.f0.ravel() for p in probs])
     fout = np.empty_like(fin)
     b.step_host(2, fin.ctypes.data, fout.ctypes.data)
@@ -127,10 +130,10 @@ def test_step_host_roundtrip(capi):
         n = p.nx * p.ny
         assert np.array_equal(fout[off:off + n].reshape(p.nx, p.ny), b.f(k))
         off += n
-    c = capi.Batch(probs, precision=capi.FP64)
+    c = capi.Batch(probs, precision=prec)
     c.step(2)
     for k in range(len(probs)):
-        assert rel(b.f(k), c.f(k)) <= 1e-13
+        assert rel(b.f(k), c.f(k)) <= 1e-12
     b.close()
     c.close()
 
@@ -177,3 +180,24 @@ def test_large_grid_properties(capi, oracle):
     ref = oracle.step(p, None, 2, solver="splu")
     assert rel(f, ref) <= TOL64, rel(f, ref)
     assert f.min() >= 0.0 and st["mass_drift"] <= 1e-9
+
+
+def test_tiny_magnitudes_scale_invariant(capi):
+    """The FP32 inner solves see residuals scaled by a power of two near max|R|: multiplying f0
+    and the Dirichlet values by 2^-100 (about 1e-30) must scale the result exactly."""
+    p = cases.synthetic_problem(48, 40, 1e-2, seed=6)
+    q = cases.synthetic_problem(48, 40, 1e-2, seed=6)
+    sc = 2.0 ** -100
+    q.f0 = p.f0 * sc
+    q.dirichlet = [None if d is None else d * sc for d in p.dirichlet]
+    for prec in (capi.FP32_REFINE, capi.FP32_REFINE_DW):
+        a = capi.Solver(p, precision=prec)
+        a.step(3)
+        c = capi.Solver(q, precision=prec)
+        c.step(3)
+        fa, fc = a.f(), c.f()
+        st = c.get_stats()
+        a.close()
+        c.close()
+        assert rel(fc / sc, fa) <= 1e-8, (prec, rel(fc / sc, fa))
+        assert st["rel_residual"] <= 1e-10 and fc.min() >= 0.0
