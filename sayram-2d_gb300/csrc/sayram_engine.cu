@@ -89,11 +89,18 @@ struct sayram_batch_s {
   std::vector<cudaEvent_t> evpool;
   size_t evused = 0;
   cudaEvent_t slots[8] = {};
+  // per-step CUDA graph with device-side loops (built on the first graph step)
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
 
   ~sayram_batch_s() { release(); }
 
   void release() {
     if (dev >= 0) cudaSetDevice(dev);
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (graph) cudaGraphDestroy(graph);
+    gexec = nullptr;
+    graph = nullptr;
     for (void* p : allocs) cudaFree(p);
     allocs.clear();
     if (h_ctl) cudaFreeHost(h_ctl);
@@ -174,6 +181,9 @@ struct sayram_batch_s {
   int finish_status();
   template <typename T, typename C, typename A>
   int step_once(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, const sg::Kry<T>& kr);
+  template <typename T, typename C, typename A>
+  int build_graph(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, const sg::Kry<T>& kr);
+  int last_captured(cudaGraphNode_t* node);
   // wide (8-byte) table entries: a double, or a (hi, lo) float pair in double-word mode
   double wide(double v) const {
     if (!dwm) return v;
@@ -443,10 +453,101 @@ int sayram_batch_s::step_once(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, c
   return SAYRAM_OK;
 }
 
+int sayram_batch_s::last_captured(cudaGraphNode_t* node) {
+  cudaStreamCaptureStatus cs;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  SG_CUDA(cudaStreamGetCaptureInfo(stream, &cs, nullptr, nullptr, &deps, nullptr, &nd));
+  if (cs != cudaStreamCaptureStatusActive || nd != 1) return fail(SAYRAM_ERR_CUDA, "unexpected capture state");
+  *node = deps[0];
+  return SAYRAM_OK;
+}
+
+// One step as a graph: memset + begin + assemble, WHILE(outer){ resid, WHILE(inner){ k1 k2 k3 } },
+// polish. The WHILE conditions are set on the device by the residual and Krylov kernels.
+template <typename T, typename C, typename A>
+int sayram_batch_s::build_graph(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, const sg::Kry<T>& kr) {
+  using namespace sg;
+  const int gs = grid_stream(), gt = grid_tiles();
+  const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
+  cudaGraph_t g = nullptr;
+  SG_CUDA(cudaGraphCreate(&g, 0));
+  graph = g;
+  cudaGraphConditionalHandle hout, hin;
+  SG_CUDA(cudaGraphConditionalHandleCreate(&hout, g, 1, cudaGraphCondAssignDefault));
+  Common c2 = cm;
+  c2.use_cond = 1;
+  c2.h_outer = hout;
+  c2.guard_refine = opt.max_refine + 1;
+  c2.guard_iters = opt.max_iters + 1;
+  int rc;
+  // prefix
+  cudaGraphNode_t pre;
+  SG_CUDA(cudaStreamBeginCaptureToGraph(stream, g, nullptr, nullptr, 0, mode));
+  cudaMemsetAsync(d_ctl, 0, 2 * sizeof(int), stream);
+  k_begin<<<(n + 255) / 256, 256, 0, stream>>>(c2);
+  k_assemble<C, A><<<gt, kAsmThreads, 0, stream>>>(c2, geo, fl, cfull);
+  if ((rc = last_captured(&pre))) { cudaStreamEndCapture(stream, &g); return rc; }
+  SG_CUDA(cudaStreamEndCapture(stream, &g));
+  // outer WHILE
+  cudaGraphNodeParams op = {};
+  op.type = cudaGraphNodeTypeConditional;
+  op.conditional.handle = hout;
+  op.conditional.type = cudaGraphCondTypeWhile;
+  op.conditional.size = 1;
+  cudaGraphNode_t outer;
+  SG_CUDA(cudaGraphAddNode(&outer, g, &pre, nullptr, 1, &op));
+  cudaGraph_t obody = op.conditional.phGraph_out[0];
+  SG_CUDA(cudaGraphConditionalHandleCreate(&hin, obody, 0, cudaGraphCondAssignDefault));
+  c2.h_inner = hin;
+  cudaGraphNode_t rnode;
+  SG_CUDA(cudaStreamBeginCaptureToGraph(stream, obody, nullptr, nullptr, 0, mode));
+  k_resid<T, C, A><<<gs, kThreads, 0, stream>>>(c2, fl, cfull, kr, opt.tol, opt.inner_tol, opt.max_refine);
+  if ((rc = last_captured(&rnode))) { cudaStreamEndCapture(stream, &obody); return rc; }
+  SG_CUDA(cudaStreamEndCapture(stream, &obody));
+  // inner WHILE inside the outer body
+  cudaGraphNodeParams ip = {};
+  ip.type = cudaGraphNodeTypeConditional;
+  ip.conditional.handle = hin;
+  ip.conditional.type = cudaGraphCondTypeWhile;
+  ip.conditional.size = 1;
+  cudaGraphNode_t inner;
+  SG_CUDA(cudaGraphAddNode(&inner, obody, &rnode, nullptr, 1, &ip));
+  cudaGraph_t ibody = ip.conditional.phGraph_out[0];
+  SG_CUDA(cudaStreamBeginCaptureToGraph(stream, ibody, nullptr, nullptr, 0, mode));
+  k_bicg1<T><<<gs, kThreads, 0, stream>>>(c2, ck, kr);
+  k_bicg2<T><<<gs, kThreads, 0, stream>>>(c2, ck, kr);
+  k_bicg3<T><<<gs, kThreads, 0, stream>>>(c2, kr, opt.max_iters);
+  SG_CUDA(cudaStreamEndCapture(stream, &ibody));
+  // suffix
+  SG_CUDA(cudaStreamBeginCaptureToGraph(stream, g, &outer, nullptr, 1, mode));
+  k_polish<C, A><<<gs, kThreads, 0, stream>>>(c2, fl, cfull);
+  SG_CUDA(cudaStreamEndCapture(stream, &g));
+  SG_CUDA(cudaGraphInstantiate(&gexec, g, 0));
+  return SAYRAM_OK;
+}
+
 int sayram_batch_s::run_steps(int nsteps) {
   if (nsteps < 0) return fail(SAYRAM_ERR_ARG, "nsteps must be >= 0");
   SG_CUDA(cudaSetDevice(dev));
+  const bool use_graph = opt.use_graph && !timing;
+  if (use_graph && !gexec) {
+    int rc = dwm ? build_graph<float, float, sg::DWA>(c32, c32, k32)
+             : mixed ? build_graph<float, float, sg::F64A>(c32, c32, k32)
+                     : build_graph<double, double, sg::F64A>(c64, c64, k64);
+    if (rc) {
+      if (gexec) cudaGraphExecDestroy(gexec);
+      if (graph) cudaGraphDestroy(graph);
+      gexec = nullptr;
+      graph = nullptr;
+      return rc;
+    }
+  }
   for (int s = 0; s < nsteps; ++s) {
+    if (use_graph) {
+      SG_CUDA(cudaGraphLaunch(gexec, stream));
+      continue;
+    }
     int rc = dwm ? step_once<float, float, sg::DWA>(c32, c32, k32)
              : mixed ? step_once<float, float, sg::F64A>(c32, c32, k32)
                      : step_once<double, double, sg::F64A>(c64, c64, k64);

@@ -71,6 +71,8 @@ struct Ctl {
   int n_inner;   // instances inside an inner Krylov solve
   unsigned long long launches;  // kernel launches (block 0 of every kernel adds one)
   unsigned int kdone[8];        // blocks finished per kernel (graph-conditional updates)
+  unsigned int outer_loops;     // residual evaluations run by the device-side loop this step
+  unsigned int inner_loops;     // Krylov iterations run by the device-side loop this solve
 };
 
 template <typename T>

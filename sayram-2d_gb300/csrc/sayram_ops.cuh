@@ -38,7 +38,39 @@ struct Common {
   const double* wy;    // per vertex row: (wB, wT)
   const double* dirv;  // Dirichlet vertex values
   double* part;        // 4 doubles per chunk
+  // device-side loops of the per-step CUDA graph (use_cond = 0: the host drives the loops)
+  unsigned long long h_outer, h_inner;  // cudaGraphConditionalHandle of the two WHILE nodes
+  int use_cond;
+  int guard_refine, guard_iters;  // hard caps on loop trips, whatever the bookkeeping says
 };
+
+// The last block of a loop-deciding kernel sets the graph's WHILE conditions from the number of
+// instances still active. The trip counters make both loops terminate after guard_refine
+// residual evaluations and guard_iters Krylov iterations even if the counts were inconsistent.
+// which = 0: after the residual (decides both loops); which = 1: after a Krylov iteration.
+__device__ __forceinline__ void loop_epilogue(const Common& cm, int which) {
+  if (!cm.use_cond) return;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned prev = atomicAdd(&cm.ctl->kdone[which], 1u);
+    if (prev == gridDim.x - 1) {
+      __threadfence();
+      const int nout = atomicAdd(&cm.ctl->n_outer, 0);
+      const int nin = atomicAdd(&cm.ctl->n_inner, 0);
+      if (which == 0) {
+        const unsigned lo = atomicAdd(&cm.ctl->outer_loops, 1u) + 1u;
+        atomicExch(&cm.ctl->inner_loops, 0u);
+        cudaGraphSetConditional(cm.h_outer, (nout > 0 && lo < (unsigned)cm.guard_refine) ? 1u : 0u);
+        cudaGraphSetConditional(cm.h_inner, (nin > 0 && lo < (unsigned)cm.guard_refine) ? 1u : 0u);
+      } else {
+        const unsigned li = atomicAdd(&cm.ctl->inner_loops, 1u) + 1u;
+        cudaGraphSetConditional(cm.h_inner, (nin > 0 && li < (unsigned)cm.guard_iters) ? 1u : 0u);
+      }
+      atomicExch(&cm.ctl->kdone[which], 0u);
+    }
+  }
+}
 
 template <typename C>
 struct Coef {  // row-oriented scaled off-diagonal magnitudes (hi parts when split)
@@ -285,6 +317,10 @@ __global__ void k_begin(Common cm) {
     s.clamped = 0;
     s.rmax_bits = 0u;
     if (on) atomicAdd(&cm.ctl->n_outer, 1);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    cm.ctl->outer_loops = 0u;
+    cm.ctl->inner_loops = 0u;
   }
 }
 
@@ -659,6 +695,7 @@ __global__ void __launch_bounds__(kThreads) k_resid(Common cm, Fields fl, Coef<C
       }
     }
   }
+  loop_epilogue(cm, 0);
 }
 
 // ------------------------------------------------------------------------------ BiCGSTAB
@@ -833,8 +870,8 @@ __global__ void __launch_bounds__(kThreads) k_bicg3(Common cm, Kry<T> kr, int ma
       }
     }
   }
+  loop_epilogue(cm, 1);
 }
-
 
 // ------------------------------------------------------------------------------ polish + checks
 // y' = R + (I - A~) max(y, 0) >= 0 (R >= 0, fractions >= 0), f = y' / D; partials: sum colsum*f,

@@ -199,3 +199,21 @@ def test_tiny_magnitudes(capi, oracle):
         c.close()
         assert rel(fc, ref) <= tol, (prec, rel(fc, ref))
         assert fc.min() >= 0.0
+
+
+@pytest.mark.parametrize("prec", [0, 1, 2])
+def test_graph_equals_host_loop(capi, prec):
+    """The per-step CUDA graph (device-side WHILE loops) runs the same kernels in the same order
+    as the host-driven loop, so the results are identical."""
+    probs = cases.batch_problems(5, seed=9, dt=1e-2, lo=20, hi=90)
+    g = capi.Batch(probs, precision=prec, use_graph=1)
+    h = capi.Batch(probs, precision=prec, use_graph=0)
+    g.step(4)
+    h.step(4)
+    for k in range(len(probs)):
+        assert np.array_equal(g.f(k), h.f(k)), (prec, k, rel(g.f(k), h.f(k)))
+        sg, sh = g.stats(k), h.stats(k)
+        assert sg["total_iterations"] == sh["total_iterations"]
+        assert sg["total_refinements"] == sh["total_refinements"]
+    g.close()
+    h.close()
