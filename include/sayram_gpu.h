@@ -179,6 +179,47 @@ int sayram_batch_kernel_times(sayram_batch b, const char** names, double* total_
 long long sayram_batch_launches(sayram_batch b);
 void sayram_batch_destroy(sayram_batch b);
 
+/* ---- serving: continuous batching of solve requests -------------------------------------
+ * No counterpart in the reference. A server owns a device arena sized by an HBM budget. Requests
+ * (a problem plus a step count) are queued by sayram_server_submit; every sayram_server_tick
+ *   1. admits waiting requests in arrival order while a slot and a contiguous region of the arena
+ *      are free (a request that does not fit waits; up to 8 later requests may pass it),
+ *   2. advances every resident instance by one backward-Euler step, all in the same launches,
+ *   3. copies the state of instances that reached their step count back to the host and frees
+ *      their memory, so that the next tick can admit more.
+ * Each instance's f, coefficients and matrix stay on the device from admission to completion.
+ * Results are collected with sayram_server_poll. Latency = completion - submission (steady clock). */
+typedef struct sayram_server_s* sayram_server;
+
+typedef struct sayram_server_config {
+  double hbm_budget_bytes; /* device bytes the server may use (arena + tables + solver state) */
+  int max_slots;           /* instances resident at once (default 4096) */
+  int max_side;            /* largest nx or ny accepted (default 1024) */
+} sayram_server_config;
+
+typedef struct sayram_server_info {
+  long long submitted, admitted, completed, waiting, resident;
+  long long ticks;              /* ticks that ran a step */
+  long long instance_steps;     /* steps executed, summed over instances */
+  double device_bytes;          /* bytes held by the server */
+  double arena_cells, arena_cells_used;
+  double busy_seconds;          /* wall time spent inside ticks that ran a step */
+} sayram_server_info;
+
+int sayram_server_create(const sayram_server_config* cfg, const sayram_options* opt, sayram_server* out);
+/* Copies the problem (arrays are not retained) and queues it for nsteps steps. SAYRAM_ERR_BUDGET
+ * if the request could never fit the server (grid larger than max_side or than the arena). */
+int sayram_server_submit(sayram_server s, const sayram_problem* p, int nsteps, long long* id_out);
+/* One scheduling round (admission, one step of every resident instance, completions). */
+int sayram_server_tick(sayram_server s, int* n_completed);
+/* SAYRAM_OK and the result (f alpha-major, stats, submit/done times in seconds of the steady
+ * clock) when request id has completed -- the result is then released; SAYRAM_ERR_STATE if not
+ * yet. Any output pointer may be NULL. */
+int sayram_server_poll(sayram_server s, long long id, double* f_out, sayram_stats* st, double* t_submit,
+                       double* t_done);
+int sayram_server_info_get(sayram_server s, sayram_server_info* out);
+void sayram_server_destroy(sayram_server s);
+
 /* ---- stepping without allocating -------------------------------------------------------
  * sayram_step_noalloc: nsteps FP64 backward-Euler steps of ONE instance that allocate no memory.
  * No counterpart in the reference. It is for callers that cannot call cudaMalloc: programs whose

@@ -57,6 +57,21 @@ class sayram_stats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class sayram_server_config(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_double), ("max_slots", ctypes.c_int), ("max_side", ctypes.c_int)]
+
+
+class sayram_server_info(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_longlong), ("admitted", ctypes.c_longlong), ("completed", ctypes.c_longlong),
+                ("waiting", ctypes.c_longlong), ("resident", ctypes.c_longlong), ("ticks", ctypes.c_longlong),
+                ("instance_steps", ctypes.c_longlong), ("device_bytes", ctypes.c_double),
+                ("arena_cells", ctypes.c_double), ("arena_cells_used", ctypes.c_double),
+                ("busy_seconds", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 # name -> (restype, argtypes); every symbol the header declares
 _P = ctypes.c_void_p
 SIGNATURES = {
@@ -94,6 +109,14 @@ SIGNATURES = {
     "sayram_batch_launches": (ctypes.c_longlong, [_P]),
     "sayram_batch_destroy": (None, [_P]),
     "sayram_instance_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "sayram_server_create": (ctypes.c_int, [ctypes.POINTER(sayram_server_config), ctypes.POINTER(sayram_options),
+                                            ctypes.POINTER(_P)]),
+    "sayram_server_submit": (ctypes.c_int, [_P, ctypes.POINTER(sayram_problem), ctypes.c_int,
+                                            ctypes.POINTER(ctypes.c_longlong)]),
+    "sayram_server_tick": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),
+    "sayram_server_poll": (ctypes.c_int, [_P, ctypes.c_longlong, _dp, ctypes.POINTER(sayram_stats), _dp, _dp]),
+    "sayram_server_info_get": (ctypes.c_int, [_P, ctypes.POINTER(sayram_server_info)]),
+    "sayram_server_destroy": (None, [_P]),
     "sayram_step_noalloc": (ctypes.c_int, [ctypes.POINTER(sayram_problem), ctypes.POINTER(sayram_options),
                                            ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                            ctypes.POINTER(sayram_stats)]),
@@ -301,6 +324,62 @@ class Solver(Batch):
 
     def get_stats(self) -> dict:
         return self.stats(0)
+
+
+class Server:
+    """Continuous-batching service of solve requests (sayram_server_*)."""
+
+    def __init__(self, hbm_budget_bytes: float, max_slots: int = 4096, max_side: int = 1024,
+                 opts: Optional[sayram_options] = None, **kw):
+        L = load()
+        self._L = L
+        cfg = sayram_server_config(float(hbm_budget_bytes), int(max_slots), int(max_side))
+        opts = opts if opts is not None else options(**kw)
+        h = ctypes.c_void_p()
+        check(L.sayram_server_create(ctypes.byref(cfg), ctypes.byref(opts), ctypes.byref(h)), "sayram_server_create")
+        self.h = h
+        self.shapes = {}
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            self._L.sayram_server_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, problem, nsteps: int) -> int:
+        pack = _Pack([problem])
+        rid = ctypes.c_longlong()
+        check(self._L.sayram_server_submit(self.h, pack.arr, int(nsteps), ctypes.byref(rid)), "sayram_server_submit")
+        self.shapes[rid.value] = (int(problem.nx), int(problem.ny))
+        return rid.value
+
+    def tick(self) -> int:
+        n = ctypes.c_int()
+        check(self._L.sayram_server_tick(self.h, ctypes.byref(n)), "sayram_server_tick")
+        return n.value
+
+    def poll(self, rid: int, want_f: bool = True):
+        """None while running; else (f or None, stats dict, t_submit, t_done) and the result is released."""
+        nx, ny = self.shapes[rid]
+        f = np.empty((nx, ny)) if want_f else None
+        st = sayram_stats()
+        t0, t1 = ctypes.c_double(), ctypes.c_double()
+        rc = self._L.sayram_server_poll(self.h, rid, _ptr(f), ctypes.byref(st), ctypes.byref(t0), ctypes.byref(t1))
+        if rc == ERR_STATE:
+            return None
+        check(rc, "sayram_server_poll")
+        del self.shapes[rid]
+        return f, st.as_dict(), t0.value, t1.value
+
+    def info(self) -> dict:
+        i = sayram_server_info()
+        check(self._L.sayram_server_info_get(self.h, ctypes.byref(i)), "sayram_server_info_get")
+        return i.as_dict()
 
 
 def instance_bytes(nx: int, ny: int, precision: int = FP32_REFINE) -> int:

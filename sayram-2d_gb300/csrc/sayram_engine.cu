@@ -4,6 +4,9 @@
 // layout, the chunk/tile work lists, the per-step launch sequence and the optional CUDA graph.
 // Every public function returns a status code and records a message for sayram_last_error().
 #include <algorithm>
+#include <chrono>
+#include <deque>
+#include <map>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -38,11 +41,6 @@ using sg::Ctl;
 using sg::InstDev;
 using sg::InstState;
 
-struct Stage {  // per-instance host data kept for the layout
-  int nx, ny;
-  std::vector<double> xe, ye;
-};
-
 }  // namespace
 
 struct sayram_batch_s {
@@ -52,8 +50,11 @@ struct sayram_batch_s {
   cudaStream_t stream = nullptr;
   int n = 0;
   std::vector<InstDev> hinst;
-  std::vector<Stage> stage;
-  long long ncell = 0;      // padded storage cells
+  long long ncell = 0;      // padded storage cells (capacity)
+  int cap_slots = 0, cap_chunks = 0, cap_tiles = 0;
+  int* d_dyn = nullptr;     // [nchunks, ntiles, ninst] read by the kernels
+  std::vector<int> h_chunk, h_tile;
+  std::vector<std::pair<void*, int>> cell_arrays;  // every per-cell array and its element size
   long long nreal = 0;      // real cells (packed alpha-major size)
   int nchunks = 0, ntiles = 0;
   size_t bytes = 0;
@@ -171,12 +172,21 @@ struct sayram_batch_s {
     evused = 0;
   }
 
-  int grid_stream() const { return std::max(1, std::min(nchunks, nsm * 16)); }
-  int grid_tiles() const { return std::max(1, std::min(ntiles, nsm * 8)); }
+  int grid_stream() const { return std::max(1, std::min(cap_chunks, nsm * 16)); }
+  int grid_tiles() const { return std::max(1, std::min(cap_tiles, nsm * 8)); }
 
   int build(const sayram_problem* probs, int count, const sayram_options* o);
+  int set_options(const sayram_options* o);
+  int init_device();
+  int alloc_storage(long long cells, int slots, int chunks_cap, int tiles_cap, long long xcap, long long ycap,
+                    long long dcap, long long stage_cap);
+  int zero_region(long long begin, long long end);
+  int place(int b, const sayram_problem& p, long long base, int xe_off, int ye_off, const int dir_off[4],
+            long long hoff);
+  int rebuild_lists();
   int upload_instance(int b, const sayram_problem& p, bool coeffs, bool f0);
   int run_steps(int nsteps);
+  int launch_steps(int nsteps);  // queue steps on the stream (no status read-back)
   int read_ctl();
   int finish_status();
   template <typename T, typename C, typename A>
@@ -223,7 +233,7 @@ static int validate_problem(const sayram_problem& p) {
   return SAYRAM_OK;
 }
 
-int sayram_batch_s::build(const sayram_problem* probs, int count, const sayram_options* o) {
+int sayram_batch_s::set_options(const sayram_options* o) {
   sayram_default_options(&opt);
   if (o) opt = *o;
   if (opt.precision != SAYRAM_FP64 && opt.precision != SAYRAM_FP32_REFINE && opt.precision != SAYRAM_FP32_REFINE_DW)
@@ -234,10 +244,10 @@ int sayram_batch_s::build(const sayram_problem* probs, int count, const sayram_o
   if (opt.max_refine < 2) opt.max_refine = 2;
   mixed = opt.precision != SAYRAM_FP64;
   dwm = opt.precision == SAYRAM_FP32_REFINE_DW;
-  for (int b = 0; b < count; ++b) {
-    int rc = validate_problem(probs[b]);
-    if (rc) return fail(rc, "instance " + std::to_string(b) + ": " + g_err);
-  }
+  return SAYRAM_OK;
+}
+
+int sayram_batch_s::init_device() {
   dev = opt.device;
   int ndev = 0;
   SG_CUDA(cudaGetDeviceCount(&ndev));
@@ -245,147 +255,214 @@ int sayram_batch_s::build(const sayram_problem* probs, int count, const sayram_o
   SG_CUDA(cudaSetDevice(dev));
   SG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   SG_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-  n = count;
-  hinst.resize(n);
-  stage.resize(n);
-  // ---- layout
-  long long cursor = 0, hoff = 0;
-  int chunk = 0, tile = 0, xoff = 0, yoff = 0, doff = 0;
-  long long maxcells = 0;
-  std::vector<int> chunk_inst, tile_inst;
-  for (int b = 0; b < n; ++b) {
-    const sayram_problem& p = probs[b];
-    InstDev& I = hinst[b];
-    std::memset(&I, 0, sizeof(I));
-    I.nx = p.nx;
-    I.ny = p.ny;
-    I.pitch = (int)round_up(p.nx, 4);
-    I.enabled = 1;
-    for (int s = 0; s < 4; ++s) I.bc[s] = p.bc[s];
-    I.base = cursor + I.pitch;
-    cursor += round_up((long long)(p.ny + 2) * I.pitch, 32);
-    I.hoff = hoff;
-    hoff += (long long)p.nx * p.ny;
-    I.chunk0 = chunk;
-    I.nchunks = (int)((round_up((long long)p.ny * I.pitch, 4) + sg::kChunk - 1) / sg::kChunk);
-    for (int k = 0; k < I.nchunks; ++k) chunk_inst.push_back(b);
-    chunk += I.nchunks;
-    I.tile0 = tile;
-    I.ntx = (p.nx + sg::kTX - 1) / sg::kTX;
-    I.nty = (p.ny + sg::kTY - 1) / sg::kTY;
-    for (int k = 0; k < I.ntx * I.nty; ++k) tile_inst.push_back(b);
-    tile += I.ntx * I.nty;
-    I.xe = xoff;
-    xoff += p.nx + 1;
-    I.ye = yoff;
-    yoff += p.ny + 1;
-    for (int s = 0; s < 4; ++s) {
-      if (p.bc[s] == SAYRAM_DIRICHLET) {
-        I.dir[s] = doff;
-        doff += (s <= 1) ? p.ny + 1 : p.nx + 1;
-      } else {
-        I.dir[s] = -1;
-      }
-    }
-    I.dt = p.dt;
-    maxcells = std::max(maxcells, (long long)p.nx * p.ny);
-  }
-  ncell = cursor + 64;
-  nreal = hoff;
-  nchunks = chunk;
-  ntiles = tile;
-  stage_cells = std::max(6 * maxcells, nreal);
-  // ---- allocations
+  return SAYRAM_OK;
+}
+
+// Device storage for `cells` padded cells, `slots` instances, the work lists and the per-instance
+// tables (edges, weights, Dirichlet values; capacities in entries).
+int sayram_batch_s::alloc_storage(long long cells, int slots, int chunks_cap, int tiles_cap, long long xcap,
+                                  long long ycap, long long dcap, long long stage_cap) {
   int rc;
 #define SG_ALLOC(p, cnt) \
   if ((rc = alloc(&(p), (cnt))) != SAYRAM_OK) return rc
-  SG_ALLOC(d_inst, n);
-  SG_ALLOC(d_st, n);
+  ncell = cells;
+  cap_slots = slots;
+  cap_chunks = chunks_cap;
+  cap_tiles = tiles_cap;
+  stage_cells = stage_cap;
+  SG_ALLOC(d_inst, slots);
+  SG_ALLOC(d_st, slots);
   SG_ALLOC(d_ctl, 1);
-  SG_ALLOC(d_chunk, nchunks);
-  SG_ALLOC(d_tile, ntiles);
-  SG_ALLOC(d_xe, xoff);
-  SG_ALLOC(d_ye, yoff);
-  SG_ALLOC(d_wx, 2 * xoff);
-  SG_ALLOC(d_wy, 2 * yoff);
-  SG_ALLOC(d_dirv, std::max(doff, 1));
-  SG_ALLOC(d_part, 4LL * nchunks);
-  SG_ALLOC(d_stage, stage_cells);
+  SG_ALLOC(d_dyn, 4);
+  SG_ALLOC(d_chunk, chunks_cap);
+  SG_ALLOC(d_tile, tiles_cap);
+  SG_ALLOC(d_xe, xcap);
+  SG_ALLOC(d_ye, ycap);
+  SG_ALLOC(d_wx, 2 * xcap);
+  SG_ALLOC(d_wy, 2 * ycap);
+  SG_ALLOC(d_dirv, std::max<long long>(dcap, 1));
+  SG_ALLOC(d_part, 4LL * chunks_cap);
+  SG_ALLOC(d_stage, stage_cap);
+  cell_arrays.clear();
   double** geos[8] = {&geo.aAx, &geo.aBx, &geo.Sx, &geo.aAy, &geo.aBy, &geo.Sy, &geo.ukk, &geo.sdiag};
-  for (auto g : geos) SG_ALLOC(*g, ncell);
-  SG_ALLOC(fl.f, ncell);
-  SG_ALLOC(fl.invD, ncell);
-  SG_ALLOC(fl.R, ncell);
-  SG_ALLOC(fl.colsum, ncell);
-  SG_ALLOC(fl.y64[0], ncell);
-  SG_ALLOC(fl.y64[1], ncell);
+  for (auto g : geos) {
+    SG_ALLOC(*g, cells);
+    cell_arrays.push_back({*g, 8});
+  }
+  double** fs[6] = {&fl.f, &fl.invD, &fl.R, &fl.colsum, &fl.y64[0], &fl.y64[1]};
+  for (auto f : fs) {
+    SG_ALLOC(*f, cells);
+    cell_arrays.push_back({*f, 8});
+  }
   if (mixed) {
     float** cs[8] = {&c32.cw, &c32.ce, &c32.cs, &c32.cn, &c32.lw, &c32.le, &c32.ls, &c32.ln};
-    for (auto c : cs) SG_ALLOC(*c, ncell);
+    for (auto c : cs) {
+      SG_ALLOC(*c, cells);
+      cell_arrays.push_back({*c, 4});
+    }
     float** ks[8] = {&k32.r, &k32.rh, &k32.t, &k32.x, &k32.p[0], &k32.p[1], &k32.v[0], &k32.v[1]};
-    for (auto k : ks) SG_ALLOC(*k, ncell);
+    for (auto k : ks) {
+      SG_ALLOC(*k, cells);
+      cell_arrays.push_back({*k, 4});
+    }
   } else {
     double** cs[4] = {&c64.cw, &c64.ce, &c64.cs, &c64.cn};
-    for (auto c : cs) SG_ALLOC(*c, ncell);
+    for (auto c : cs) {
+      SG_ALLOC(*c, cells);
+      cell_arrays.push_back({*c, 8});
+    }
     double** ks[8] = {&k64.r, &k64.rh, &k64.t, &k64.x, &k64.p[0], &k64.p[1], &k64.v[0], &k64.v[1]};
-    for (auto k : ks) SG_ALLOC(*k, ncell);
+    for (auto k : ks) {
+      SG_ALLOC(*k, cells);
+      cell_arrays.push_back({*k, 8});
+    }
   }
 #undef SG_ALLOC
   SG_CUDA(cudaMallocHost(&h_ctl, sizeof(Ctl)));
   std::memset(h_ctl, 0, sizeof(Ctl));
-  // ---- tables
-  std::vector<double> xe(xoff), ye(yoff), wx(2 * xoff, 0.0), wy(2 * yoff, 0.0), dirv(std::max(doff, 1), 0.0);
-  for (int b = 0; b < n; ++b) {
-    const sayram_problem& p = probs[b];
-    const InstDev& I = hinst[b];
-    for (int i = 0; i <= p.nx; ++i) xe[I.xe + i] = p.x_edges[i];
-    for (int j = 0; j <= p.ny; ++j) ye[I.ye + j] = p.y_edges[j];
-    // bilinear weights of Solver.cc:333-336 (per vertex column / row, interior and edges)
-    for (int i = 1; i < p.nx; ++i) {
-      const double xv = p.x_edges[i];
-      const double xl = 0.5 * (p.x_edges[i - 1] + p.x_edges[i]), xr = 0.5 * (p.x_edges[i] + p.x_edges[i + 1]);
-      wx[2 * (I.xe + i)] = wide((xr - xv) / (xr - xl));
-      wx[2 * (I.xe + i) + 1] = wide((xv - xl) / (xr - xl));
-    }
-    for (int j = 1; j < p.ny; ++j) {
-      const double yv = p.y_edges[j];
-      const double yb = 0.5 * (p.y_edges[j - 1] + p.y_edges[j]), yt = 0.5 * (p.y_edges[j] + p.y_edges[j + 1]);
-      wy[2 * (I.ye + j)] = wide((yt - yv) / (yt - yb));
-      wy[2 * (I.ye + j) + 1] = wide((yv - yb) / (yt - yb));
-    }
-    for (int s = 0; s < 4; ++s)
-      if (I.dir[s] >= 0) {
-        const int m = (s <= 1) ? p.ny + 1 : p.nx + 1;
-        for (int k = 0; k < m; ++k) dirv[I.dir[s] + k] = wide(p.dirichlet[s][k]);
-      }
-    stage[b].nx = p.nx;
-    stage[b].ny = p.ny;
-  }
-  SG_CUDA(cudaMemcpyAsync(d_inst, hinst.data(), sizeof(InstDev) * n, cudaMemcpyHostToDevice, stream));
-  SG_CUDA(cudaMemcpyAsync(d_chunk, chunk_inst.data(), sizeof(int) * nchunks, cudaMemcpyHostToDevice, stream));
-  SG_CUDA(cudaMemcpyAsync(d_tile, tile_inst.data(), sizeof(int) * ntiles, cudaMemcpyHostToDevice, stream));
-  SG_CUDA(cudaMemcpyAsync(d_xe, xe.data(), sizeof(double) * xoff, cudaMemcpyHostToDevice, stream));
-  SG_CUDA(cudaMemcpyAsync(d_ye, ye.data(), sizeof(double) * yoff, cudaMemcpyHostToDevice, stream));
-  SG_CUDA(cudaMemcpyAsync(d_wx, wx.data(), sizeof(double) * 2 * xoff, cudaMemcpyHostToDevice, stream));
-  SG_CUDA(cudaMemcpyAsync(d_wy, wy.data(), sizeof(double) * 2 * yoff, cudaMemcpyHostToDevice, stream));
-  SG_CUDA(cudaMemcpyAsync(d_dirv, dirv.data(), sizeof(double) * dirv.size(), cudaMemcpyHostToDevice, stream));
-  SG_CUDA(cudaStreamSynchronize(stream));
+  hinst.assign(slots, InstDev{});
+  cm = sg::Common{};
   cm.inst = d_inst;
   cm.st = d_st;
   cm.ctl = d_ctl;
   cm.chunk_inst = d_chunk;
-  cm.nchunks = nchunks;
   cm.tile_inst = d_tile;
-  cm.ntiles = ntiles;
-  cm.ninst = n;
   cm.wx = d_wx;
   cm.wy = d_wy;
   cm.dirv = d_dirv;
   cm.part = d_part;
-  for (int b = 0; b < n; ++b) {
-    rc = upload_instance(b, probs[b], true, true);
-    if (rc) return rc;
+  cm.dyn = d_dyn;
+  return SAYRAM_OK;
+}
+
+// Zeroes cells [begin, end) of every per-cell array (a reused region must start at zero).
+int sayram_batch_s::zero_region(long long begin, long long end) {
+  for (auto& a : cell_arrays)
+    SG_CUDA(cudaMemsetAsync((char*)a.first + begin * a.second, 0, (size_t)(end - begin) * a.second, stream));
+  return SAYRAM_OK;
+}
+
+// Places instance b at cell index `base` (cell (0,0); one pad row precedes it) with its tables
+// at the given offsets, uploads the tables and coefficients and runs the set-up kernel.
+int sayram_batch_s::place(int b, const sayram_problem& p, long long base, int xe_off, int ye_off,
+                          const int dir_off[4], long long hoff) {
+  InstDev& I = hinst[b];
+  std::memset(&I, 0, sizeof(I));
+  I.nx = p.nx;
+  I.ny = p.ny;
+  I.pitch = (int)round_up(p.nx, 4);
+  I.enabled = 1;
+  for (int s = 0; s < 4; ++s) I.bc[s] = p.bc[s];
+  I.base = base;
+  I.hoff = hoff;
+  I.ntx = (p.nx + sg::kTX - 1) / sg::kTX;
+  I.nty = (p.ny + sg::kTY - 1) / sg::kTY;
+  I.nchunks = (int)((round_up((long long)p.ny * I.pitch, 4) + sg::kChunk - 1) / sg::kChunk);
+  I.xe = xe_off;
+  I.ye = ye_off;
+  for (int s = 0; s < 4; ++s) I.dir[s] = p.bc[s] == SAYRAM_DIRICHLET ? dir_off[s] : -1;
+  I.dt = p.dt;
+  // tables: edges, bilinear weights of Solver.cc:333-336, Dirichlet vertex values
+  std::vector<double> wx(2 * (p.nx + 1), 0.0), wy(2 * (p.ny + 1), 0.0);
+  for (int i = 1; i < p.nx; ++i) {
+    const double xv = p.x_edges[i];
+    const double xl = 0.5 * (p.x_edges[i - 1] + p.x_edges[i]), xr = 0.5 * (p.x_edges[i] + p.x_edges[i + 1]);
+    wx[2 * i] = wide((xr - xv) / (xr - xl));
+    wx[2 * i + 1] = wide((xv - xl) / (xr - xl));
   }
+  for (int j = 1; j < p.ny; ++j) {
+    const double yv = p.y_edges[j];
+    const double yb = 0.5 * (p.y_edges[j - 1] + p.y_edges[j]), yt = 0.5 * (p.y_edges[j] + p.y_edges[j + 1]);
+    wy[2 * j] = wide((yt - yv) / (yt - yb));
+    wy[2 * j + 1] = wide((yv - yb) / (yt - yb));
+  }
+  SG_CUDA(cudaMemcpyAsync(d_xe + xe_off, p.x_edges, sizeof(double) * (p.nx + 1), cudaMemcpyHostToDevice, stream));
+  SG_CUDA(cudaMemcpyAsync(d_ye + ye_off, p.y_edges, sizeof(double) * (p.ny + 1), cudaMemcpyHostToDevice, stream));
+  SG_CUDA(cudaMemcpyAsync(d_wx + 2LL * xe_off, wx.data(), sizeof(double) * wx.size(), cudaMemcpyHostToDevice, stream));
+  SG_CUDA(cudaMemcpyAsync(d_wy + 2LL * ye_off, wy.data(), sizeof(double) * wy.size(), cudaMemcpyHostToDevice, stream));
+  for (int s = 0; s < 4; ++s)
+    if (I.dir[s] >= 0) {
+      const int m = (s <= 1) ? p.ny + 1 : p.nx + 1;
+      std::vector<double> v(m);
+      for (int k = 0; k < m; ++k) v[k] = wide(p.dirichlet[s][k]);
+      SG_CUDA(cudaMemcpyAsync(d_dirv + I.dir[s], v.data(), sizeof(double) * m, cudaMemcpyHostToDevice, stream));
+    }
+  SG_CUDA(cudaMemcpyAsync(d_inst + b, &I, sizeof(InstDev), cudaMemcpyHostToDevice, stream));
+  SG_CUDA(cudaMemsetAsync(d_st + b, 0, sizeof(InstState), stream));
+  return upload_instance(b, p, true, true);
+}
+
+// Work lists of the enabled instances, in slot order: 1024-cell chunks and 32x16 tiles.
+int sayram_batch_s::rebuild_lists() {
+  h_chunk.clear();
+  h_tile.clear();
+  int ninst = 0;
+  for (int b = 0; b < cap_slots; ++b) {
+    InstDev& I = hinst[b];
+    if (!I.enabled) continue;
+    ninst = b + 1;
+    I.chunk0 = (int)h_chunk.size();
+    for (int k = 0; k < I.nchunks; ++k) h_chunk.push_back(b);
+    I.tile0 = (int)h_tile.size();
+    for (int k = 0; k < I.ntx * I.nty; ++k) h_tile.push_back(b);
+  }
+  if ((int)h_chunk.size() > cap_chunks || (int)h_tile.size() > cap_tiles)
+    return fail(SAYRAM_ERR_STATE, "work lists exceed their capacity");
+  nchunks = (int)h_chunk.size();
+  ntiles = (int)h_tile.size();
+  n = std::max(n, ninst);
+  const int dyn[4] = {nchunks, ntiles, cap_slots, 0};
+  SG_CUDA(cudaMemcpyAsync(d_inst, hinst.data(), sizeof(InstDev) * cap_slots, cudaMemcpyHostToDevice, stream));
+  if (nchunks) SG_CUDA(cudaMemcpyAsync(d_chunk, h_chunk.data(), sizeof(int) * nchunks, cudaMemcpyHostToDevice, stream));
+  if (ntiles) SG_CUDA(cudaMemcpyAsync(d_tile, h_tile.data(), sizeof(int) * ntiles, cudaMemcpyHostToDevice, stream));
+  // the dyn counts travel by value too: pageable source, so the copy completes before return
+  SG_CUDA(cudaMemcpyAsync(d_dyn, dyn, sizeof(dyn), cudaMemcpyHostToDevice, stream));
+  SG_CUDA(cudaStreamSynchronize(stream));
+  cm.nchunks = nchunks;
+  cm.ntiles = ntiles;
+  cm.ninst = cap_slots;
+  return SAYRAM_OK;
+}
+
+int sayram_batch_s::build(const sayram_problem* probs, int count, const sayram_options* o) {
+  int rc = set_options(o);
+  if (rc) return rc;
+  for (int b = 0; b < count; ++b) {
+    rc = validate_problem(probs[b]);
+    if (rc) return fail(rc, "instance " + std::to_string(b) + ": " + g_err);
+  }
+  if ((rc = init_device())) return rc;
+  // compact layout: instances back to back, each with a pad row above and below
+  std::vector<long long> base(count), hoff(count);
+  std::vector<int> xoffv(count), yoffv(count), doffv(4 * count);
+  long long cursor = 0, h = 0, maxcells = 0;
+  int chunks = 0, tiles = 0, xoff = 0, yoff = 0, doff = 0;
+  for (int b = 0; b < count; ++b) {
+    const sayram_problem& p = probs[b];
+    const long long pitch = round_up(p.nx, 4);
+    base[b] = cursor + pitch;
+    cursor += round_up((long long)(p.ny + 2) * pitch, 32);
+    hoff[b] = h;
+    h += (long long)p.nx * p.ny;
+    chunks += (int)((round_up((long long)p.ny * pitch, 4) + sg::kChunk - 1) / sg::kChunk);
+    tiles += ((p.nx + sg::kTX - 1) / sg::kTX) * ((p.ny + sg::kTY - 1) / sg::kTY);
+    xoffv[b] = xoff;
+    xoff += p.nx + 1;
+    yoffv[b] = yoff;
+    yoff += p.ny + 1;
+    for (int s = 0; s < 4; ++s) {
+      doffv[4 * b + s] = doff;
+      if (p.bc[s] == SAYRAM_DIRICHLET) doff += (s <= 1) ? p.ny + 1 : p.nx + 1;
+    }
+    maxcells = std::max(maxcells, (long long)p.nx * p.ny);
+  }
+  nreal = h;
+  if ((rc = alloc_storage(cursor + 64, count, chunks, tiles, xoff, yoff, doff, std::max(6 * maxcells, nreal))))
+    return rc;
+  n = count;
+  for (int b = 0; b < count; ++b)
+    if ((rc = place(b, probs[b], base[b], xoffv[b], yoffv[b], &doffv[4 * b], hoff[b]))) return rc;
+  if ((rc = rebuild_lists())) return rc;
   SG_CUDA(cudaStreamSynchronize(stream));
   return SAYRAM_OK;
 }
@@ -528,6 +605,14 @@ int sayram_batch_s::build_graph(const sg::Coef<C>& cfull, const sg::Coef<T>& ck,
 }
 
 int sayram_batch_s::run_steps(int nsteps) {
+  int rc = launch_steps(nsteps);
+  if (rc) return rc;
+  SG_CUDA(cudaStreamSynchronize(stream));
+  if (timing) collect_timing();
+  return finish_status();
+}
+
+int sayram_batch_s::launch_steps(int nsteps) {
   if (nsteps < 0) return fail(SAYRAM_ERR_ARG, "nsteps must be >= 0");
   SG_CUDA(cudaSetDevice(dev));
   const bool use_graph = opt.use_graph && !timing;
@@ -553,9 +638,7 @@ int sayram_batch_s::run_steps(int nsteps) {
                      : step_once<double, double, sg::F64A>(c64, c64, k64);
     if (rc) return rc;
   }
-  SG_CUDA(cudaStreamSynchronize(stream));
-  if (timing) collect_timing();
-  return finish_status();
+  return SAYRAM_OK;
 }
 
 int sayram_batch_s::finish_status() {
@@ -870,6 +953,336 @@ int sayram_set_coeffs(sayram_solver s, const double* G, const double* Dxx, const
 }
 int sayram_get_stats(sayram_solver s, sayram_stats* out) { return sayram_batch_stats(s, 0, out); }
 void sayram_destroy(sayram_solver s) { sayram_batch_destroy(s); }
+
+}  // extern "C"
+
+
+// ================================================================================== server
+namespace {
+
+double now_seconds() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct Request {
+  long long id = 0;
+  int nsteps = 0;
+  double t_submit = 0.0;
+  sayram_problem p{};
+  std::vector<double> xe, ye, G, Dxx, Dxy, Dyy, itau, f0, dir[4];
+  void own(const sayram_problem& q) {
+    const size_t nc = (size_t)q.nx * q.ny;
+    xe.assign(q.x_edges, q.x_edges + q.nx + 1);
+    ye.assign(q.y_edges, q.y_edges + q.ny + 1);
+    G.assign(q.G, q.G + nc);
+    Dxx.assign(q.Dxx, q.Dxx + nc);
+    Dxy.assign(q.Dxy, q.Dxy + nc);
+    Dyy.assign(q.Dyy, q.Dyy + nc);
+    itau.assign(q.inv_tau, q.inv_tau + nc);
+    f0.assign(q.f0, q.f0 + nc);
+    p = q;
+    p.x_edges = xe.data();
+    p.y_edges = ye.data();
+    p.G = G.data();
+    p.Dxx = Dxx.data();
+    p.Dxy = Dxy.data();
+    p.Dyy = Dyy.data();
+    p.inv_tau = itau.data();
+    p.f0 = f0.data();
+    for (int s = 0; s < 4; ++s) {
+      if (q.bc[s] == SAYRAM_DIRICHLET) {
+        const int m = (s <= 1) ? q.ny + 1 : q.nx + 1;
+        dir[s].assign(q.dirichlet[s], q.dirichlet[s] + m);
+        p.dirichlet[s] = dir[s].data();
+      } else {
+        p.dirichlet[s] = nullptr;
+      }
+    }
+  }
+};
+
+struct Result {
+  std::vector<double> f;
+  sayram_stats st{};
+  double t_submit = 0.0, t_done = 0.0;
+};
+
+long long region_cells(int nx, int ny) { return round_up((long long)(ny + 2) * round_up(nx, 4), 32); }
+
+}  // namespace
+
+struct sayram_server_s {
+  sayram_batch_s eng;
+  sayram_server_config cfg{};
+  long long arena = 0;
+  std::map<long long, long long> free_;  // offset -> length (cells), coalesced
+  struct Slot {
+    bool used = false;
+    long long id = 0, begin = 0, len = 0;
+    int nsteps = 0, done = 0, nx = 0, ny = 0;
+    double t_submit = 0.0;
+  };
+  std::vector<Slot> slots;
+  std::deque<Request*> waiting;
+  std::map<long long, Result> results;
+  long long next_id = 1;
+  sayram_server_info info{};
+  bool dirty = false;
+
+  ~sayram_server_s() {
+    for (Request* r : waiting) delete r;
+  }
+
+  bool take(long long len, long long* off) {  // first fit
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+      if (it->second >= len) {
+        *off = it->first;
+        const long long rest = it->second - len, start = it->first + len;
+        free_.erase(it);
+        if (rest > 0) free_[start] = rest;
+        return true;
+      }
+    }
+    return false;
+  }
+  void give(long long off, long long len) {
+    auto it = free_.emplace(off, len).first;
+    auto nx = std::next(it);
+    if (nx != free_.end() && it->first + it->second == nx->first) {
+      it->second += nx->second;
+      free_.erase(nx);
+    }
+    if (it != free_.begin()) {
+      auto pv = std::prev(it);
+      if (pv->first + pv->second == it->first) {
+        pv->second += it->second;
+        free_.erase(it);
+      }
+    }
+  }
+
+  int admit_one(Request* r, int slot, long long off) {
+    const int ms = cfg.max_side + 1;
+    int dir_off[4];
+    for (int s2 = 0; s2 < 4; ++s2) dir_off[s2] = (slot * 4 + s2) * ms;
+    const long long len = region_cells(r->p.nx, r->p.ny);
+    int rc = eng.zero_region(off, off + len);
+    if (rc) return rc;
+    rc = eng.place(slot, r->p, off + round_up(r->p.nx, 4), slot * ms, slot * ms, dir_off, 0);
+    if (rc) return rc;
+    Slot& S = slots[slot];
+    S.used = true;
+    S.id = r->id;
+    S.begin = off;
+    S.len = len;
+    S.nsteps = r->nsteps;
+    S.done = 0;
+    S.nx = r->p.nx;
+    S.ny = r->p.ny;
+    S.t_submit = r->t_submit;
+    info.admitted++;
+    info.resident++;
+    info.arena_cells_used += (double)len;
+    return SAYRAM_OK;
+  }
+
+  int admit() {
+    int scanned = 0;
+    for (auto it = waiting.begin(); it != waiting.end() && scanned < 9;) {
+      Request* r = *it;
+      int slot = -1;
+      for (int k = 0; k < cfg.max_slots; ++k)
+        if (!slots[k].used) {
+          slot = k;
+          break;
+        }
+      if (slot < 0) break;
+      long long off;
+      if (!take(region_cells(r->p.nx, r->p.ny), &off)) {
+        ++it;
+        ++scanned;
+        continue;
+      }
+      int rc = admit_one(r, slot, off);
+      if (rc) return rc;
+      delete r;
+      it = waiting.erase(it);
+      info.waiting--;
+      dirty = true;
+    }
+    return SAYRAM_OK;
+  }
+
+  int tick(int* ncomp) {
+    if (ncomp) *ncomp = 0;
+    SG_CUDA(cudaSetDevice(eng.dev));
+    const double t0 = now_seconds();
+    int rc = admit();
+    if (rc) return rc;
+    if (dirty) {
+      if ((rc = eng.rebuild_lists())) return rc;
+      dirty = false;
+    }
+    if (info.resident == 0) return SAYRAM_OK;
+    if ((rc = eng.launch_steps(1))) return rc;
+    info.ticks++;
+    info.instance_steps += info.resident;
+    // completions: state rows back to the host, then free the slot
+    std::vector<int> fin;
+    for (int k = 0; k < cfg.max_slots; ++k)
+      if (slots[k].used && ++slots[k].done >= slots[k].nsteps) fin.push_back(k);
+    std::vector<std::vector<double>> rows(fin.size());
+    std::vector<InstState> sts(fin.size());
+    for (size_t q = 0; q < fin.size(); ++q) {
+      const InstDev& I = eng.hinst[fin[q]];
+      rows[q].resize((size_t)I.ny * I.pitch);
+      SG_CUDA(cudaMemcpyAsync(rows[q].data(), eng.fl.f + I.base, sizeof(double) * rows[q].size(),
+                              cudaMemcpyDeviceToHost, eng.stream));
+      SG_CUDA(cudaMemcpyAsync(&sts[q], eng.d_st + fin[q], sizeof(InstState), cudaMemcpyDeviceToHost, eng.stream));
+    }
+    SG_CUDA(cudaStreamSynchronize(eng.stream));
+    const double t1 = now_seconds();
+    info.busy_seconds += t1 - t0;
+    for (size_t q = 0; q < fin.size(); ++q) {
+      Slot& S = slots[fin[q]];
+      InstDev& I = eng.hinst[fin[q]];
+      Result& R = results[S.id];
+      R.f.resize((size_t)S.nx * S.ny);
+      for (int i = 0; i < S.nx; ++i)
+        for (int j = 0; j < S.ny; ++j) R.f[(size_t)i * S.ny + j] = eng.unwide(rows[q][(size_t)j * I.pitch + i]);
+      const InstState& hs = sts[q];
+      R.st.steps = hs.steps;
+      R.st.t = (double)hs.steps * I.dt;
+      R.st.status = hs.status == sg::ST_NEGATIVE ? SAYRAM_ERR_NEGATIVE
+                    : hs.status == sg::ST_NOT_CONVERGED ? SAYRAM_ERR_NOT_CONVERGED : SAYRAM_OK;
+      R.st.refinements = hs.refines;
+      R.st.iterations = hs.iters_total;
+      R.st.rel_residual = hs.rel;
+      R.st.min_f = hs.min_f;
+      R.st.clamped = hs.clamped;
+      R.st.mass_drift = hs.mass_drift;
+      R.st.total_iterations = hs.cum_iters;
+      R.st.total_refinements = hs.cum_refines;
+      R.t_submit = S.t_submit;
+      R.t_done = t1;
+      I.enabled = 0;
+      give(S.begin, S.len);
+      info.arena_cells_used -= (double)S.len;
+      S.used = false;
+      info.resident--;
+      info.completed++;
+      dirty = true;
+    }
+    if (ncomp) *ncomp = (int)fin.size();
+    return SAYRAM_OK;
+  }
+};
+
+extern "C" {
+
+int sayram_server_create(const sayram_server_config* cfg, const sayram_options* opt, sayram_server* out) {
+  if (!out || !cfg) return fail(SAYRAM_ERR_ARG, "null config or output handle");
+  *out = nullptr;
+  sayram_server_config c = *cfg;
+  if (c.max_slots <= 0) c.max_slots = 4096;
+  if (c.max_side <= 0) c.max_side = 1024;
+  if (!(c.hbm_budget_bytes > 0)) return fail(SAYRAM_ERR_ARG, "HBM budget must be positive");
+  sayram_server_s* s = new (std::nothrow) sayram_server_s();
+  if (!s) return fail(SAYRAM_ERR_OOM, "host allocation failed");
+  s->cfg = c;
+  sayram_batch_s& e = s->eng;
+  int rc = e.set_options(opt);
+  if (!rc) rc = e.init_device();
+  if (rc) {
+    std::string m = g_err;
+    delete s;
+    return fail(rc, m);
+  }
+  // budget split: per-slot tables, staging, work lists, then the cell arena
+  const long long ms = c.max_side + 1;
+  const double table_bytes = (double)c.max_slots * ms * (1 + 1 + 2 + 2 + 4) * 8.0;
+  const double stage_bytes = 6.0 * (double)c.max_side * c.max_side * 8.0;
+  const double per_cell = (double)sayram_instance_bytes(64, 64, e.opt.precision) /
+                          (double)region_cells(64, 64);  // bytes per arena cell (all arrays)
+  const double avail = c.hbm_budget_bytes - table_bytes - stage_bytes - 64.0 * 1048576.0;
+  const long long cells = (long long)(avail / (per_cell + 4.0 / 1024 * 2 + 8.0 * 4 / 1024));
+  if (cells < region_cells(1, 1) + 64) {
+    delete s;
+    return fail(SAYRAM_ERR_BUDGET, "HBM budget too small for any instance");
+  }
+  const long long side_tiles = (long long)c.max_slots * (c.max_side / sg::kTX + c.max_side / sg::kTY + 2);
+  const int chunks_cap = (int)std::min<long long>(cells / sg::kChunk + c.max_slots + 1, 1LL << 30);
+  const int tiles_cap = (int)std::min<long long>(cells / (sg::kTX * sg::kTY) + side_tiles, 1LL << 30);
+  rc = e.alloc_storage(cells + 64, c.max_slots, chunks_cap, tiles_cap, (long long)c.max_slots * ms,
+                       (long long)c.max_slots * ms, 4LL * c.max_slots * ms,
+                       std::max<long long>(6LL * c.max_side * c.max_side, 1));
+  if (rc) {
+    std::string m = g_err;
+    delete s;
+    return fail(rc, m);
+  }
+  e.n = c.max_slots;
+  if ((rc = e.rebuild_lists())) {
+    std::string m = g_err;
+    delete s;
+    return fail(rc, m);
+  }
+  s->arena = cells;
+  s->free_[0] = cells;
+  s->slots.resize(c.max_slots);
+  s->info.arena_cells = (double)cells;
+  s->info.device_bytes = (double)e.bytes;
+  *out = s;
+  g_err.clear();
+  return SAYRAM_OK;
+}
+
+int sayram_server_submit(sayram_server s, const sayram_problem* p, int nsteps, long long* id_out) {
+  if (!s || !p || nsteps < 1) return fail(SAYRAM_ERR_ARG, "bad server, problem or step count");
+  int rc = validate_problem(*p);
+  if (rc) return rc;
+  if (p->nx > s->cfg.max_side || p->ny > s->cfg.max_side)
+    return fail(SAYRAM_ERR_BUDGET, "grid side exceeds the server's max_side");
+  if (region_cells(p->nx, p->ny) > s->arena) return fail(SAYRAM_ERR_BUDGET, "request larger than the HBM budget");
+  Request* r = new (std::nothrow) Request();
+  if (!r) return fail(SAYRAM_ERR_OOM, "host allocation failed");
+  r->own(*p);
+  r->nsteps = nsteps;
+  r->id = s->next_id++;
+  r->t_submit = now_seconds();
+  s->waiting.push_back(r);
+  s->info.submitted++;
+  s->info.waiting++;
+  if (id_out) *id_out = r->id;
+  return SAYRAM_OK;
+}
+
+int sayram_server_tick(sayram_server s, int* n_completed) {
+  if (!s) return fail(SAYRAM_ERR_ARG, "null server");
+  return s->tick(n_completed);
+}
+
+int sayram_server_poll(sayram_server s, long long id, double* f_out, sayram_stats* st, double* t_submit,
+                       double* t_done) {
+  if (!s) return fail(SAYRAM_ERR_ARG, "null server");
+  auto it = s->results.find(id);
+  if (it == s->results.end()) return fail(SAYRAM_ERR_STATE, "request not completed");
+  if (f_out) std::memcpy(f_out, it->second.f.data(), sizeof(double) * it->second.f.size());
+  if (st) *st = it->second.st;
+  if (t_submit) *t_submit = it->second.t_submit;
+  if (t_done) *t_done = it->second.t_done;
+  s->results.erase(it);
+  return SAYRAM_OK;
+}
+
+int sayram_server_info_get(sayram_server s, sayram_server_info* out) {
+  if (!s || !out) return fail(SAYRAM_ERR_ARG, "null server or output");
+  *out = s->info;
+  out->device_bytes = (double)s->eng.bytes;
+  return SAYRAM_OK;
+}
+
+void sayram_server_destroy(sayram_server s) { delete s; }
 
 }  // extern "C"
 

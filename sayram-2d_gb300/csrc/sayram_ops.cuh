@@ -38,11 +38,18 @@ struct Common {
   const double* wy;    // per vertex row: (wB, wT)
   const double* dirv;  // Dirichlet vertex values
   double* part;        // 4 doubles per chunk
+  // when set, [nchunks, ntiles, ninst] are read from device memory (lists that change between
+  // steps, as in the server) instead of the by-value counts above
+  const int* dyn;
   // device-side loops of the per-step CUDA graph (use_cond = 0: the host drives the loops)
   unsigned long long h_outer, h_inner;  // cudaGraphConditionalHandle of the two WHILE nodes
   int use_cond;
   int guard_refine, guard_iters;  // hard caps on loop trips, whatever the bookkeeping says
 };
+
+__device__ __forceinline__ int n_chunks(const Common& cm) { return cm.dyn ? cm.dyn[0] : cm.nchunks; }
+__device__ __forceinline__ int n_tiles(const Common& cm) { return cm.dyn ? cm.dyn[1] : cm.ntiles; }
+__device__ __forceinline__ int n_inst(const Common& cm) { return cm.dyn ? cm.dyn[2] : cm.ninst; }
 
 // The last block of a loop-deciding kernel sets the graph's WHILE conditions from the number of
 // instances still active. The trip counters make both loops terminate after guard_refine
@@ -271,7 +278,7 @@ __global__ void k_setup(Common cm, Geo geo, double* f, const double* stage, cons
 template <typename A>
 __global__ void k_field_in(Common cm, double* dst, const double* src) {
   count_launch(cm.ctl);
-  for (int t = blockIdx.x; t < cm.ntiles; t += gridDim.x) {
+  for (int t = blockIdx.x, nt_ = n_tiles(cm); t < nt_; t += gridDim.x) {
     const int b = cm.tile_inst[t];
     const InstDev I = cm.inst[b];
     if (!I.enabled) continue;
@@ -287,7 +294,7 @@ __global__ void k_field_in(Common cm, double* dst, const double* src) {
 template <typename A>
 __global__ void k_field_out(Common cm, double* dst, const double* src) {
   count_launch(cm.ctl);
-  for (int t = blockIdx.x; t < cm.ntiles; t += gridDim.x) {
+  for (int t = blockIdx.x, nt_ = n_tiles(cm); t < nt_; t += gridDim.x) {
     const int b = cm.tile_inst[t];
     const InstDev I = cm.inst[b];
     if (!I.enabled) continue;
@@ -303,7 +310,7 @@ __global__ void k_field_out(Common cm, double* dst, const double* src) {
 // ------------------------------------------------------------------------------ step control
 __global__ void k_begin(Common cm) {
   count_launch(cm.ctl);
-  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < cm.ninst; b += gridDim.x * blockDim.x) {
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x, ni_ = n_inst(cm); b < ni_; b += gridDim.x * blockDim.x) {
     InstState& s = cm.st[b];
     const bool on = cm.inst[b].enabled != 0;
     s.outer_active = on ? 1 : 0;
@@ -385,7 +392,7 @@ __global__ void __launch_bounds__(kAsmThreads) k_assemble(Common cm, Geo geo, Fi
   __shared__ V xL[kTY][VX], xR[kTY][VX], xB[kTY][VX];  // x-faces: left/right outflow, R part
   __shared__ V yB[VY][kTX], yT[VY][kTX], yR[VY][kTX];  // y-faces: below/above outflow, R part
   const V zero = A::k(0.0);
-  for (int t = blockIdx.x; t < cm.ntiles; t += gridDim.x) {
+  for (int t = blockIdx.x, nt_ = n_tiles(cm); t < nt_; t += gridDim.x) {
     const int b = cm.tile_inst[t];
     const InstDev I = cm.inst[b];
     if (!I.enabled) continue;  // uniform in the block
@@ -620,7 +627,7 @@ __global__ void __launch_bounds__(kThreads) k_resid(Common cm, Fields fl, Coef<C
                                                      double tol, double inner_tol, int max_refine) {
   using V = typename A::V;
   count_launch(cm.ctl);
-  for (int c = blockIdx.x; c < cm.nchunks; c += gridDim.x) {
+  for (int c = blockIdx.x, nc_ = n_chunks(cm); c < nc_; c += gridDim.x) {
     const int b = cm.chunk_inst[c];
     InstState& st = cm.st[b];
     if (!st.outer_active) continue;
@@ -704,7 +711,7 @@ __global__ void __launch_bounds__(kThreads) k_resid(Common cm, Fields fl, Coef<C
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_bicg1(Common cm, Coef<T> co, Kry<T> kr) {
   count_launch(cm.ctl);
-  for (int c = blockIdx.x; c < cm.nchunks; c += gridDim.x) {
+  for (int c = blockIdx.x, nc_ = n_chunks(cm); c < nc_; c += gridDim.x) {
     const int b = cm.chunk_inst[c];
     InstState& st = cm.st[b];
     if (!st.inner_active) continue;
@@ -769,7 +776,7 @@ __global__ void __launch_bounds__(kThreads) k_bicg1(Common cm, Coef<T> co, Kry<T
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_bicg2(Common cm, Coef<T> co, Kry<T> kr) {
   count_launch(cm.ctl);
-  for (int c = blockIdx.x; c < cm.nchunks; c += gridDim.x) {
+  for (int c = blockIdx.x, nc_ = n_chunks(cm); c < nc_; c += gridDim.x) {
     const int b = cm.chunk_inst[c];
     InstState& st = cm.st[b];
     if (!st.inner_active) continue;
@@ -817,7 +824,7 @@ __global__ void __launch_bounds__(kThreads) k_bicg2(Common cm, Coef<T> co, Kry<T
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_bicg3(Common cm, Kry<T> kr, int max_iters) {
   count_launch(cm.ctl);
-  for (int c = blockIdx.x; c < cm.nchunks; c += gridDim.x) {
+  for (int c = blockIdx.x, nc_ = n_chunks(cm); c < nc_; c += gridDim.x) {
     const int b = cm.chunk_inst[c];
     InstState& st = cm.st[b];
     if (!st.inner_active) continue;
@@ -881,7 +888,7 @@ __global__ void __launch_bounds__(kThreads) k_polish(Common cm, Fields fl, Coef<
   using V = typename A::V;
   count_launch(cm.ctl);
   __shared__ float smin[kThreads / 32];
-  for (int c = blockIdx.x; c < cm.nchunks; c += gridDim.x) {
+  for (int c = blockIdx.x, nc_ = n_chunks(cm); c < nc_; c += gridDim.x) {
     const int b = cm.chunk_inst[c];
     InstState& st = cm.st[b];
     const InstDev I = cm.inst[b];

@@ -1,0 +1,90 @@
+"""Serving (continuous batching): requests of different grid sizes and step counts arrive while
+others run; each result must equal the same request run alone (FP64: 1e-12, FP32 modes: 1e-8 in
+relative L2), admission respects the HBM budget, and oversized requests are refused."""
+import numpy as np
+import pytest
+
+from sayram2d_gb300 import cases
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def _alone(capi, p, nsteps, prec):
+    s = capi.Solver(p, precision=prec)
+    s.step(nsteps)
+    f = s.f()
+    s.close()
+    return f
+
+
+def _requests():
+    shapes = [(40, 33, 7), (96, 80, 12), (33, 64, 3), (128, 120, 9), (64, 64, 15), (17, 23, 5)]
+    return [(cases.synthetic_problem(a, e, 1e-2, seed=100 + k, tau=0.3 + 0.2 * k), n)
+            for k, (a, e, n) in enumerate(shapes)]
+
+
+@pytest.mark.parametrize("prec,tol", [(0, 1e-12), (2, 1e-8), (1, 1e-8)])
+def test_same_alone_and_in_the_mix(capi, prec, tol):
+    reqs = _requests()
+    srv = capi.Server(2e9, max_slots=16, max_side=256, precision=prec)
+    ids = {}
+    # staggered arrivals: two at once, then one per tick while the others run
+    ids[srv.submit(*reqs[0])] = 0
+    ids[srv.submit(*reqs[1])] = 1
+    pending = list(range(2, len(reqs)))
+    got = {}
+    for _ in range(200):
+        if pending:
+            k = pending.pop(0)
+            ids[srv.submit(*reqs[k])] = k
+        srv.tick()
+        for rid in list(ids):
+            r = srv.poll(rid)
+            if r is not None:
+                got[ids.pop(rid)] = r
+        if not ids and not pending:
+            break
+    info = srv.info()
+    srv.close()
+    assert len(got) == len(reqs) and info["completed"] == len(reqs)
+    for k, (p, n) in enumerate(reqs):
+        f, st, t0, t1 = got[k]
+        assert st["steps"] == n and t1 >= t0
+        assert f.min() >= 0.0 and st["min_f"] >= 0.0
+        assert rel(f, _alone(capi, p, n, prec)) <= tol, (prec, k)
+
+
+def test_admission_waits_for_memory(capi):
+    """A budget that holds about one instance: later requests wait, then run, all correct."""
+    reqs = _requests()[:3]
+    per = capi.instance_bytes(128, 128, capi.FP32_REFINE_DW)
+    srv = capi.Server(per * 1.5 + 400e6, max_slots=8, max_side=128, precision=capi.FP32_REFINE_DW)
+    ids = {srv.submit(p, n): k for k, (p, n) in enumerate(reqs)}
+    srv.tick()
+    info = srv.info()
+    assert info["resident"] >= 1 and info["waiting"] >= 1
+    got = {}
+    for _ in range(200):
+        srv.tick()
+        for rid in list(ids):
+            r = srv.poll(rid)
+            if r is not None:
+                got[ids.pop(rid)] = r
+        if not ids:
+            break
+    srv.close()
+    assert len(got) == 3
+    for k, (p, n) in enumerate(reqs):
+        assert rel(got[k][0], _alone(capi, p, n, capi.FP32_REFINE_DW)) <= 1e-8
+
+
+def test_oversized_request_refused(capi):
+    srv = capi.Server(600e6, max_slots=4, max_side=64, precision=capi.FP32_REFINE_DW)
+    p = cases.synthetic_problem(100, 50, 1e-2, seed=1)
+    with pytest.raises(RuntimeError, match="max_side"):
+        srv.submit(p, 3)
+    srv.close()
