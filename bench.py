@@ -58,6 +58,10 @@ def parse():
     ap.add_argument("--plain-sample", type=int, default=64)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--quick", action="store_true", help="skip the plain/FP64/e2e/CPU side measurements")
+    ap.add_argument("--serve-requests", type=int, default=600, help="requests in the serving run (0: skip)")
+    ap.add_argument("--serve-rate", type=float, default=30.0, help="Poisson arrival rate (requests/s)")
+    ap.add_argument("--serve-budget-gb", type=float, default=150.0)
+    ap.add_argument("--serve-only", action="store_true")
     ap.add_argument("--precision", choices=["dw", "fp64res"], default="dw",
                     help="refinement arithmetic of the headline: double-word (FP32 pairs) or IEEE FP64")
     return ap.parse_args()
@@ -248,6 +252,59 @@ def kernel_roofline(b, probs, peak, steps=2):
     return roof, out
 
 
+def serving_requests(nreq, rate, seed):
+    """Seeded request stream: Poisson arrivals at `rate`, n log-uniform in [32, 512] (n x n grid),
+    steps log-uniform in [10, 2000], seeded D fields, rho and tau per request."""
+    rng = np.random.default_rng([seed, 4242])
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=nreq))
+    n = np.rint(np.exp(rng.uniform(np.log(32), np.log(512), size=nreq))).astype(int)
+    steps = np.rint(np.exp(rng.uniform(np.log(10), np.log(2000), size=nreq))).astype(int)
+    probs = []
+    for k in range(nreq):
+        r = np.random.default_rng([seed, k, 99])
+        probs.append(cases.synthetic_problem(int(n[k]), int(n[k]), DT, seed=seed * 104729 + k,
+                                             tau=float(10.0 ** r.uniform(-1, 1)), rho=float(r.uniform(-0.9, 0.9))))
+    return arrivals, probs, steps
+
+
+def run_serving(capi, arrivals, probs, steps, precision, budget_gb):
+    """Drives a server in real time: submits each request at its arrival time, ticks, polls.
+    Latency = result ready - arrival time (both on the monotonic clock)."""
+    srv = capi.Server(budget_gb * 1e9, max_slots=4096, max_side=512, precision=precision)
+    nreq = len(probs)
+    t0 = time.monotonic()
+    nxt, live, lat, min_f, not_conv = 0, {}, [], float("inf"), 0
+    while len(lat) < nreq:
+        now = time.monotonic() - t0
+        while nxt < nreq and arrivals[nxt] <= now:
+            live[srv.submit(probs[nxt], int(steps[nxt]))] = nxt
+            nxt += 1
+        info = srv.info()
+        if info["resident"] == 0 and info["waiting"] == 0:
+            if nxt < nreq:
+                time.sleep(max(0.0, arrivals[nxt] - (time.monotonic() - t0)))
+            continue
+        if srv.tick() > 0:
+            for rid in list(live):
+                r = srv.poll(rid, want_f=False)
+                if r is not None:
+                    k = live.pop(rid)
+                    _, st, ts, td = r
+                    lat.append(td - (t0 + arrivals[k]))
+                    min_f = min(min_f, st["min_f"])
+                    not_conv += int(st["status"] != 0)
+    wall = time.monotonic() - t0
+    info = srv.info()
+    srv.close()
+    lat = np.array(lat) * 1e3
+    return {"requests": nreq, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "mean_ms": float(lat.mean()), "wall_s": wall,
+            "instance_steps_per_s": info["instance_steps"] / wall,
+            "cell_steps_per_s": float(sum(p.nx * p.ny * int(s) for p, s in zip(probs, steps))) / wall,
+            "requests_per_s": nreq / wall, "ticks": info["ticks"], "busy_s": info["busy_seconds"],
+            "min_f": min_f, "not_converged": not_conv, "device_gb": info["device_bytes"] / 1e9}
+
+
 def run_ours(a):
     from sayram2d_gb300 import build, capi
 
@@ -359,6 +416,15 @@ def run_ours(a):
         line["cpu_baseline"] = cpu_baseline_single(a.seed, a.instances, a.cpu_seconds)
     else:
         b.close()
+    if a.serve_requests > 0:
+        arr, sprobs, ssteps = serving_requests(a.serve_requests, a.serve_rate, a.seed)
+        cfg = (f"{a.serve_requests} Poisson requests at {a.serve_rate}/s, n~logU[32,512] (n x n), "
+               f"steps~logU[10,2000], dt={DT} day, HBM budget {a.serve_budget_gb} GB")
+        line["serving"] = {"config": cfg, "precision": "fp32_refine_dw",
+                           **run_serving(capi, arr, sprobs, ssteps, capi.FP32_REFINE_DW, a.serve_budget_gb)}
+        if not a.quick:
+            line["serving_plain_fp64"] = {"config": cfg, "precision": "fp64",
+                                          **run_serving(capi, arr, sprobs, ssteps, capi.FP64, a.serve_budget_gb)}
     print(json.dumps(line))
 
 

@@ -59,14 +59,19 @@ def test_same_alone_and_in_the_mix(capi, prec, tol):
 
 
 def test_admission_waits_for_memory(capi):
-    """A budget that holds about one instance: later requests wait, then run, all correct."""
-    reqs = _requests()[:3]
-    per = capi.instance_bytes(128, 128, capi.FP32_REFINE_DW)
-    srv = capi.Server(per * 1.5 + 400e6, max_slots=8, max_side=128, precision=capi.FP32_REFINE_DW)
-    ids = {srv.submit(p, n): k for k, (p, n) in enumerate(reqs)}
+    """An arena that holds one instance but not two: later requests wait, then run, all correct."""
+    probe = capi.Server(80e6, max_slots=8, max_side=128, precision=capi.FP32_REFINE_DW)
+    arena = probe.info()["arena_cells"]
+    probe.close()
+    region = lambda n: ((n + 2) * ((n + 3) // 4 * 4) + 31) // 32 * 32
+    n = max(k for k in range(8, 129) if region(k) <= arena)
+    assert 2 * region(n) > arena
+    reqs = [(cases.synthetic_problem(n, n, 1e-2, seed=200 + k), 3 + k) for k in range(3)]
+    srv = capi.Server(80e6, max_slots=8, max_side=128, precision=capi.FP32_REFINE_DW)
+    ids = {srv.submit(p, m): k for k, (p, m) in enumerate(reqs)}
     srv.tick()
     info = srv.info()
-    assert info["resident"] >= 1 and info["waiting"] >= 1
+    assert info["resident"] == 1 and info["waiting"] == 2
     got = {}
     for _ in range(200):
         srv.tick()
@@ -78,8 +83,8 @@ def test_admission_waits_for_memory(capi):
             break
     srv.close()
     assert len(got) == 3
-    for k, (p, n) in enumerate(reqs):
-        assert rel(got[k][0], _alone(capi, p, n, capi.FP32_REFINE_DW)) <= 1e-8
+    for k, (p, m) in enumerate(reqs):
+        assert rel(got[k][0], _alone(capi, p, m, capi.FP32_REFINE_DW)) <= 1e-8
 
 
 def test_oversized_request_refused(capi):
