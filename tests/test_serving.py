@@ -60,14 +60,19 @@ def test_same_alone_and_in_the_mix(capi, prec, tol):
 
 def test_admission_waits_for_memory(capi):
     """An arena that holds one instance but not two: later requests wait, then run, all correct."""
-    probe = capi.Server(80e6, max_slots=8, max_side=128, precision=capi.FP32_REFINE_DW)
-    arena = probe.info()["arena_cells"]
-    probe.close()
     region = lambda n: ((n + 2) * ((n + 3) // 4 * 4) + 31) // 32 * 32
-    n = max(k for k in range(8, 129) if region(k) <= arena)
-    assert 2 * region(n) > arena
+    n = 64
+    budget = None
+    for b in np.arange(60e6, 90e6, 0.25e6):  # find a budget whose arena fits one 64x64, not two
+        probe = capi.Server(float(b), max_slots=8, max_side=128, precision=capi.FP32_REFINE_DW)
+        arena = probe.info()["arena_cells"]
+        probe.close()
+        if region(n) <= arena < 2 * region(n):
+            budget = float(b)
+            break
+    assert budget is not None
     reqs = [(cases.synthetic_problem(n, n, 1e-2, seed=200 + k), 3 + k) for k in range(3)]
-    srv = capi.Server(80e6, max_slots=8, max_side=128, precision=capi.FP32_REFINE_DW)
+    srv = capi.Server(budget, max_slots=8, max_side=128, precision=capi.FP32_REFINE_DW)
     ids = {srv.submit(p, m): k for k, (p, m) in enumerate(reqs)}
     srv.tick()
     info = srv.info()
