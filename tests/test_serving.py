@@ -63,8 +63,11 @@ def test_admission_waits_for_memory(capi):
     region = lambda n: ((n + 2) * ((n + 3) // 4 * 4) + 31) // 32 * 32
     n = 64
     budget = None
-    for b in np.arange(60e6, 90e6, 0.25e6):  # find a budget whose arena fits one 64x64, not two
-        probe = capi.Server(float(b), max_slots=8, max_side=128, precision=capi.FP32_REFINE_DW)
+    for b in np.arange(68e6, 90e6, 0.25e6):  # find a budget whose arena fits one 64x64, not two
+        try:
+            probe = capi.Server(float(b), max_slots=8, max_side=128, precision=capi.FP32_REFINE_DW)
+        except RuntimeError:  # below the server's fixed reserve
+            continue
         arena = probe.info()["arena_cells"]
         probe.close()
         if region(n) <= arena < 2 * region(n):
