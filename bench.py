@@ -62,6 +62,9 @@ def parse():
     ap.add_argument("--serve-rate", type=float, default=30.0, help="Poisson arrival rate (requests/s)")
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
     ap.add_argument("--serve-only", action="store_true")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="host-driven loops instead of the per-step CUDA graph (for ncu, which cannot profile "
+                         "kernels inside graphs with conditional nodes)")
     ap.add_argument("--precision", choices=["dw", "fp64res"], default="dw",
                     help="refinement arithmetic of the headline: double-word (FP32 pairs) or IEEE FP64")
     return ap.parse_args()
@@ -316,7 +319,7 @@ def run_ours(a):
     ncells = int(sum(p.nx * p.ny for p in probs))
     prec = capi.FP32_REFINE_DW if a.precision == "dw" else capi.FP32_REFINE
     other = capi.FP32_REFINE if a.precision == "dw" else capi.FP32_REFINE_DW
-    b = capi.Batch(probs, precision=prec)
+    b = capi.Batch(probs, precision=prec, use_graph=0 if a.no_graph else 1)
     for _ in range(a.warmup):
         b.step(1, allow_not_converged=True)
     l0 = b.launches()

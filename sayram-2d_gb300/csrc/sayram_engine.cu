@@ -52,6 +52,7 @@ struct sayram_batch_s {
   std::vector<InstDev> hinst;
   long long ncell = 0;      // padded storage cells (capacity)
   int cap_slots = 0, cap_chunks = 0, cap_tiles = 0;
+  int pmax = 4;             // widest row pitch the SpMV kernels must stage
   int* d_dyn = nullptr;     // [nchunks, ntiles, ninst] read by the kernels
   std::vector<int> h_chunk, h_tile;
   std::vector<std::pair<void*, int>> cell_arrays;  // every per-cell array and its element size
@@ -173,6 +174,17 @@ struct sayram_batch_s {
   }
 
   int grid_stream() const { return std::max(1, std::min(cap_chunks, nsm * 16)); }
+  // dynamic shared memory of the SpMV kernels: the chunk plus one row above and below
+  template <typename T>
+  size_t smem_spmv() const { return (size_t)(sg::kChunk + 2 * pmax) * sizeof(T); }
+  template <typename T>
+  int prep_spmv() {
+    const int bytes = (int)smem_spmv<T>();
+    if (bytes > 227 * 1024) return fail(SAYRAM_ERR_ARG, "rows too wide for the shared-memory stencil");
+    SG_CUDA(cudaFuncSetAttribute(sg::k_bicg1<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    SG_CUDA(cudaFuncSetAttribute(sg::k_bicg2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    return SAYRAM_OK;
+  }
   int grid_tiles() const { return std::max(1, std::min(cap_tiles, nsm * 8)); }
 
   int build(const sayram_problem* probs, int count, const sayram_options* o);
@@ -351,6 +363,10 @@ int sayram_batch_s::place(int b, const sayram_problem& p, long long base, int xe
   I.nx = p.nx;
   I.ny = p.ny;
   I.pitch = (int)round_up(p.nx, 4);
+  if (I.pitch > pmax) {
+    if (gexec) return fail(SAYRAM_ERR_STATE, "instance wider than the rows the step graph was built for");
+    pmax = I.pitch;
+  }
   I.enabled = 1;
   for (int s = 0; s < 4; ++s) I.bc[s] = p.bc[s];
   I.base = base;
@@ -501,6 +517,8 @@ template <typename T, typename C, typename A>
 int sayram_batch_s::step_once(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, const sg::Kry<T>& kr) {
   using namespace sg;
   const int gs = grid_stream(), gt = grid_tiles();
+  int prc = prep_spmv<T>();
+  if (prc) return prc;
   SG_CUDA(cudaMemsetAsync(d_ctl, 0, 2 * sizeof(int), stream));
   launch("begin", [&] { k_begin<<<(n + 255) / 256, 256, 0, stream>>>(cm); });
   launch("assemble", [&] { k_assemble<C, A><<<gt, kAsmThreads, 0, stream>>>(cm, geo, fl, cfull); });
@@ -514,8 +532,8 @@ int sayram_batch_s::step_once(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, c
     if (rc) return rc;
     if (h_ctl->n_outer == 0) break;
     for (int it = 0; it < opt.max_iters; ++it) {
-      launch("bicg1", [&] { k_bicg1<T><<<gs, kThreads, 0, stream>>>(cm, ck, kr); });
-      launch("bicg2", [&] { k_bicg2<T><<<gs, kThreads, 0, stream>>>(cm, ck, kr); });
+      launch("bicg1", [&] { k_bicg1<T><<<gs, kThreads, smem_spmv<T>(), stream>>>(cm, ck, kr); });
+      launch("bicg2", [&] { k_bicg2<T><<<gs, kThreads, smem_spmv<T>(), stream>>>(cm, ck, kr); });
       launch("bicg3", [&] { k_bicg3<T><<<gs, kThreads, 0, stream>>>(cm, kr, opt.max_iters); });
       SG_CUDA(cudaGetLastError());
       if (it < 4 || (it & 3) == 3) {
@@ -546,6 +564,8 @@ template <typename T, typename C, typename A>
 int sayram_batch_s::build_graph(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, const sg::Kry<T>& kr) {
   using namespace sg;
   const int gs = grid_stream(), gt = grid_tiles();
+  int prc = prep_spmv<T>();
+  if (prc) return prc;
   const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
   cudaGraph_t g = nullptr;
   SG_CUDA(cudaGraphCreate(&g, 0));
@@ -592,8 +612,8 @@ int sayram_batch_s::build_graph(const sg::Coef<C>& cfull, const sg::Coef<T>& ck,
   SG_CUDA(cudaGraphAddNode(&inner, obody, &rnode, nullptr, 1, &ip));
   cudaGraph_t ibody = ip.conditional.phGraph_out[0];
   SG_CUDA(cudaStreamBeginCaptureToGraph(stream, ibody, nullptr, nullptr, 0, mode));
-  k_bicg1<T><<<gs, kThreads, 0, stream>>>(c2, ck, kr);
-  k_bicg2<T><<<gs, kThreads, 0, stream>>>(c2, ck, kr);
+  k_bicg1<T><<<gs, kThreads, smem_spmv<T>(), stream>>>(c2, ck, kr);
+  k_bicg2<T><<<gs, kThreads, smem_spmv<T>(), stream>>>(c2, ck, kr);
   k_bicg3<T><<<gs, kThreads, 0, stream>>>(c2, kr, opt.max_iters);
   SG_CUDA(cudaStreamEndCapture(stream, &ibody));
   // suffix
@@ -1222,6 +1242,7 @@ int sayram_server_create(const sayram_server_config* cfg, const sayram_options* 
     return fail(rc, m);
   }
   e.n = c.max_slots;
+  e.pmax = (int)round_up(c.max_side, 4);
   if ((rc = e.rebuild_lists())) {
     std::string m = g_err;
     delete s;
@@ -1517,6 +1538,9 @@ extern "C" int sayram_step_noalloc(const sayram_problem* pd, const sayram_option
   const int gt = std::max(1, std::min(cm.ntiles, nsm * 8));
   const int gs = std::max(1, std::min(cm.nchunks, nsm * 16));
   k_field_in<F64A><<<gt, 256, 0, stream>>>(cm, fl.f, f_in);
+  const size_t smem_na = (size_t)(kChunk + 2 * pitch) * sizeof(double);
+  SG_CUDA(cudaFuncSetAttribute(k_bicg1<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_na));
+  SG_CUDA(cudaFuncSetAttribute(k_bicg2<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_na));
   SG_CUDA(cudaGetLastError());
   Ctl hctl;
   for (int s = 0; s < nsteps; ++s) {
@@ -1531,8 +1555,8 @@ extern "C" int sayram_step_noalloc(const sayram_problem* pd, const sayram_option
       SG_CUDA(cudaStreamSynchronize(stream));
       if (hctl.n_outer == 0) break;
       for (int it = 0; it < o.max_iters; ++it) {
-        k_bicg1<double><<<gs, kThreads, 0, stream>>>(cm, co, kr);
-        k_bicg2<double><<<gs, kThreads, 0, stream>>>(cm, co, kr);
+        k_bicg1<double><<<gs, kThreads, smem_na, stream>>>(cm, co, kr);
+        k_bicg2<double><<<gs, kThreads, smem_na, stream>>>(cm, co, kr);
         k_bicg3<double><<<gs, kThreads, 0, stream>>>(cm, kr, o.max_iters);
         SG_CUDA(cudaGetLastError());
         if (it < 4 || (it & 3) == 3) {

@@ -26,8 +26,9 @@
 
 namespace sg {
 
-constexpr int kChunk = 1024;   // cells per chunk of the streaming kernels
-constexpr int kThreads = 256;  // threads per block of the streaming kernels (4 cells each)
+constexpr int kChunk = 2048;   // cells per chunk of the streaming kernels
+constexpr int kThreads = 256;  // threads per block of the streaming kernels
+constexpr int kGroups = kChunk / (4 * kThreads);  // 4-cell groups per thread and chunk
 constexpr int kTX = 32;        // assembly tile width (alpha0, contiguous)
 constexpr int kTY = 16;        // assembly tile height (log E)
 constexpr int kAsmThreads = 256;

@@ -41,6 +41,7 @@ struct Common {
   // when set, [nchunks, ntiles, ninst] are read from device memory (lists that change between
   // steps, as in the server) instead of the by-value counts above
   const int* dyn;
+  int pmax;  // largest row pitch of any instance (shared-memory halo of the SpMV kernels)
   // device-side loops of the per-step CUDA graph (use_cond = 0: the host drives the loops)
   unsigned long long h_outer, h_inner;  // cudaGraphConditionalHandle of the two WHILE nodes
   int use_cond;
@@ -544,18 +545,47 @@ __global__ void __launch_bounds__(kAsmThreads) k_assemble(Common cm, Geo geo, Fi
 }
 
 // ------------------------------------------------------------------------------ streaming helpers
-// Locates chunk c: instance b and the first cell index K0 of this thread's 4-cell group.
+// Locates 4-cell group g (0..kGroups-1) of this thread in chunk c of instance I.
 struct Slot {
-  int b;
   long long K;
   bool valid;
 };
-__device__ __forceinline__ Slot slot_of(const Common& cm, int c, const InstDev& I) {
+__device__ __forceinline__ long long chunk_start(int c, const InstDev& I) {
+  return I.base + (long long)(c - I.chunk0) * kChunk;
+}
+__device__ __forceinline__ long long inst_end(const InstDev& I) { return I.base + (long long)I.ny * I.pitch; }
+__device__ __forceinline__ Slot slot_of(int c, const InstDev& I, int g) {
   Slot s;
-  s.b = cm.chunk_inst[c];
-  s.K = I.base + (long long)(c - I.chunk0) * kChunk + 4 * threadIdx.x;
-  s.valid = s.K < I.base + (long long)I.ny * I.pitch;
+  s.K = chunk_start(c, I) + 4 * (threadIdx.x + g * kThreads);
+  s.valid = s.K < inst_end(I);
   return s;
+}
+
+// Fills smem[0 .. n) with a 4-aligned stretch [e0, e0 + n) of a vector computed cell-wise by
+// f(k) -> Q4<T> (k a multiple of 4): the chunk plus one row above and below, so that the stencil
+// of every cell in the chunk reads shared memory only.
+template <typename T, typename F>
+__device__ __forceinline__ void stage_rows(T* sm, long long e0, long long n, F&& f) {
+  for (long long q = 4LL * threadIdx.x; q < n; q += 4LL * blockDim.x) {
+    const Q4<T> v = f(e0 + q);
+    *reinterpret_cast<Q4<T>*>(sm + q) = v;
+  }
+}
+
+// A~ x over a 4-cell group from a staged vector (sm holds x at global index e0 + offset)
+template <typename T>
+__device__ __forceinline__ Q4<T> stencil_sm(const T* sm, long long o, int P, const Q4<T>& cw,
+                                            const Q4<T>& ce, const Q4<T>& cs, const Q4<T>& cn) {
+  const Q4<T> c = *reinterpret_cast<const Q4<T>*>(sm + o);
+  const Q4<T> d = *reinterpret_cast<const Q4<T>*>(sm + o - P);
+  const Q4<T> u = *reinterpret_cast<const Q4<T>*>(sm + o + P);
+  const T w0 = sm[o - 1], e3 = sm[o + 4];
+  Q4<T> r;
+  const T wv[4] = {w0, c.a[0], c.a[1], c.a[2]};
+  const T ev[4] = {c.a[1], c.a[2], c.a[3], e3};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) r.a[k] = c.a[k] - (cw.a[k] * wv[k] + ce.a[k] * ev[k] + cs.a[k] * d.a[k] + cn.a[k] * u.a[k]);
+  return r;
 }
 
 // Coefficients of a row in the wide arithmetic: from the FP64 arrays or the (hi, lo) split
@@ -632,13 +662,15 @@ __global__ void __launch_bounds__(kThreads) k_resid(Common cm, Fields fl, Coef<C
     InstState& st = cm.st[b];
     if (!st.outer_active) continue;
     const InstDev I = cm.inst[b];
-    const Slot s = slot_of(cm, c, I);
     const double* yin = fl.y64[st.ycur];
     double* yout = fl.y64[st.ycur ^ 1];
     const bool hx = st.has_x != 0;
     const float sc = rhs_scale(st.rmax_bits);  // r is handed over as r * sc
     const float isc = 1.0f / sc;                // exact: sc is a power of two
     typename A::Acc q0 = 0, q1 = 0;
+#pragma unroll 1
+    for (int g = 0; g < kGroups; ++g) {
+    const Slot s = slot_of(c, I, g);
     if (s.valid) {
       const long long K = s.K, P = I.pitch;
       auto Y4 = [&](long long k) {
@@ -669,6 +701,7 @@ __global__ void __launch_bounds__(kThreads) k_resid(Common cm, Fields fl, Coef<C
       }
       A::st4(yout + K, yc);
       st4(kr.r + K, r);
+    }
     }
     const double w[2] = {A::warp_total(q0), A::warp_total(q1)};
     double tot[2], mine[2];
@@ -707,51 +740,60 @@ __global__ void __launch_bounds__(kThreads) k_resid(Common cm, Fields fl, Coef<C
 
 // ------------------------------------------------------------------------------ BiCGSTAB
 // k1: p = r + beta (p_old - omega v_old)  (p = r on a restart, which also sets r^ = r);
-//     v = A~ p;  partial (r^, v).
+//     v = A~ p;  partial (r^, v). p is computed once per cell into shared memory (chunk plus one
+//     row above and below) and the stencil reads it there.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_bicg1(Common cm, Coef<T> co, Kry<T> kr) {
   count_launch(cm.ctl);
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* sm = reinterpret_cast<T*>(smraw);
   for (int c = blockIdx.x, nc_ = n_chunks(cm); c < nc_; c += gridDim.x) {
     const int b = cm.chunk_inst[c];
     InstState& st = cm.st[b];
     if (!st.inner_active) continue;
     const InstDev I = cm.inst[b];
-    const Slot s = slot_of(cm, c, I);
     const int pc = st.pcur;
     const bool rs = st.restart != 0;
     const T beta = (T)st.beta, omega = (T)st.omega;
-    const T* po = kr.p[pc];
-    const T* vo = kr.v[pc];
-    T* pn = kr.p[pc ^ 1];
-    T* vn = kr.v[pc ^ 1];
-    T q[1] = {(T)0};
-    if (s.valid) {
-      const long long K = s.K, P = I.pitch;
-      auto P4 = [&](long long k) {
-        Q4<T> r = ld4(kr.r + k);
-        if (!rs) {
-          const Q4<T> a = ld4(po + k), v = ld4(vo + k);
+    const T* __restrict__ r = kr.r;
+    const T* __restrict__ po = kr.p[pc];
+    const T* __restrict__ vo = kr.v[pc];
+    T* __restrict__ pn = kr.p[pc ^ 1];
+    T* __restrict__ vn = kr.v[pc ^ 1];
+    const int P = I.pitch;
+    const long long c0 = chunk_start(c, I);
+    const long long c1 = min(c0 + (long long)kChunk, inst_end(I));
+    const long long e0 = c0 - P;
+    stage_rows<T>(sm, e0, (c1 - c0) + 2LL * P, [&](long long k) {
+      Q4<T> x = ld4(r + k);
+      if (!rs) {
+        const Q4<T> a = ld4(po + k), v = ld4(vo + k);
 #pragma unroll
-          for (int m = 0; m < 4; ++m) r.a[m] = r.a[m] + beta * (a.a[m] - omega * v.a[m]);
-        }
-        return r;
-      };
-      auto P1 = [&](long long k) { return rs ? kr.r[k] : kr.r[k] + beta * (po[k] - omega * vo[k]); };
-      const Q4<T> pcv = P4(K), pd = P4(K - P), pu = P4(K + P);
-      const T w0 = P1(K - 1), e3 = P1(K + 4);
-      const Q4<T> v = stencil<T, T>(pcv, w0, e3, pd, pu, ld4(co.cw + K), ld4(co.ce + K),
-                                    ld4(co.cs + K), ld4(co.cn + K));
-      st4(pn + K, pcv);
-      st4(vn + K, v);
-      Q4<T> rh;
-      if (rs) {
-        rh = ld4(kr.r + K);
-        st4(kr.rh + K, rh);
-      } else {
-        rh = ld4(kr.rh + K);
+        for (int m = 0; m < 4; ++m) x.a[m] = x.a[m] + beta * (a.a[m] - omega * v.a[m]);
       }
+      return x;
+    });
+    __syncthreads();
+    T q[1] = {(T)0};
 #pragma unroll
-      for (int m = 0; m < 4; ++m) q[0] += rh.a[m] * v.a[m];
+    for (int g = 0; g < kGroups; ++g) {
+      const long long K = c0 + 4 * (threadIdx.x + g * kThreads);
+      if (K < c1) {
+        const long long o = K - e0;
+        const Q4<T> pcv = *reinterpret_cast<const Q4<T>*>(sm + o);
+        const Q4<T> v = stencil_sm<T>(sm, o, P, ld4(co.cw + K), ld4(co.ce + K), ld4(co.cs + K), ld4(co.cn + K));
+        st4(pn + K, pcv);
+        st4(vn + K, v);
+        Q4<T> rh;
+        if (rs) {
+          rh = ld4(r + K);
+          st4(kr.rh + K, rh);
+        } else {
+          rh = ld4(kr.rh + K);
+        }
+#pragma unroll
+        for (int m = 0; m < 4; ++m) q[0] += rh.a[m] * v.a[m];
+      }
     }
     double tot[1], mine[1];
     block_sum<1, T>(q, mine);
@@ -772,38 +814,46 @@ __global__ void __launch_bounds__(kThreads) k_bicg1(Common cm, Coef<T> co, Kry<T
   }
 }
 
-// k2: s = r - alpha v;  t = A~ s;  partials (t, s), (t, t).
+// k2: s = r - alpha v;  t = A~ s;  partials (t, s), (t, t). s is staged like p in k1.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_bicg2(Common cm, Coef<T> co, Kry<T> kr) {
   count_launch(cm.ctl);
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* sm = reinterpret_cast<T*>(smraw);
   for (int c = blockIdx.x, nc_ = n_chunks(cm); c < nc_; c += gridDim.x) {
     const int b = cm.chunk_inst[c];
     InstState& st = cm.st[b];
     if (!st.inner_active) continue;
     const InstDev I = cm.inst[b];
-    const Slot s = slot_of(cm, c, I);
     const T alpha = (T)st.alpha;
-    const T* vv = kr.v[st.pcur];
+    const T* __restrict__ r = kr.r;
+    const T* __restrict__ vv = kr.v[st.pcur];
+    const int P = I.pitch;
+    const long long c0 = chunk_start(c, I);
+    const long long c1 = min(c0 + (long long)kChunk, inst_end(I));
+    const long long e0 = c0 - P;
+    stage_rows<T>(sm, e0, (c1 - c0) + 2LL * P, [&](long long k) {
+      Q4<T> x = ld4(r + k);
+      const Q4<T> v = ld4(vv + k);
+#pragma unroll
+      for (int m = 0; m < 4; ++m) x.a[m] -= alpha * v.a[m];
+      return x;
+    });
+    __syncthreads();
     T q[2] = {(T)0, (T)0};
-    if (s.valid) {
-      const long long K = s.K, P = I.pitch;
-      auto S4 = [&](long long k) {
-        Q4<T> r = ld4(kr.r + k);
-        const Q4<T> v = ld4(vv + k);
 #pragma unroll
-        for (int m = 0; m < 4; ++m) r.a[m] -= alpha * v.a[m];
-        return r;
-      };
-      auto S1 = [&](long long k) { return kr.r[k] - alpha * vv[k]; };
-      const Q4<T> sc = S4(K), sd = S4(K - P), su = S4(K + P);
-      const T w0 = S1(K - 1), e3 = S1(K + 4);
-      const Q4<T> t = stencil<T, T>(sc, w0, e3, sd, su, ld4(co.cw + K), ld4(co.ce + K),
-                                    ld4(co.cs + K), ld4(co.cn + K));
-      st4(kr.t + K, t);
+    for (int g = 0; g < kGroups; ++g) {
+      const long long K = c0 + 4 * (threadIdx.x + g * kThreads);
+      if (K < c1) {
+        const long long o = K - e0;
+        const Q4<T> sc = *reinterpret_cast<const Q4<T>*>(sm + o);
+        const Q4<T> t = stencil_sm<T>(sm, o, P, ld4(co.cw + K), ld4(co.ce + K), ld4(co.cs + K), ld4(co.cn + K));
+        st4(kr.t + K, t);
 #pragma unroll
-      for (int m = 0; m < 4; ++m) {
-        q[0] += t.a[m] * sc.a[m];
-        q[1] += t.a[m] * t.a[m];
+        for (int m = 0; m < 4; ++m) {
+          q[0] += t.a[m] * sc.a[m];
+          q[1] += t.a[m] * t.a[m];
+        }
       }
     }
     double tot[2], mine[2];
@@ -829,12 +879,14 @@ __global__ void __launch_bounds__(kThreads) k_bicg3(Common cm, Kry<T> kr, int ma
     InstState& st = cm.st[b];
     if (!st.inner_active) continue;
     const InstDev I = cm.inst[b];
-    const Slot s = slot_of(cm, c, I);
     const T alpha = (T)st.alpha, omega = (T)st.omega;
     const bool fresh = st.fresh != 0;
     const T* pp = kr.p[st.pcur];
     const T* vv = kr.v[st.pcur];
     T q[2] = {(T)0, (T)0};
+#pragma unroll
+    for (int g = 0; g < kGroups; ++g) {
+    const Slot s = slot_of(c, I, g);
     if (s.valid) {
       const long long K = s.K;
       const Q4<T> r = ld4(kr.r + K), v = ld4(vv + K), p = ld4(pp + K), t = ld4(kr.t + K);
@@ -851,6 +903,7 @@ __global__ void __launch_bounds__(kThreads) k_bicg3(Common cm, Kry<T> kr, int ma
       }
       st4(kr.x + K, x);
       st4(kr.r + K, rn);
+    }
     }
     double tot[2], mine[2];
     block_sum<2, T>(q, mine);
@@ -893,11 +946,13 @@ __global__ void __launch_bounds__(kThreads) k_polish(Common cm, Fields fl, Coef<
     InstState& st = cm.st[b];
     const InstDev I = cm.inst[b];
     if (!I.enabled) continue;
-    const Slot s = slot_of(cm, c, I);
     const double* y = fl.y64[st.ycur];
     V mass = A::k(0.0), rsum = A::k(0.0);
     float clamp = 0.0f;
     float mn = 3.0e38f;
+#pragma unroll 1
+    for (int g = 0; g < kGroups; ++g) {
+    const Slot s = slot_of(c, I, g);
     if (s.valid) {
       const long long K = s.K, P = I.pitch;
       auto Yp4 = [&](long long k) {
@@ -933,6 +988,7 @@ __global__ void __launch_bounds__(kThreads) k_polish(Common cm, Fields fl, Coef<
         }
       }
       A::st4(fl.f + K, fo);
+    }
     }
     // block minimum (separate from the sums)
 #pragma unroll
