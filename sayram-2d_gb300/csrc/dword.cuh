@@ -88,9 +88,14 @@ SG_HD dw dw_mul(dw x, dw y) {
   return fast2sum(c.hi, cl3);
 }
 
-// 1/y: FP32 reciprocal t, then r = t + t*(1 - y*t) with y*t formed in double-word
+// 1/y: approximate FP32 reciprocal t (a few ulps), then r = t + t*(1 - y*t) with y*t formed in
+// double-word; the Newton step squares the relative error of t.
 SG_HD dw dw_rcp(dw y) {
+#ifdef __CUDA_ARCH__
+  const float t = __fdividef(1.0f, y.hi);
+#else
   const float t = 1.0f / y.hi;
+#endif
   const dw p = dw_mul_f(y, t);               // y*t ~ 1
   const float e = (1.0f - p.hi) - p.lo;      // 1 - p.hi is exact (Sterbenz)
   return fast2sum(t, t * e);

@@ -185,6 +185,16 @@ struct sayram_batch_s {
     SG_CUDA(cudaFuncSetAttribute(sg::k_bicg2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
     return SAYRAM_OK;
   }
+  // the residual and polish kernels stage the 8-byte wide solution
+  size_t smem_wide() const { return (size_t)(sg::kChunk + 2 * pmax) * 8; }
+  template <typename T, typename C, typename A>
+  int prep_wide() {
+    const int bytes = (int)smem_wide();
+    if (bytes > 227 * 1024) return fail(SAYRAM_ERR_ARG, "rows too wide for the shared-memory stencil");
+    SG_CUDA(cudaFuncSetAttribute(sg::k_resid<T, C, A>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    SG_CUDA(cudaFuncSetAttribute(sg::k_polish<C, A>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    return SAYRAM_OK;
+  }
   int grid_tiles() const { return std::max(1, std::min(cap_tiles, nsm * 8)); }
 
   int build(const sayram_problem* probs, int count, const sayram_options* o);
@@ -518,13 +528,14 @@ int sayram_batch_s::step_once(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, c
   using namespace sg;
   const int gs = grid_stream(), gt = grid_tiles();
   int prc = prep_spmv<T>();
+  if (!prc) prc = prep_wide<T, C, A>();
   if (prc) return prc;
   SG_CUDA(cudaMemsetAsync(d_ctl, 0, 2 * sizeof(int), stream));
   launch("begin", [&] { k_begin<<<(n + 255) / 256, 256, 0, stream>>>(cm); });
   launch("assemble", [&] { k_assemble<C, A><<<gt, kAsmThreads, 0, stream>>>(cm, geo, fl, cfull); });
   for (int o = 0; o < opt.max_refine; ++o) {
     launch("resid", [&] {
-      k_resid<T, C, A><<<gs, kThreads, 0, stream>>>(cm, fl, cfull, kr, opt.tol, opt.inner_tol, opt.max_refine);
+      k_resid<T, C, A><<<gs, kThreads, smem_wide(), stream>>>(cm, fl, cfull, kr, opt.tol, opt.inner_tol, opt.max_refine);
     });
     SG_CUDA(cudaGetLastError());
     if (o == opt.max_refine - 1) break;
@@ -543,7 +554,7 @@ int sayram_batch_s::step_once(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, c
       }
     }
   }
-  launch("polish", [&] { k_polish<C, A><<<gs, kThreads, 0, stream>>>(cm, fl, cfull); });
+  launch("polish", [&] { k_polish<C, A><<<gs, kThreads, smem_wide(), stream>>>(cm, fl, cfull); });
   SG_CUDA(cudaGetLastError());
   return SAYRAM_OK;
 }
@@ -565,6 +576,7 @@ int sayram_batch_s::build_graph(const sg::Coef<C>& cfull, const sg::Coef<T>& ck,
   using namespace sg;
   const int gs = grid_stream(), gt = grid_tiles();
   int prc = prep_spmv<T>();
+  if (!prc) prc = prep_wide<T, C, A>();
   if (prc) return prc;
   const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
   cudaGraph_t g = nullptr;
@@ -599,7 +611,7 @@ int sayram_batch_s::build_graph(const sg::Coef<C>& cfull, const sg::Coef<T>& ck,
   c2.h_inner = hin;
   cudaGraphNode_t rnode;
   SG_CUDA(cudaStreamBeginCaptureToGraph(stream, obody, nullptr, nullptr, 0, mode));
-  k_resid<T, C, A><<<gs, kThreads, 0, stream>>>(c2, fl, cfull, kr, opt.tol, opt.inner_tol, opt.max_refine);
+  k_resid<T, C, A><<<gs, kThreads, smem_wide(), stream>>>(c2, fl, cfull, kr, opt.tol, opt.inner_tol, opt.max_refine);
   if ((rc = last_captured(&rnode))) { cudaStreamEndCapture(stream, &obody); return rc; }
   SG_CUDA(cudaStreamEndCapture(stream, &obody));
   // inner WHILE inside the outer body
@@ -618,7 +630,7 @@ int sayram_batch_s::build_graph(const sg::Coef<C>& cfull, const sg::Coef<T>& ck,
   SG_CUDA(cudaStreamEndCapture(stream, &ibody));
   // suffix
   SG_CUDA(cudaStreamBeginCaptureToGraph(stream, g, &outer, nullptr, 1, mode));
-  k_polish<C, A><<<gs, kThreads, 0, stream>>>(c2, fl, cfull);
+  k_polish<C, A><<<gs, kThreads, smem_wide(), stream>>>(c2, fl, cfull);
   SG_CUDA(cudaStreamEndCapture(stream, &g));
   SG_CUDA(cudaGraphInstantiate(&gexec, g, 0));
   return SAYRAM_OK;
@@ -1541,6 +1553,8 @@ extern "C" int sayram_step_noalloc(const sayram_problem* pd, const sayram_option
   const size_t smem_na = (size_t)(kChunk + 2 * pitch) * sizeof(double);
   SG_CUDA(cudaFuncSetAttribute(k_bicg1<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_na));
   SG_CUDA(cudaFuncSetAttribute(k_bicg2<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_na));
+  SG_CUDA(cudaFuncSetAttribute(k_resid<double, double, F64A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_na));
+  SG_CUDA(cudaFuncSetAttribute(k_polish<double, F64A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_na));
   SG_CUDA(cudaGetLastError());
   Ctl hctl;
   for (int s = 0; s < nsteps; ++s) {
@@ -1548,7 +1562,7 @@ extern "C" int sayram_step_noalloc(const sayram_problem* pd, const sayram_option
     k_begin<<<1, 32, 0, stream>>>(cm);
     k_assemble<double, F64A><<<gt, kAsmThreads, 0, stream>>>(cm, geo, fl, co);
     for (int r = 0; r < o.max_refine; ++r) {
-      k_resid<double, double, F64A><<<gs, kThreads, 0, stream>>>(cm, fl, co, kr, o.tol, o.inner_tol, o.max_refine);
+      k_resid<double, double, F64A><<<gs, kThreads, smem_na, stream>>>(cm, fl, co, kr, o.tol, o.inner_tol, o.max_refine);
       SG_CUDA(cudaGetLastError());
       if (r == o.max_refine - 1) break;
       SG_CUDA(cudaMemcpyAsync(&hctl, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, stream));
@@ -1566,7 +1580,7 @@ extern "C" int sayram_step_noalloc(const sayram_problem* pd, const sayram_option
         }
       }
     }
-    k_polish<double, F64A><<<gs, kThreads, 0, stream>>>(cm, fl, co);
+    k_polish<double, F64A><<<gs, kThreads, smem_na, stream>>>(cm, fl, co);
     SG_CUDA(cudaGetLastError());
   }
   k_field_out<F64A><<<gt, 256, 0, stream>>>(cm, f_out, fl.f);

@@ -653,10 +653,12 @@ __device__ __forceinline__ Q4<typename A::V> stencilW(const Q4<typename A::V>& c
 // r = R - A~ (y + x) in the wide arithmetic; writes y + x to the other y buffer and r (T precision).
 // Partials: ||r||^2, ||R||^2.
 template <typename T, typename C, typename A>
-__global__ void __launch_bounds__(kThreads) k_resid(Common cm, Fields fl, Coef<C> co, Kry<T> kr,
-                                                     double tol, double inner_tol, int max_refine) {
+__global__ void __launch_bounds__(kThreads, 3) k_resid(Common cm, Fields fl, Coef<C> co, Kry<T> kr,
+                                                        double tol, double inner_tol, int max_refine) {
   using V = typename A::V;
   count_launch(cm.ctl);
+  extern __shared__ __align__(16) unsigned char smraw[];
+  V* sm = reinterpret_cast<V*>(smraw);
   for (int c = blockIdx.x, nc_ = n_chunks(cm); c < nc_; c += gridDim.x) {
     const int b = cm.chunk_inst[c];
     InstState& st = cm.st[b];
@@ -667,41 +669,46 @@ __global__ void __launch_bounds__(kThreads) k_resid(Common cm, Fields fl, Coef<C
     const bool hx = st.has_x != 0;
     const float sc = rhs_scale(st.rmax_bits);  // r is handed over as r * sc
     const float isc = 1.0f / sc;                // exact: sc is a power of two
+    const int P = I.pitch;
+    const long long c0 = chunk_start(c, I);
+    const long long c1 = min(c0 + (long long)kChunk, inst_end(I));
+    const long long e0 = c0 - P;
+    // y + x (the last Krylov correction, in scaled units) over the chunk and one row each side
+    stage_rows<V>(sm, e0, (c1 - c0) + 2LL * P, [&](long long k) {
+      Q4<V> y = A::ld4(yin + k);
+      if (hx) {
+        const Q4<T> x = ld4(kr.x + k);
+#pragma unroll
+        for (int m = 0; m < 4; ++m) y.a[m] = A::template add_scaled<T>(y.a[m], x.a[m], isc);
+      }
+      return y;
+    });
+    __syncthreads();
     typename A::Acc q0 = 0, q1 = 0;
 #pragma unroll 1
     for (int g = 0; g < kGroups; ++g) {
-    const Slot s = slot_of(c, I, g);
-    if (s.valid) {
-      const long long K = s.K, P = I.pitch;
-      auto Y4 = [&](long long k) {
-        Q4<V> y = A::ld4(yin + k);
-        if (hx) {
-          const Q4<T> x = ld4(kr.x + k);
+      const long long K = c0 + 4 * (threadIdx.x + g * kThreads);
+      if (K < c1) {
+        const long long o = K - e0;
+        const Q4<V> cw = CoefW<C, A>::row(co, 0, K), ce = CoefW<C, A>::row(co, 1, K);
+        const Q4<V> cs = CoefW<C, A>::row(co, 2, K), cn = CoefW<C, A>::row(co, 3, K);
+        const Q4<V> R = A::ld4(fl.R + K);
+        Q4<T> r;
+        Q4<V> yc;
 #pragma unroll
-          for (int m = 0; m < 4; ++m) y.a[m] = A::template add_scaled<T>(y.a[m], x.a[m], isc);
+        for (int m = 0; m < 4; ++m) {
+          const V yv = sm[o + m];
+          const V s1 = A::fma(cn.a[m], sm[o + m + P], A::fma(cs.a[m], sm[o + m - P],
+                              A::fma(ce.a[m], sm[o + m + 1], A::mul(cw.a[m], sm[o + m - 1]))));
+          const V rv = A::sub(R.a[m], A::sub(yv, s1));
+          yc.a[m] = yv;
+          r.a[m] = A::template scaled<T>(rv, sc);
+          q0 += A::sq_scaled(rv, sc);
+          q1 += A::sq_scaled(R.a[m], sc);
         }
-        return y;
-      };
-      auto Y1 = [&](long long k) {
-        return hx ? A::template add_scaled<T>(A::ld(yin, k), kr.x[k], isc) : A::ld(yin, k);
-      };
-      const Q4<V> yc = Y4(K), yd = Y4(K - P), yu = Y4(K + P);
-      const V w0 = Y1(K - 1), e3 = Y1(K + 4);
-      const Q4<V> cw = CoefW<C, A>::row(co, 0, K), ce = CoefW<C, A>::row(co, 1, K);
-      const Q4<V> cs = CoefW<C, A>::row(co, 2, K), cn = CoefW<C, A>::row(co, 3, K);
-      const Q4<V> Ay = stencilW<A>(yc, w0, e3, yd, yu, cw, ce, cs, cn);
-      const Q4<V> R = A::ld4(fl.R + K);
-      Q4<T> r;
-#pragma unroll
-      for (int m = 0; m < 4; ++m) {
-        const V rv = A::sub(R.a[m], Ay.a[m]);
-        r.a[m] = A::template scaled<T>(rv, sc);
-        q0 += A::sq_scaled(rv, sc);
-        q1 += A::sq_scaled(R.a[m], sc);
+        A::st4(yout + K, yc);
+        st4(kr.r + K, r);
       }
-      A::st4(yout + K, yc);
-      st4(kr.r + K, r);
-    }
     }
     const double w[2] = {A::warp_total(q0), A::warp_total(q1)};
     double tot[2], mine[2];
@@ -937,9 +944,11 @@ __global__ void __launch_bounds__(kThreads) k_bicg3(Common cm, Kry<T> kr, int ma
 // y' = R + (I - A~) max(y, 0) >= 0 (R >= 0, fractions >= 0), f = y' / D; partials: sum colsum*f,
 // sum R, clamped count; the chunk minimum of f travels in part slot 3.
 template <typename C, typename A>
-__global__ void __launch_bounds__(kThreads) k_polish(Common cm, Fields fl, Coef<C> co) {
+__global__ void __launch_bounds__(kThreads, 3) k_polish(Common cm, Fields fl, Coef<C> co) {
   using V = typename A::V;
   count_launch(cm.ctl);
+  extern __shared__ __align__(16) unsigned char smraw[];
+  V* sm = reinterpret_cast<V*>(smraw);
   __shared__ float smin[kThreads / 32];
   for (int c = blockIdx.x, nc_ = n_chunks(cm); c < nc_; c += gridDim.x) {
     const int b = cm.chunk_inst[c];
@@ -947,48 +956,45 @@ __global__ void __launch_bounds__(kThreads) k_polish(Common cm, Fields fl, Coef<
     const InstDev I = cm.inst[b];
     if (!I.enabled) continue;
     const double* y = fl.y64[st.ycur];
+    const int P = I.pitch;
+    const long long c0 = chunk_start(c, I);
+    const long long c1 = min(c0 + (long long)kChunk, inst_end(I));
+    const long long e0 = c0 - P;
+    stage_rows<V>(sm, e0, (c1 - c0) + 2LL * P, [&](long long k) {
+      Q4<V> v = A::ld4(y + k);
+#pragma unroll
+      for (int m = 0; m < 4; ++m) v.a[m] = A::max0(v.a[m]);
+      return v;
+    });
+    __syncthreads();
     V mass = A::k(0.0), rsum = A::k(0.0);
     float clamp = 0.0f;
     float mn = 3.0e38f;
 #pragma unroll 1
     for (int g = 0; g < kGroups; ++g) {
-    const Slot s = slot_of(c, I, g);
-    if (s.valid) {
-      const long long K = s.K, P = I.pitch;
-      auto Yp4 = [&](long long k) {
-        Q4<V> v = A::ld4(y + k);
+      const long long K = c0 + 4 * (threadIdx.x + g * kThreads);
+      if (K < c1) {
+        const long long o = K - e0;
+        const Q4<V> cw = CoefW<C, A>::row(co, 0, K), ce = CoefW<C, A>::row(co, 1, K);
+        const Q4<V> cs = CoefW<C, A>::row(co, 2, K), cn = CoefW<C, A>::row(co, 3, K);
+        const Q4<V> R = A::ld4(fl.R + K), inv = A::ld4(fl.invD + K), cols = A::ld4(fl.colsum + K);
+        const int row_i0 = (int)((K - I.base) % I.pitch);
+        Q4<V> fo;
 #pragma unroll
-        for (int m = 0; m < 4; ++m) v.a[m] = A::max0(v.a[m]);
-        return v;
-      };
-      const Q4<V> yc = A::ld4(y + K);
-      Q4<V> ycp;
-#pragma unroll
-      for (int m = 0; m < 4; ++m) ycp.a[m] = A::max0(yc.a[m]);
-      const Q4<V> yd = Yp4(K - P), yu = Yp4(K + P);
-      const V w0 = A::max0(A::ld(y, K - 1)), e3 = A::max0(A::ld(y, K + 4));
-      const Q4<V> cw = CoefW<C, A>::row(co, 0, K), ce = CoefW<C, A>::row(co, 1, K);
-      const Q4<V> cs = CoefW<C, A>::row(co, 2, K), cn = CoefW<C, A>::row(co, 3, K);
-      const Q4<V> R = A::ld4(fl.R + K), inv = A::ld4(fl.invD + K), cols = A::ld4(fl.colsum + K);
-      const V wv[4] = {w0, ycp.a[0], ycp.a[1], ycp.a[2]};
-      const V ev[4] = {ycp.a[1], ycp.a[2], ycp.a[3], e3};
-      Q4<V> fo;
-      const int row_i0 = (int)((K - I.base) % I.pitch);
-#pragma unroll
-      for (int m = 0; m < 4; ++m) {
-        const V yp = A::add(R.a[m], A::fma(cn.a[m], yu.a[m], A::fma(cs.a[m], yd.a[m],
-                                           A::fma(ce.a[m], ev[m], A::mul(cw.a[m], wv[m])))));
-        const V fv = A::mul(yp, inv.a[m]);
-        fo.a[m] = fv;
-        mass = A::fma(cols.a[m], fv, mass);
-        rsum = A::add(rsum, R.a[m]);
-        if (row_i0 + m < I.nx) {
-          clamp += A::lt0(yc.a[m]) ? 1.0f : 0.0f;
-          mn = fminf(mn, A::f32(fv));
+        for (int m = 0; m < 4; ++m) {
+          const V yp = A::add(R.a[m], A::fma(cn.a[m], sm[o + m + P], A::fma(cs.a[m], sm[o + m - P],
+                                           A::fma(ce.a[m], sm[o + m + 1], A::mul(cw.a[m], sm[o + m - 1])))));
+          const V fv = A::mul(yp, inv.a[m]);
+          fo.a[m] = fv;
+          mass = A::fma(cols.a[m], fv, mass);
+          rsum = A::add(rsum, R.a[m]);
+          if (row_i0 + m < I.nx) {
+            clamp += A::lt0(A::ld(y, K + m)) ? 1.0f : 0.0f;
+            mn = fminf(mn, A::f32(fv));
+          }
         }
+        A::st4(fl.f + K, fo);
       }
-      A::st4(fl.f + K, fo);
-    }
     }
     // block minimum (separate from the sums)
 #pragma unroll
