@@ -233,7 +233,7 @@ void sayram_server_destroy(sayram_server s);
  * default stream); the call returns once that stream has finished the work. opt may be NULL and
  * must select SAYRAM_FP64. stats (may be NULL) receives this call's statistics.
  *
- * Working memory is one fixed device array of 16,384,000 bytes defined in this library; every
+ * Working memory is one fixed device array of 16,973,824 bytes defined in this library; every
  * GPU that loads the library holds it until the process exits. A grid fits when
  * round_up((ny+2) * round_up(nx,4), 32) + 64 <= 73728 cells and nx, ny <= 4096 (256 x 256
  * fits); larger grids return SAYRAM_ERR_ARG with a message saying so.

@@ -311,7 +311,7 @@ int sayram_batch_s::alloc_storage(long long cells, int slots, int chunks_cap, in
     SG_ALLOC(*g, cells);
     cell_arrays.push_back({*g, 8});
   }
-  double** fs[6] = {&fl.f, &fl.invD, &fl.R, &fl.colsum, &fl.y64[0], &fl.y64[1]};
+  double** fs[7] = {&fl.f, &fl.fprev, &fl.invD, &fl.R, &fl.colsum, &fl.y64[0], &fl.y64[1]};
   for (auto f : fs) {
     SG_ALLOC(*f, cells);
     cell_arrays.push_back({*f, 8});
@@ -751,6 +751,8 @@ int sayram_batch_step_host(sayram_batch b, int nsteps, const double* f_in, doubl
   SG_CUDA(cudaSetDevice(b->dev));
   if (f_in) {
     SG_CUDA(cudaMemcpyAsync(b->d_stage, f_in, sizeof(double) * b->nreal, cudaMemcpyHostToDevice, b->stream));
+    for (int k = 0; k < b->n; ++k)  // a replaced state has no previous step to extrapolate from
+      SG_CUDA(cudaMemsetAsync((char*)(b->d_st + k) + offsetof(InstState, has_prev), 0, sizeof(int), b->stream));
     b->launch("field_in", [&] {
       if (b->dwm)
         sg::k_field_in<sg::DWA><<<b->grid_tiles(), 256, 0, b->stream>>>(b->cm, b->fl.f, b->d_stage);
@@ -795,6 +797,7 @@ int sayram_batch_set_f(sayram_batch b, int idx, const double* f) {
   for (int i = 0; i < I.nx; ++i)
     for (int j = 0; j < I.ny; ++j) rows[(size_t)j * I.pitch + i] = b->wide(f[(size_t)i * I.ny + j]);
   SG_CUDA(cudaMemcpyAsync(b->fl.f + I.base, rows.data(), sizeof(double) * rows.size(), cudaMemcpyHostToDevice, b->stream));
+  SG_CUDA(cudaMemsetAsync((char*)(b->d_st + idx) + offsetof(InstState, has_prev), 0, sizeof(int), b->stream));
   SG_CUDA(cudaStreamSynchronize(b->stream));
   return SAYRAM_OK;
 }
@@ -959,7 +962,7 @@ void sayram_batch_destroy(sayram_batch b) { delete b; }
 size_t sayram_instance_bytes(int nx, int ny, int precision) {
   const long long pitch = round_up(nx, 4);
   const long long cells = round_up((long long)(ny + 2) * pitch, 32);
-  const long long per = 14 * 8 + (precision != SAYRAM_FP64 ? 8 * 4 + 8 * 4 : 4 * 8 + 8 * 8) + 8;
+  const long long per = 15 * 8 + (precision != SAYRAM_FP64 ? 8 * 4 + 8 * 4 : 4 * 8 + 8 * 8) + 8;
   return (size_t)(cells * per + 4096);
 }
 
@@ -1331,7 +1334,7 @@ constexpr int kNoAllocMaxSide = 4096;       // nx, ny limit (host tables are on 
 constexpr int kNoAllocMaxChunks = (int)(kNoAllocCells / sg::kChunk) + 2;
 constexpr int kNoAllocMaxTiles = 8192;
 constexpr size_t kNoAllocTableBytes = 1u << 20;
-constexpr size_t kNoAllocBytes = kNoAllocTableBytes + (size_t)kNoAllocCells * 26 * sizeof(double);
+constexpr size_t kNoAllocBytes = kNoAllocTableBytes + (size_t)kNoAllocCells * 27 * sizeof(double);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
@@ -1486,8 +1489,8 @@ extern "C" int sayram_step_noalloc(const sayram_problem* pd, const sayram_option
   Fields fl{};
   Coef<double> co{};
   Kry<double> kr{};
-  double** cellarrs[26] = {&geo.aAx, &geo.aBx, &geo.Sx, &geo.aAy, &geo.aBy, &geo.Sy, &geo.ukk, &geo.sdiag,
-                           &fl.f, &fl.invD, &fl.R, &fl.colsum, &fl.y64[0], &fl.y64[1],
+  double** cellarrs[27] = {&geo.aAx, &geo.aBx, &geo.Sx, &geo.aAy, &geo.aBy, &geo.Sy, &geo.ukk, &geo.sdiag,
+                           &fl.f, &fl.fprev, &fl.invD, &fl.R, &fl.colsum, &fl.y64[0], &fl.y64[1],
                            &co.cw, &co.ce, &co.cs, &co.cn,
                            &kr.r, &kr.rh, &kr.t, &kr.x, &kr.p[0], &kr.p[1], &kr.v[0], &kr.v[1]};
   for (auto a : cellarrs) {

@@ -26,7 +26,7 @@
 
 namespace sg {
 
-constexpr int kChunk = 2048;   // cells per chunk of the streaming kernels
+constexpr int kChunk = 4096;   // cells per chunk of the streaming kernels
 constexpr int kThreads = 256;  // threads per block of the streaming kernels
 constexpr int kGroups = kChunk / (4 * kThreads);  // 4-cell groups per thread and chunk
 constexpr int kTX = 32;        // assembly tile width (alpha0, contiguous)
@@ -62,6 +62,7 @@ struct InstState {
   int ycur, pcur, outer_active, inner_active;
   int restart, fresh, has_x, iters;
   int iters_total, refines, status;
+  int has_prev;            // fprev holds the state of the previous step (extrapolated start)
   unsigned int rmax_bits;  // bits of max |R| over the instance (non-negative float; atomicMax order)
   unsigned int cnt[PH_COUNT];
 };

@@ -88,6 +88,7 @@ struct Coef {  // row-oriented scaled off-diagonal magnitudes (hi parts when spl
 
 struct Fields {
   double* f;       // state, padded system order
+  double* fprev;   // state of the previous step
   double* invD;    // 1 / diag(M)
   double* R;       // right-hand side
   double* colsum;  // 1^T M per column (conservation check)
@@ -401,6 +402,7 @@ __global__ void __launch_bounds__(kAsmThreads) k_assemble(Common cm, Geo geo, Fi
     const int i0 = (lt % I.ntx) * kTX, j0 = (lt / I.ntx) * kTY;
     const int nx = I.nx, ny = I.ny, P = I.pitch;
     const long long base = I.base;
+    const bool has_prev = cm.st[b].has_prev != 0;
     // 1) f and 1/(f+eps) on the tile plus a one-cell halo
     for (int q = threadIdx.x; q < HX * HY; q += blockDim.x) {
       const int hx = q % HX, hy = q / HX;
@@ -531,7 +533,10 @@ __global__ void __launch_bounds__(kAsmThreads) k_assemble(Common cm, Geo geo, Fi
       A::st(fl.invD, K, inv);
       A::st(fl.R, K, Rv);
       A::st(fl.colsum, K, A::add(sd, dir));
-      A::st(fl.y64[cm.st[b].ycur], K, A::mul(D, fK));
+      // start the solve from the linear extrapolation 2 f^n - f^(n-1) (only the starting point of
+      // the iteration; the converged answer does not depend on it)
+      const V g0 = has_prev ? A::sub(A::add(fK, fK), A::ld(fl.fprev, K)) : fK;
+      A::st(fl.y64[cm.st[b].ycur], K, A::mul(D, g0));
       if (wIn) AsmOut<C, A>::put(co, 1, K - 1, A::mul(Aw, inv));  // row K-1, east entry
       if (eIn) AsmOut<C, A>::put(co, 0, K + 1, A::mul(Ae, inv));  // row K+1, west entry
       if (sIn) AsmOut<C, A>::put(co, 3, K - P, A::mul(As, inv));  // row K-P, north entry
@@ -566,6 +571,7 @@ __device__ __forceinline__ Slot slot_of(int c, const InstDev& I, int g) {
 // of every cell in the chunk reads shared memory only.
 template <typename T, typename F>
 __device__ __forceinline__ void stage_rows(T* sm, long long e0, long long n, F&& f) {
+#pragma unroll 2
   for (long long q = 4LL * threadIdx.x; q < n; q += 4LL * blockDim.x) {
     const Q4<T> v = f(e0 + q);
     *reinterpret_cast<Q4<T>*>(sm + q) = v;
@@ -782,7 +788,7 @@ __global__ void __launch_bounds__(kThreads) k_bicg1(Common cm, Coef<T> co, Kry<T
     });
     __syncthreads();
     T q[1] = {(T)0};
-#pragma unroll
+#pragma unroll 2
     for (int g = 0; g < kGroups; ++g) {
       const long long K = c0 + 4 * (threadIdx.x + g * kThreads);
       if (K < c1) {
@@ -848,7 +854,7 @@ __global__ void __launch_bounds__(kThreads) k_bicg2(Common cm, Coef<T> co, Kry<T
     });
     __syncthreads();
     T q[2] = {(T)0, (T)0};
-#pragma unroll
+#pragma unroll 2
     for (int g = 0; g < kGroups; ++g) {
       const long long K = c0 + 4 * (threadIdx.x + g * kThreads);
       if (K < c1) {
@@ -891,7 +897,7 @@ __global__ void __launch_bounds__(kThreads) k_bicg3(Common cm, Kry<T> kr, int ma
     const T* pp = kr.p[st.pcur];
     const T* vv = kr.v[st.pcur];
     T q[2] = {(T)0, (T)0};
-#pragma unroll
+#pragma unroll 2
     for (int g = 0; g < kGroups; ++g) {
     const Slot s = slot_of(c, I, g);
     if (s.valid) {
@@ -993,6 +999,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_polish(Common cm, Fields fl, Co
             mn = fminf(mn, A::f32(fv));
           }
         }
+        A::st4(fl.fprev + K, A::ld4(fl.f + K));
         A::st4(fl.f + K, fo);
       }
     }
@@ -1020,6 +1027,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_polish(Common cm, Fields fl, Co
       st.clamped = (long long)tot[2];
       st.mass_drift = tot[1] != 0.0 ? fabs(tot[0] - tot[1]) / fabs(tot[1]) : 0.0;
       st.steps += 1;
+      st.has_prev = 1;
       if (!(gmin >= 0.0)) st.status = ST_NEGATIVE;
     }
     __syncthreads();

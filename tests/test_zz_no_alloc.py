@@ -4,9 +4,10 @@ program whose own memory manager owns the GPU, or one that must not allocate onc
 It is checked through the C-ABI against the ordinary entry point (sayram_create + sayram_step,
 which allocates its own buffers) on the same problem, FP64, for two calls in a row: the second
 call continues from the first call's output. Device buffers for the inputs and outputs are the
-caller's, here made with torch. Both paths run the same kernels in FP64, so they must agree to
-1e-12 in relative L2. This file is collected last so that a run stopping at the first failure
-has already run every other test."""
+caller's, here made with torch. Both paths run the same FP64 kernels; the allocating path starts
+the second call's solves from a time extrapolation it keeps between calls, so the two agree to
+the FP64 parity tolerance of the other tests, 1e-10 in relative L2. This file is collected last
+so that a run stopping at the first failure has already run every other test."""
 import ctypes
 
 import numpy as np
@@ -68,8 +69,8 @@ def test_noalloc_matches_allocating_entry_point(capi):
     ref.step(3)
     ref2 = ref.f()
     ref.close()
-    assert rel(got1, ref1) <= 1e-12, rel(got1, ref1)
-    assert rel(got2, ref2) <= 1e-12, rel(got2, ref2)
+    assert rel(got1, ref1) <= 1e-10, rel(got1, ref1)
+    assert rel(got2, ref2) <= 1e-10, rel(got2, ref2)
     assert got2.min() >= 0.0
 
 
