@@ -112,6 +112,9 @@ struct F64A {
   __device__ static V sub(V a, V b) { return a - b; }
   __device__ static V mul(V a, V b) { return a * b; }
   __device__ static V fma(V a, V b, V c) { return a * b + c; }
+  // sums whose terms all have the same sign (cheaper in double-word form)
+  __device__ static V addp(V a, V b) { return a + b; }
+  __device__ static V fmap(V a, V b, V c) { return a * b + c; }
   __device__ static V addf(V a, float b) { return a + (double)b; }
   __device__ static V rcp(V a) { return 1.0 / a; }
   __device__ static V div(V a, V b) { return a / b; }
@@ -164,6 +167,8 @@ struct DWA {
   __device__ static V sub(V a, V b) { return dw_sub(a, b); }
   __device__ static V mul(V a, V b) { return dw_mul(a, b); }
   __device__ static V fma(V a, V b, V c) { return dw_add(dw_mul(a, b), c); }
+  __device__ static V addp(V a, V b) { return dw_add_same(a, b); }
+  __device__ static V fmap(V a, V b, V c) { return dw_add_same(dw_mul(a, b), c); }
   __device__ static V addf(V a, float b) { return dw_add_f(a, b); }
   __device__ static V rcp(V a) { return dw_rcp(a); }
   __device__ static V div(V a, V b) { return dw_div(a, b); }
@@ -363,21 +368,21 @@ __device__ __forceinline__ void inner_face(typename A::V aK, typename A::V SK, t
                                            typename A::V* AK, typename A::V* AL) {
   using V = typename A::V;
   const V absK = A::abs(aK), absL = A::abs(aL);
-  const V denom = A::add(A::add(absK, absL), A::k(2 * kEps));
-  const V muK = A::div(A::add(absL, A::k(kEps)), denom);
+  const V denom = A::addp(A::addp(absK, absL), A::k(2 * kEps));
+  const V muK = A::div(A::addp(absL, A::k(kEps)), denom);
   const V muL = A::sub(A::k(1.0), muK);
   const V B = A::sub(A::mul(muL, aL), A::mul(muK, aK));
   const V Bp = A::max0(B);             // (|B| + B) / 2
   const V Bm = A::max0(A::sub(A::k(0.0), B));  // (|B| - B) / 2
-  *AK = A::fma(Bp, invK, A::mul(muK, SK));
-  *AL = A::fma(Bm, invL, A::mul(muL, SL));
+  *AK = A::fmap(Bp, invK, A::mul(muK, SK));  // all terms >= 0
+  *AL = A::fmap(Bm, invL, A::mul(muL, SL));
 }
 
 // Dirichlet face (Solver.cc:143-164): B = -a_sigma; A = S + B+/(f+eps); R += B-.
 template <typename A>
 __device__ __forceinline__ void dirichlet_face(typename A::V aK, typename A::V SK, typename A::V invK,
                                                typename A::V* Aout, typename A::V* Bm) {
-  *Aout = A::fma(A::max0(A::sub(A::k(0.0), aK)), invK, SK);
+  *Aout = A::fmap(A::max0(A::sub(A::k(0.0), aK)), invK, SK);
   *Bm = A::max0(aK);
 }
 
@@ -410,7 +415,7 @@ __global__ void __launch_bounds__(kAsmThreads) k_assemble(Common cm, Geo geo, Fi
       V fv = zero, iv = zero;
       if (i >= 0 && i < nx && j >= 0 && j < ny) {
         fv = A::ld(fl.f, base + (long long)j * P + i);
-        iv = A::rcp(A::add(fv, A::k(kEps)));
+        iv = A::rcp(A::addp(fv, A::k(kEps)));
       }
       fS[hy][hx] = fv;
       iS[hy][hx] = iv;
@@ -437,13 +442,13 @@ __global__ void __launch_bounds__(kAsmThreads) k_assemble(Common cm, Geo geo, Fi
         if (xin && yin) {
           const V wL = A::ld(cm.wx, 2 * (I.xe + Iv)), wR = A::ld(cm.wx, 2 * (I.xe + Iv) + 1);
           const V wB = A::ld(cm.wy, 2 * (I.ye + Jv)), wT = A::ld(cm.wy, 2 * (I.ye + Jv) + 1);
-          val = A::fma(wB, A::fma(wL, f00, A::mul(wR, f10)), A::mul(wT, A::fma(wL, f01, A::mul(wR, f11))));
+          val = A::fmap(wB, A::fmap(wL, f00, A::mul(wR, f10)), A::mul(wT, A::fmap(wL, f01, A::mul(wR, f11))));
         } else if (yin) {  // vertical boundary edge: linear in y
           const V wB = A::ld(cm.wy, 2 * (I.ye + Jv)), wT = A::ld(cm.wy, 2 * (I.ye + Jv) + 1);
-          val = A::fma(wB, f00, A::mul(wT, f01));
+          val = A::fmap(wB, f00, A::mul(wT, f01));
         } else if (xin) {  // horizontal boundary edge: linear in x
           const V wL = A::ld(cm.wx, 2 * (I.xe + Iv)), wR = A::ld(cm.wx, 2 * (I.xe + Iv) + 1);
-          val = A::fma(wL, f00, A::mul(wR, f10));
+          val = A::fmap(wL, f00, A::mul(wR, f10));
         } else {
           val = f00;  // corner: the single adjacent cell
         }
@@ -516,23 +521,24 @@ __global__ void __launch_bounds__(kAsmThreads) k_assemble(Common cm, Geo geo, Fi
       const V Aw = xR[cy][cx], Ae = xL[cy][cx + 1], As = yT[cy][cx], An = yB[cy + 1][cx];
       const bool wIn = i > 0, eIn = i < nx - 1, sIn = j > 0, nIn = j < ny - 1;
       V D = zero, Rv = zero, dir = zero;
-      if (wIn) D = A::add(D, Aw);
-      if (eIn) D = A::add(D, Ae);
-      if (sIn) D = A::add(D, As);
-      if (nIn) D = A::add(D, An);
-      if (!wIn && I.bc[XMIN] == DIRICHLET) { D = A::add(D, Aw); dir = A::add(dir, Aw); Rv = A::add(Rv, xB[cy][cx]); }
-      if (!eIn && I.bc[XMAX] == DIRICHLET) { D = A::add(D, Ae); dir = A::add(dir, Ae); Rv = A::add(Rv, xB[cy][cx + 1]); }
-      if (!sIn && I.bc[YMIN] == DIRICHLET) { D = A::add(D, As); dir = A::add(dir, As); Rv = A::add(Rv, yR[cy][cx]); }
-      if (!nIn && I.bc[YMAX] == DIRICHLET) { D = A::add(D, An); dir = A::add(dir, An); Rv = A::add(Rv, yR[cy + 1][cx]); }
+      // every term below is >= 0
+      if (wIn) D = A::addp(D, Aw);
+      if (eIn) D = A::addp(D, Ae);
+      if (sIn) D = A::addp(D, As);
+      if (nIn) D = A::addp(D, An);
+      if (!wIn && I.bc[XMIN] == DIRICHLET) { D = A::addp(D, Aw); dir = A::addp(dir, Aw); Rv = A::addp(Rv, xB[cy][cx]); }
+      if (!eIn && I.bc[XMAX] == DIRICHLET) { D = A::addp(D, Ae); dir = A::addp(dir, Ae); Rv = A::addp(Rv, xB[cy][cx + 1]); }
+      if (!sIn && I.bc[YMIN] == DIRICHLET) { D = A::addp(D, As); dir = A::addp(dir, As); Rv = A::addp(Rv, yR[cy][cx]); }
+      if (!nIn && I.bc[YMAX] == DIRICHLET) { D = A::addp(D, An); dir = A::addp(dir, An); Rv = A::addp(Rv, yR[cy + 1][cx]); }
       const V sd = A::ld(geo.sdiag, K);
-      D = A::add(D, sd);
+      D = A::addp(D, sd);
       const V fK = fS[cy + 1][cx + 1];
-      Rv = A::fma(A::ld(geo.ukk, K), fK, Rv);
+      Rv = A::fmap(A::ld(geo.ukk, K), fK, Rv);
       rmax = fmaxf(rmax, fabsf(A::f32(Rv)));
       const V inv = A::rcp(D);
       A::st(fl.invD, K, inv);
       A::st(fl.R, K, Rv);
-      A::st(fl.colsum, K, A::add(sd, dir));
+      A::st(fl.colsum, K, A::addp(sd, dir));
       // start the solve from the linear extrapolation 2 f^n - f^(n-1) (only the starting point of
       // the iteration; the converged answer does not depend on it)
       const V g0 = has_prev ? A::sub(A::add(fK, fK), A::ld(fl.fprev, K)) : fK;
@@ -988,12 +994,13 @@ __global__ void __launch_bounds__(kThreads, 3) k_polish(Common cm, Fields fl, Co
         Q4<V> fo;
 #pragma unroll
         for (int m = 0; m < 4; ++m) {
-          const V yp = A::add(R.a[m], A::fma(cn.a[m], sm[o + m + P], A::fma(cs.a[m], sm[o + m - P],
-                                           A::fma(ce.a[m], sm[o + m + 1], A::mul(cw.a[m], sm[o + m - 1])))));
+          // every term is >= 0: R, the outflow fractions and max(y, 0)
+          const V yp = A::addp(R.a[m], A::fmap(cn.a[m], sm[o + m + P], A::fmap(cs.a[m], sm[o + m - P],
+                                            A::fmap(ce.a[m], sm[o + m + 1], A::mul(cw.a[m], sm[o + m - 1])))));
           const V fv = A::mul(yp, inv.a[m]);
           fo.a[m] = fv;
-          mass = A::fma(cols.a[m], fv, mass);
-          rsum = A::add(rsum, R.a[m]);
+          mass = A::fmap(cols.a[m], fv, mass);
+          rsum = A::addp(rsum, R.a[m]);
           if (row_i0 + m < I.nx) {
             clamp += A::lt0(A::ld(y, K + m)) ? 1.0f : 0.0f;
             mn = fminf(mn, A::f32(fv));
