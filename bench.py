@@ -288,14 +288,13 @@ def run_serving(capi, arrivals, probs, steps, precision, budget_gb):
                 time.sleep(max(0.0, arrivals[nxt] - (time.monotonic() - t0)))
             continue
         if srv.tick() > 0:
-            for rid in list(live):
+            for rid in srv.completed_ids():
                 r = srv.poll(rid, want_f=False)
-                if r is not None:
-                    k = live.pop(rid)
-                    _, st, ts, td = r
-                    lat.append(td - (t0 + arrivals[k]))
-                    min_f = min(min_f, st["min_f"])
-                    not_conv += int(st["status"] != 0)
+                k = live.pop(rid)
+                _, st, ts, td = r
+                lat.append(td - (t0 + arrivals[k]))
+                min_f = min(min_f, st["min_f"])
+                not_conv += int(st["status"] != 0)
     wall = time.monotonic() - t0
     info = srv.info()
     srv.close()
@@ -305,6 +304,7 @@ def run_serving(capi, arrivals, probs, steps, precision, budget_gb):
             "instance_steps_per_s": info["instance_steps"] / wall,
             "cell_steps_per_s": float(sum(p.nx * p.ny * int(s) for p, s in zip(probs, steps))) / wall,
             "requests_per_s": nreq / wall, "ticks": info["ticks"], "busy_s": info["busy_seconds"],
+            "tick_split_s": {k: info[k + "_seconds"] for k in ("admit", "lists", "step", "collect")},
             "min_f": min_f, "not_converged": not_conv, "device_gb": info["device_bytes"] / 1e9}
 
 

@@ -204,6 +204,10 @@ typedef struct sayram_server_info {
   double device_bytes;          /* bytes held by the server */
   double arena_cells, arena_cells_used;
   double busy_seconds;          /* wall time spent inside ticks that ran a step */
+  double admit_seconds;         /* of which: admitting requests (copies + set-up) */
+  double lists_seconds;         /*           rebuilding the work lists */
+  double step_seconds;          /*           launching the step and waiting for it */
+  double collect_seconds;       /*           copying finished results out */
 } sayram_server_info;
 
 int sayram_server_create(const sayram_server_config* cfg, const sayram_options* opt, sayram_server* out);
@@ -218,6 +222,8 @@ int sayram_server_tick(sayram_server s, int* n_completed);
 int sayram_server_poll(sayram_server s, long long id, double* f_out, sayram_stats* st, double* t_submit,
                        double* t_done);
 int sayram_server_info_get(sayram_server s, sayram_server_info* out);
+/* Ids of completed requests not yet polled (up to cap); returns how many were written. */
+int sayram_server_completed_ids(sayram_server s, long long* ids, int cap);
 void sayram_server_destroy(sayram_server s);
 
 /* ---- stepping without allocating -------------------------------------------------------

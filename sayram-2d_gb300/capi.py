@@ -66,7 +66,9 @@ class sayram_server_info(ctypes.Structure):
                 ("waiting", ctypes.c_longlong), ("resident", ctypes.c_longlong), ("ticks", ctypes.c_longlong),
                 ("instance_steps", ctypes.c_longlong), ("device_bytes", ctypes.c_double),
                 ("arena_cells", ctypes.c_double), ("arena_cells_used", ctypes.c_double),
-                ("busy_seconds", ctypes.c_double)]
+                ("busy_seconds", ctypes.c_double), ("admit_seconds", ctypes.c_double),
+                ("lists_seconds", ctypes.c_double), ("step_seconds", ctypes.c_double),
+                ("collect_seconds", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -116,6 +118,7 @@ SIGNATURES = {
     "sayram_server_tick": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),
     "sayram_server_poll": (ctypes.c_int, [_P, ctypes.c_longlong, _dp, ctypes.POINTER(sayram_stats), _dp, _dp]),
     "sayram_server_info_get": (ctypes.c_int, [_P, ctypes.POINTER(sayram_server_info)]),
+    "sayram_server_completed_ids": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
     "sayram_server_destroy": (None, [_P]),
     "sayram_step_noalloc": (ctypes.c_int, [ctypes.POINTER(sayram_problem), ctypes.POINTER(sayram_options),
                                            ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -375,6 +378,11 @@ class Server:
         check(rc, "sayram_server_poll")
         del self.shapes[rid]
         return f, st.as_dict(), t0.value, t1.value
+
+    def completed_ids(self, cap: int = 4096):
+        buf = (ctypes.c_longlong * cap)()
+        n = self._L.sayram_server_completed_ids(self.h, buf, cap)
+        return [buf[k] for k in range(n)]
 
     def info(self) -> dict:
         i = sayram_server_info()

@@ -1154,12 +1154,19 @@ struct sayram_server_s {
     const double t0 = now_seconds();
     int rc = admit();
     if (rc) return rc;
+    const double ta = now_seconds();
+    info.admit_seconds += ta - t0;
     if (dirty) {
       if ((rc = eng.rebuild_lists())) return rc;
       dirty = false;
     }
+    const double tl = now_seconds();
+    info.lists_seconds += tl - ta;
     if (info.resident == 0) return SAYRAM_OK;
     if ((rc = eng.launch_steps(1))) return rc;
+    SG_CUDA(cudaStreamSynchronize(eng.stream));
+    const double ts = now_seconds();
+    info.step_seconds += ts - tl;
     info.ticks++;
     info.instance_steps += info.resident;
     // completions: state rows back to the host, then free the slot
@@ -1178,6 +1185,7 @@ struct sayram_server_s {
     SG_CUDA(cudaStreamSynchronize(eng.stream));
     const double t1 = now_seconds();
     info.busy_seconds += t1 - t0;
+    info.collect_seconds += t1 - ts;
     for (size_t q = 0; q < fin.size(); ++q) {
       Slot& S = slots[fin[q]];
       InstDev& I = eng.hinst[fin[q]];
@@ -1316,6 +1324,16 @@ int sayram_server_info_get(sayram_server s, sayram_server_info* out) {
   *out = s->info;
   out->device_bytes = (double)s->eng.bytes;
   return SAYRAM_OK;
+}
+
+int sayram_server_completed_ids(sayram_server s, long long* ids, int cap) {
+  if (!s || (!ids && cap > 0)) return 0;
+  int n = 0;
+  for (auto& kv : s->results) {
+    if (n >= cap) break;
+    ids[n++] = kv.first;
+  }
+  return n;
 }
 
 void sayram_server_destroy(sayram_server s) { delete s; }
