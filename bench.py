@@ -320,6 +320,9 @@ def run_ours(a):
     prec = capi.FP32_REFINE_DW if a.precision == "dw" else capi.FP32_REFINE
     other = capi.FP32_REFINE if a.precision == "dw" else capi.FP32_REFINE_DW
     b = capi.Batch(probs, precision=prec, use_graph=0 if a.no_graph else 1)
+    t0 = time.perf_counter()
+    shape = b.autotune(2)
+    tune_s = time.perf_counter() - t0
     for _ in range(a.warmup):
         b.step(1, allow_not_converged=True)
     l0 = b.launches()
@@ -343,7 +346,9 @@ def run_ours(a):
                        "precision": ("fp32_refine_dw: FP32 Krylov, double-word (FP32-pair, ~48-bit) residual/"
                                      "refinement/assembly/checks" if a.precision == "dw" else
                                      "fp32_refine: FP32 Krylov, IEEE FP64 residual/refinement/assembly/checks"),
-                       "l2": f"working set {b.device_bytes() / 1e9:.1f} GB >> 129 MB L2 (no flush needed)"},
+                       "l2": f"working set {b.device_bytes() / 1e9:.1f} GB >> 129 MB L2 (no flush needed)",
+                       "launch_shape": {"cells_per_chunk": shape[0], "blocks_per_sm": shape[1],
+                                        "autotune_s": tune_s, "candidates": b.tuning_log()}},
             "gpu_launches": int(launches), "roofline": roof, "kernels": kern, "clocks": clocks,
             "status_last_step": rc, "setup_s": {"generate": gen_s}}
     # accuracy: per-instance stats and rel L2 against the batched FP64 path after the same steps
@@ -377,6 +382,7 @@ def run_ours(a):
         b.close()
         # the other refinement arithmetic on the same batch (device-timed, a few steps)
         bo = capi.Batch(probs, precision=other)
+        bo.autotune(2)
         for _ in range(2):
             bo.step(1, allow_not_converged=True)
         bo.record_event(0)
@@ -388,6 +394,7 @@ def run_ours(a):
         bo.close()
         # batched FP64 on the same batch, same number of steps -> accuracy + precision gain
         b64 = capi.Batch(probs, precision=capi.FP64)
+        b64.autotune(1)
         b64.step(nsteps_done - 1, allow_not_converged=True)
         b64.record_event(0)
         b64.step(1, allow_not_converged=True)

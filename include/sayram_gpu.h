@@ -175,6 +175,14 @@ int sayram_batch_elapsed_ms(sayram_batch b, int slot0, int slot1, double* ms);
 int sayram_batch_enable_timing(sayram_batch b, int enable);
 int sayram_batch_kernel_times(sayram_batch b, const char** names, double* total_ms,
                               long long* launches, int cap);
+/* Autotuner: times `steps` steps of each launch shape -- cells per block iteration (1024, 2048,
+ * 4096) x resident blocks per SM (8, 16, 32) -- on this batch's own instances and keeps the
+ * fastest. The instances' state is restored afterwards, so tuning does not advance the
+ * simulation. Writes the choice if the pointers are not NULL. */
+int sayram_batch_autotune(sayram_batch b, int steps, int* chunk_out, int* blocks_per_sm_out);
+/* The timings of the last autotune: up to cap (chunk, blocks per SM, ms per step) entries;
+ * returns the number of candidates measured. */
+int sayram_batch_tuning_log(sayram_batch b, int* chunks, int* blocks_per_sm, double* ms_per_step, int cap);
 /* Kernel launches issued by this batch since creation (counted on the device). */
 long long sayram_batch_launches(sayram_batch b);
 void sayram_batch_destroy(sayram_batch b);

@@ -108,6 +108,8 @@ SIGNATURES = {
     "sayram_batch_elapsed_ms": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, _dp]),
     "sayram_batch_enable_timing": (ctypes.c_int, [_P, ctypes.c_int]),
     "sayram_batch_kernel_times": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_char_p), _dp, ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
+    "sayram_batch_autotune": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
+    "sayram_batch_tuning_log": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), _dp, ctypes.c_int]),
     "sayram_batch_launches": (ctypes.c_longlong, [_P]),
     "sayram_batch_destroy": (None, [_P]),
     "sayram_instance_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
@@ -295,6 +297,18 @@ class Batch:
         cnt = (ctypes.c_longlong * cap)()
         m = self._L.sayram_batch_kernel_times(self.h, names, ms, cnt, cap)
         return {names[k].decode(): (ms[k], cnt[k]) for k in range(min(m, cap))}
+
+    def autotune(self, steps: int = 2):
+        """Picks the fastest launch shape on this batch (state restored); returns (chunk, blocks/SM)."""
+        ch, gm = ctypes.c_int(), ctypes.c_int()
+        check(self._L.sayram_batch_autotune(self.h, int(steps), ctypes.byref(ch), ctypes.byref(gm)), "sayram_batch_autotune")
+        return ch.value, gm.value
+
+    def tuning_log(self):
+        cap = 32
+        c, g, m = (ctypes.c_int * cap)(), (ctypes.c_int * cap)(), (ctypes.c_double * cap)()
+        n = self._L.sayram_batch_tuning_log(self.h, c, g, m, cap)
+        return [{"chunk": c[k], "blocks_per_sm": g[k], "ms_per_step": m[k]} for k in range(min(n, cap))]
 
     def launches(self) -> int:
         return int(self._L.sayram_batch_launches(self.h))

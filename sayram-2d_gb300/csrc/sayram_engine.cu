@@ -173,28 +173,55 @@ struct sayram_batch_s {
     evused = 0;
   }
 
-  int grid_stream() const { return std::max(1, std::min(cap_chunks, nsm * 16)); }
+  // launch shape of the streaming kernels: cells per chunk (one block iteration) and blocks per SM
+  int chunk = 2048;
+  int gmult = 16;
+  int grid_stream() const { return std::max(1, std::min(cap_chunks, nsm * gmult)); }
+  int nchunks_of(int nx, int ny) const {
+    const long long cells = round_up((long long)ny * round_up(nx, 4), 4);
+    return (int)((cells + chunk - 1) / chunk);
+  }
   // dynamic shared memory of the SpMV kernels: the chunk plus one row above and below
   template <typename T>
-  size_t smem_spmv() const { return (size_t)(sg::kChunk + 2 * pmax) * sizeof(T); }
-  template <typename T>
-  int prep_spmv() {
-    const int bytes = (int)smem_spmv<T>();
-    if (bytes > 227 * 1024) return fail(SAYRAM_ERR_ARG, "rows too wide for the shared-memory stencil");
-    SG_CUDA(cudaFuncSetAttribute(sg::k_bicg1<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-    SG_CUDA(cudaFuncSetAttribute(sg::k_bicg2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-    return SAYRAM_OK;
-  }
+  size_t smem_spmv() const { return (size_t)(chunk + 2 * pmax) * sizeof(T); }
   // the residual and polish kernels stage the 8-byte wide solution
-  size_t smem_wide() const { return (size_t)(sg::kChunk + 2 * pmax) * 8; }
-  template <typename T, typename C, typename A>
-  int prep_wide() {
-    const int bytes = (int)smem_wide();
-    if (bytes > 227 * 1024) return fail(SAYRAM_ERR_ARG, "rows too wide for the shared-memory stencil");
-    SG_CUDA(cudaFuncSetAttribute(sg::k_resid<T, C, A>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-    SG_CUDA(cudaFuncSetAttribute(sg::k_polish<C, A>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  size_t smem_wide() const { return (size_t)(chunk + 2 * pmax) * 8; }
+  template <typename T, typename C, typename A, int CH>
+  int prep_kernels() {
+    const int b1 = (int)smem_spmv<T>(), b2 = (int)smem_wide();
+    if (b1 > 227 * 1024 || b2 > 227 * 1024) return fail(SAYRAM_ERR_ARG, "rows too wide for the shared-memory stencil");
+    SG_CUDA(cudaFuncSetAttribute(sg::k_bicg1<T, CH>, cudaFuncAttributeMaxDynamicSharedMemorySize, b1));
+    SG_CUDA(cudaFuncSetAttribute(sg::k_bicg2<T, CH>, cudaFuncAttributeMaxDynamicSharedMemorySize, b1));
+    SG_CUDA(cudaFuncSetAttribute(sg::k_resid<T, C, A, CH>, cudaFuncAttributeMaxDynamicSharedMemorySize, b2));
+    SG_CUDA(cudaFuncSetAttribute(sg::k_polish<C, A, CH>, cudaFuncAttributeMaxDynamicSharedMemorySize, b2));
     return SAYRAM_OK;
   }
+  // dispatch of the per-step sequence on precision and chunk size (graph: build it; else: run it)
+  template <typename T, typename C, typename A>
+  int run_chunked(const sg::Coef<C>& cf, const sg::Coef<T>& ck, const sg::Kry<T>& kr, bool as_graph) {
+    switch (chunk) {
+      case 1024: return as_graph ? build_graph<T, C, A, 1024>(cf, ck, kr) : step_once<T, C, A, 1024>(cf, ck, kr);
+      case 2048: return as_graph ? build_graph<T, C, A, 2048>(cf, ck, kr) : step_once<T, C, A, 2048>(cf, ck, kr);
+      default: return as_graph ? build_graph<T, C, A, 4096>(cf, ck, kr) : step_once<T, C, A, 4096>(cf, ck, kr);
+    }
+  }
+  int run_mode(bool as_graph) {
+    return dwm ? run_chunked<float, float, sg::DWA>(c32, c32, k32, as_graph)
+           : mixed ? run_chunked<float, float, sg::F64A>(c32, c32, k32, as_graph)
+                   : run_chunked<double, double, sg::F64A>(c64, c64, k64, as_graph);
+  }
+  void drop_graph() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (graph) cudaGraphDestroy(graph);
+    gexec = nullptr;
+    graph = nullptr;
+  }
+  int autotune(int steps, int* best_chunk, int* best_grid);
+  struct Tuned {
+    int chunk, gmult;
+    double ms_per_step;
+  };
+  std::vector<Tuned> tune_log;
   int grid_tiles() const { return std::max(1, std::min(cap_tiles, nsm * 8)); }
 
   int build(const sayram_problem* probs, int count, const sayram_options* o);
@@ -211,9 +238,9 @@ struct sayram_batch_s {
   int launch_steps(int nsteps);  // queue steps on the stream (no status read-back)
   int read_ctl();
   int finish_status();
-  template <typename T, typename C, typename A>
+  template <typename T, typename C, typename A, int CH>
   int step_once(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, const sg::Kry<T>& kr);
-  template <typename T, typename C, typename A>
+  template <typename T, typename C, typename A, int CH>
   int build_graph(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, const sg::Kry<T>& kr);
   int last_captured(cudaGraphNode_t* node);
   // wide (8-byte) table entries: a double, or a (hi, lo) float pair in double-word mode
@@ -383,7 +410,7 @@ int sayram_batch_s::place(int b, const sayram_problem& p, long long base, int xe
   I.hoff = hoff;
   I.ntx = (p.nx + sg::kTX - 1) / sg::kTX;
   I.nty = (p.ny + sg::kTY - 1) / sg::kTY;
-  I.nchunks = (int)((round_up((long long)p.ny * I.pitch, 4) + sg::kChunk - 1) / sg::kChunk);
+  I.nchunks = nchunks_of(p.nx, p.ny);
   I.xe = xe_off;
   I.ye = ye_off;
   for (int s = 0; s < 4; ++s) I.dir[s] = p.bc[s] == SAYRAM_DIRICHLET ? dir_off[s] : -1;
@@ -427,6 +454,7 @@ int sayram_batch_s::rebuild_lists() {
     InstDev& I = hinst[b];
     if (!I.enabled) continue;
     ninst = b + 1;
+    I.nchunks = nchunks_of(I.nx, I.ny);
     I.chunk0 = (int)h_chunk.size();
     for (int k = 0; k < I.nchunks; ++k) h_chunk.push_back(b);
     I.tile0 = (int)h_tile.size();
@@ -470,7 +498,7 @@ int sayram_batch_s::build(const sayram_problem* probs, int count, const sayram_o
     cursor += round_up((long long)(p.ny + 2) * pitch, 32);
     hoff[b] = h;
     h += (long long)p.nx * p.ny;
-    chunks += (int)((round_up((long long)p.ny * pitch, 4) + sg::kChunk - 1) / sg::kChunk);
+    chunks += (int)((round_up((long long)p.ny * pitch, 4) + 1023) / 1024);  // room for any chunk size
     tiles += ((p.nx + sg::kTX - 1) / sg::kTX) * ((p.ny + sg::kTY - 1) / sg::kTY);
     xoffv[b] = xoff;
     xoff += p.nx + 1;
@@ -483,6 +511,8 @@ int sayram_batch_s::build(const sayram_problem* probs, int count, const sayram_o
     maxcells = std::max(maxcells, (long long)p.nx * p.ny);
   }
   nreal = h;
+  // default launch shape: the largest chunk that still gives every SM several blocks
+  chunk = nreal >= 8LL * 4096 * nsm ? 4096 : nreal >= 8LL * 2048 * nsm ? 2048 : 1024;
   if ((rc = alloc_storage(cursor + 64, count, chunks, tiles, xoff, yoff, doff, std::max(6 * maxcells, nreal))))
     return rc;
   n = count;
@@ -523,19 +553,18 @@ int sayram_batch_s::read_ctl() {
   return SAYRAM_OK;
 }
 
-template <typename T, typename C, typename A>
+template <typename T, typename C, typename A, int CH>
 int sayram_batch_s::step_once(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, const sg::Kry<T>& kr) {
   using namespace sg;
   const int gs = grid_stream(), gt = grid_tiles();
-  int prc = prep_spmv<T>();
-  if (!prc) prc = prep_wide<T, C, A>();
+  int prc = prep_kernels<T, C, A, CH>();
   if (prc) return prc;
   SG_CUDA(cudaMemsetAsync(d_ctl, 0, 2 * sizeof(int), stream));
   launch("begin", [&] { k_begin<<<(n + 255) / 256, 256, 0, stream>>>(cm); });
   launch("assemble", [&] { k_assemble<C, A><<<gt, kAsmThreads, 0, stream>>>(cm, geo, fl, cfull); });
   for (int o = 0; o < opt.max_refine; ++o) {
     launch("resid", [&] {
-      k_resid<T, C, A><<<gs, kThreads, smem_wide(), stream>>>(cm, fl, cfull, kr, opt.tol, opt.inner_tol, opt.max_refine);
+      k_resid<T, C, A, CH><<<gs, kThreads, smem_wide(), stream>>>(cm, fl, cfull, kr, opt.tol, opt.inner_tol, opt.max_refine);
     });
     SG_CUDA(cudaGetLastError());
     if (o == opt.max_refine - 1) break;
@@ -543,9 +572,9 @@ int sayram_batch_s::step_once(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, c
     if (rc) return rc;
     if (h_ctl->n_outer == 0) break;
     for (int it = 0; it < opt.max_iters; ++it) {
-      launch("bicg1", [&] { k_bicg1<T><<<gs, kThreads, smem_spmv<T>(), stream>>>(cm, ck, kr); });
-      launch("bicg2", [&] { k_bicg2<T><<<gs, kThreads, smem_spmv<T>(), stream>>>(cm, ck, kr); });
-      launch("bicg3", [&] { k_bicg3<T><<<gs, kThreads, 0, stream>>>(cm, kr, opt.max_iters); });
+      launch("bicg1", [&] { k_bicg1<T, CH><<<gs, kThreads, smem_spmv<T>(), stream>>>(cm, ck, kr); });
+      launch("bicg2", [&] { k_bicg2<T, CH><<<gs, kThreads, smem_spmv<T>(), stream>>>(cm, ck, kr); });
+      launch("bicg3", [&] { k_bicg3<T, CH><<<gs, kThreads, 0, stream>>>(cm, kr, opt.max_iters); });
       SG_CUDA(cudaGetLastError());
       if (it < 4 || (it & 3) == 3) {
         rc = read_ctl();
@@ -554,7 +583,7 @@ int sayram_batch_s::step_once(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, c
       }
     }
   }
-  launch("polish", [&] { k_polish<C, A><<<gs, kThreads, smem_wide(), stream>>>(cm, fl, cfull); });
+  launch("polish", [&] { k_polish<C, A, CH><<<gs, kThreads, smem_wide(), stream>>>(cm, fl, cfull); });
   SG_CUDA(cudaGetLastError());
   return SAYRAM_OK;
 }
@@ -571,12 +600,11 @@ int sayram_batch_s::last_captured(cudaGraphNode_t* node) {
 
 // One step as a graph: memset + begin + assemble, WHILE(outer){ resid, WHILE(inner){ k1 k2 k3 } },
 // polish. The WHILE conditions are set on the device by the residual and Krylov kernels.
-template <typename T, typename C, typename A>
+template <typename T, typename C, typename A, int CH>
 int sayram_batch_s::build_graph(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, const sg::Kry<T>& kr) {
   using namespace sg;
   const int gs = grid_stream(), gt = grid_tiles();
-  int prc = prep_spmv<T>();
-  if (!prc) prc = prep_wide<T, C, A>();
+  int prc = prep_kernels<T, C, A, CH>();
   if (prc) return prc;
   const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
   cudaGraph_t g = nullptr;
@@ -611,7 +639,7 @@ int sayram_batch_s::build_graph(const sg::Coef<C>& cfull, const sg::Coef<T>& ck,
   c2.h_inner = hin;
   cudaGraphNode_t rnode;
   SG_CUDA(cudaStreamBeginCaptureToGraph(stream, obody, nullptr, nullptr, 0, mode));
-  k_resid<T, C, A><<<gs, kThreads, smem_wide(), stream>>>(c2, fl, cfull, kr, opt.tol, opt.inner_tol, opt.max_refine);
+  k_resid<T, C, A, CH><<<gs, kThreads, smem_wide(), stream>>>(c2, fl, cfull, kr, opt.tol, opt.inner_tol, opt.max_refine);
   if ((rc = last_captured(&rnode))) { cudaStreamEndCapture(stream, &obody); return rc; }
   SG_CUDA(cudaStreamEndCapture(stream, &obody));
   // inner WHILE inside the outer body
@@ -624,13 +652,13 @@ int sayram_batch_s::build_graph(const sg::Coef<C>& cfull, const sg::Coef<T>& ck,
   SG_CUDA(cudaGraphAddNode(&inner, obody, &rnode, nullptr, 1, &ip));
   cudaGraph_t ibody = ip.conditional.phGraph_out[0];
   SG_CUDA(cudaStreamBeginCaptureToGraph(stream, ibody, nullptr, nullptr, 0, mode));
-  k_bicg1<T><<<gs, kThreads, smem_spmv<T>(), stream>>>(c2, ck, kr);
-  k_bicg2<T><<<gs, kThreads, smem_spmv<T>(), stream>>>(c2, ck, kr);
-  k_bicg3<T><<<gs, kThreads, 0, stream>>>(c2, kr, opt.max_iters);
+  k_bicg1<T, CH><<<gs, kThreads, smem_spmv<T>(), stream>>>(c2, ck, kr);
+  k_bicg2<T, CH><<<gs, kThreads, smem_spmv<T>(), stream>>>(c2, ck, kr);
+  k_bicg3<T, CH><<<gs, kThreads, 0, stream>>>(c2, kr, opt.max_iters);
   SG_CUDA(cudaStreamEndCapture(stream, &ibody));
   // suffix
   SG_CUDA(cudaStreamBeginCaptureToGraph(stream, g, &outer, nullptr, 1, mode));
-  k_polish<C, A><<<gs, kThreads, smem_wide(), stream>>>(c2, fl, cfull);
+  k_polish<C, A, CH><<<gs, kThreads, smem_wide(), stream>>>(c2, fl, cfull);
   SG_CUDA(cudaStreamEndCapture(stream, &g));
   SG_CUDA(cudaGraphInstantiate(&gexec, g, 0));
   return SAYRAM_OK;
@@ -649,14 +677,9 @@ int sayram_batch_s::launch_steps(int nsteps) {
   SG_CUDA(cudaSetDevice(dev));
   const bool use_graph = opt.use_graph && !timing;
   if (use_graph && !gexec) {
-    int rc = dwm ? build_graph<float, float, sg::DWA>(c32, c32, k32)
-             : mixed ? build_graph<float, float, sg::F64A>(c32, c32, k32)
-                     : build_graph<double, double, sg::F64A>(c64, c64, k64);
+    int rc = run_mode(true);
     if (rc) {
-      if (gexec) cudaGraphExecDestroy(gexec);
-      if (graph) cudaGraphDestroy(graph);
-      gexec = nullptr;
-      graph = nullptr;
+      drop_graph();
       return rc;
     }
   }
@@ -665,11 +688,81 @@ int sayram_batch_s::launch_steps(int nsteps) {
       SG_CUDA(cudaGraphLaunch(gexec, stream));
       continue;
     }
-    int rc = dwm ? step_once<float, float, sg::DWA>(c32, c32, k32)
-             : mixed ? step_once<float, float, sg::F64A>(c32, c32, k32)
-                     : step_once<double, double, sg::F64A>(c64, c64, k64);
+    int rc = run_mode(false);
     if (rc) return rc;
   }
+  return SAYRAM_OK;
+}
+
+// Times `steps` steps of every launch shape (cells per chunk x blocks per SM) from the same
+// state and keeps the fastest; f, the previous f and the per-instance state are restored
+// afterwards, so tuning does not advance the simulation.
+int sayram_batch_s::autotune(int steps, int* best_chunk, int* best_grid) {
+  if (steps < 1) steps = 1;
+  SG_CUDA(cudaSetDevice(dev));
+  double *bf = nullptr, *bp = nullptr;
+  if (cudaMalloc(&bf, sizeof(double) * ncell) != cudaSuccess || cudaMalloc(&bp, sizeof(double) * ncell) != cudaSuccess) {
+    cudaGetLastError();
+    if (bf) cudaFree(bf);
+    return fail(SAYRAM_ERR_OOM, "autotune: no room for the state snapshot");
+  }
+  std::vector<InstState> hs(cap_slots);
+  SG_CUDA(cudaMemcpyAsync(bf, fl.f, sizeof(double) * ncell, cudaMemcpyDeviceToDevice, stream));
+  SG_CUDA(cudaMemcpyAsync(bp, fl.fprev, sizeof(double) * ncell, cudaMemcpyDeviceToDevice, stream));
+  SG_CUDA(cudaMemcpyAsync(hs.data(), d_st, sizeof(InstState) * cap_slots, cudaMemcpyDeviceToHost, stream));
+  SG_CUDA(cudaStreamSynchronize(stream));
+  auto restore = [&]() -> int {
+    SG_CUDA(cudaMemcpyAsync(fl.f, bf, sizeof(double) * ncell, cudaMemcpyDeviceToDevice, stream));
+    SG_CUDA(cudaMemcpyAsync(fl.fprev, bp, sizeof(double) * ncell, cudaMemcpyDeviceToDevice, stream));
+    SG_CUDA(cudaMemcpyAsync(d_st, hs.data(), sizeof(InstState) * cap_slots, cudaMemcpyHostToDevice, stream));
+    SG_CUDA(cudaStreamSynchronize(stream));
+    return SAYRAM_OK;
+  };
+  cudaEvent_t e0, e1;
+  SG_CUDA(cudaEventCreate(&e0));
+  SG_CUDA(cudaEventCreate(&e1));
+  const int chunks[3] = {1024, 2048, 4096}, grids[3] = {8, 16, 32};
+  const bool timing_was = timing;
+  timing = false;  // per-kernel events would split the graph into a host loop
+  double best = 1e300;
+  int bc = chunk, bg = gmult, rc = SAYRAM_OK;
+  tune_log.clear();
+  for (int ci = 0; ci < 3 && rc == SAYRAM_OK; ++ci)
+    for (int gi = 0; gi < 3 && rc == SAYRAM_OK; ++gi) {
+      chunk = chunks[ci];
+      gmult = grids[gi];
+      drop_graph();
+      if ((rc = rebuild_lists())) break;
+      if ((rc = launch_steps(1))) break;  // builds the graph, warms up
+      if ((rc = restore())) break;
+      cudaEventRecord(e0, stream);
+      if ((rc = launch_steps(steps))) break;
+      cudaEventRecord(e1, stream);
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      tune_log.push_back({chunk, gmult, (double)ms / steps});
+      if (ms < best) {
+        best = ms;
+        bc = chunk;
+        bg = gmult;
+      }
+      if ((rc = restore())) break;
+    }
+  chunk = bc;
+  gmult = bg;
+  drop_graph();
+  int rc2 = rebuild_lists();
+  if (!rc2) rc2 = restore();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(bf);
+  cudaFree(bp);
+  timing = timing_was;
+  if (rc) return rc;
+  if (rc2) return rc2;
+  if (best_chunk) *best_chunk = bc;
+  if (best_grid) *best_grid = bg;
   return SAYRAM_OK;
 }
 
@@ -751,8 +844,9 @@ int sayram_batch_step_host(sayram_batch b, int nsteps, const double* f_in, doubl
   SG_CUDA(cudaSetDevice(b->dev));
   if (f_in) {
     SG_CUDA(cudaMemcpyAsync(b->d_stage, f_in, sizeof(double) * b->nreal, cudaMemcpyHostToDevice, b->stream));
-    for (int k = 0; k < b->n; ++k)  // a replaced state has no previous step to extrapolate from
-      SG_CUDA(cudaMemsetAsync((char*)(b->d_st + k) + offsetof(InstState, has_prev), 0, sizeof(int), b->stream));
+    // a replaced state has no previous step to extrapolate from
+    SG_CUDA(cudaMemset2DAsync((char*)b->d_st + offsetof(InstState, has_prev), sizeof(InstState), 0, sizeof(int),
+                              (size_t)b->n, b->stream));
     b->launch("field_in", [&] {
       if (b->dwm)
         sg::k_field_in<sg::DWA><<<b->grid_tiles(), 256, 0, b->stream>>>(b->cm, b->fl.f, b->d_stage);
@@ -944,6 +1038,22 @@ int sayram_batch_kernel_times(sayram_batch b, const char** names, double* total_
     if (names) names[k] = b->tnames[k].c_str();
     if (total_ms) total_ms[k] = b->tms[k];
     if (launches) launches[k] = b->tcount[k];
+  }
+  return m;
+}
+
+int sayram_batch_autotune(sayram_batch b, int steps, int* chunk_out, int* blocks_per_sm_out) {
+  if (!b) return fail(SAYRAM_ERR_ARG, "null handle");
+  return b->autotune(steps, chunk_out, blocks_per_sm_out);
+}
+
+int sayram_batch_tuning_log(sayram_batch b, int* chunks, int* blocks_per_sm, double* ms_per_step, int cap) {
+  if (!b) return fail(SAYRAM_ERR_ARG, "null handle");
+  const int m = (int)b->tune_log.size();
+  for (int k = 0; k < m && k < cap; ++k) {
+    if (chunks) chunks[k] = b->tune_log[k].chunk;
+    if (blocks_per_sm) blocks_per_sm[k] = b->tune_log[k].gmult;
+    if (ms_per_step) ms_per_step[k] = b->tune_log[k].ms_per_step;
   }
   return m;
 }
@@ -1254,7 +1364,7 @@ int sayram_server_create(const sayram_server_config* cfg, const sayram_options* 
     return fail(SAYRAM_ERR_BUDGET, "HBM budget too small for any instance");
   }
   const long long side_tiles = (long long)c.max_slots * (c.max_side / sg::kTX + c.max_side / sg::kTY + 2);
-  const int chunks_cap = (int)std::min<long long>(cells / sg::kChunk + c.max_slots + 1, 1LL << 30);
+  const int chunks_cap = (int)std::min<long long>(cells / 1024 + c.max_slots + 1, 1LL << 30);
   const int tiles_cap = (int)std::min<long long>(cells / (sg::kTX * sg::kTY) + side_tiles, 1LL << 30);
   rc = e.alloc_storage(cells + 64, c.max_slots, chunks_cap, tiles_cap, (long long)c.max_slots * ms,
                        (long long)c.max_slots * ms, 4LL * c.max_slots * ms,
@@ -1349,7 +1459,8 @@ namespace {
 
 constexpr long long kNoAllocCells = 73728;  // padded cells: round_up((ny+2)*round_up(nx,4), 32) + 64
 constexpr int kNoAllocMaxSide = 4096;       // nx, ny limit (host tables are on the stack)
-constexpr int kNoAllocMaxChunks = (int)(kNoAllocCells / sg::kChunk) + 2;
+constexpr int kNoAllocChunk = 1024;  // cells per chunk of the streaming kernels on this path
+constexpr int kNoAllocMaxChunks = (int)(kNoAllocCells / kNoAllocChunk) + 2;
 constexpr int kNoAllocMaxTiles = 8192;
 constexpr size_t kNoAllocTableBytes = 1u << 20;
 constexpr size_t kNoAllocBytes = kNoAllocTableBytes + (size_t)kNoAllocCells * 27 * sizeof(double);
@@ -1471,7 +1582,7 @@ extern "C" int sayram_step_noalloc(const sayram_problem* pd, const sayram_option
   I.base = pitch;
   I.hoff = 0;
   I.chunk0 = 0;
-  I.nchunks = (int)((round_up((long long)ny * pitch, 4) + kChunk - 1) / kChunk);
+  I.nchunks = (int)((round_up((long long)ny * pitch, 4) + kNoAllocChunk - 1) / kNoAllocChunk);
   I.tile0 = 0;
   I.ntx = (nx + kTX - 1) / kTX;
   I.nty = (ny + kTY - 1) / kTY;
@@ -1571,11 +1682,11 @@ extern "C" int sayram_step_noalloc(const sayram_problem* pd, const sayram_option
   const int gt = std::max(1, std::min(cm.ntiles, nsm * 8));
   const int gs = std::max(1, std::min(cm.nchunks, nsm * 16));
   k_field_in<F64A><<<gt, 256, 0, stream>>>(cm, fl.f, f_in);
-  const size_t smem_na = (size_t)(kChunk + 2 * pitch) * sizeof(double);
-  SG_CUDA(cudaFuncSetAttribute(k_bicg1<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_na));
-  SG_CUDA(cudaFuncSetAttribute(k_bicg2<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_na));
-  SG_CUDA(cudaFuncSetAttribute(k_resid<double, double, F64A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_na));
-  SG_CUDA(cudaFuncSetAttribute(k_polish<double, F64A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_na));
+  const size_t smem_na = (size_t)(kNoAllocChunk + 2 * pitch) * sizeof(double);
+  SG_CUDA(cudaFuncSetAttribute(k_bicg1<double, kNoAllocChunk>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_na));
+  SG_CUDA(cudaFuncSetAttribute(k_bicg2<double, kNoAllocChunk>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_na));
+  SG_CUDA(cudaFuncSetAttribute(k_resid<double, double, F64A, kNoAllocChunk>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_na));
+  SG_CUDA(cudaFuncSetAttribute(k_polish<double, F64A, kNoAllocChunk>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_na));
   SG_CUDA(cudaGetLastError());
   Ctl hctl;
   for (int s = 0; s < nsteps; ++s) {
@@ -1583,16 +1694,16 @@ extern "C" int sayram_step_noalloc(const sayram_problem* pd, const sayram_option
     k_begin<<<1, 32, 0, stream>>>(cm);
     k_assemble<double, F64A><<<gt, kAsmThreads, 0, stream>>>(cm, geo, fl, co);
     for (int r = 0; r < o.max_refine; ++r) {
-      k_resid<double, double, F64A><<<gs, kThreads, smem_na, stream>>>(cm, fl, co, kr, o.tol, o.inner_tol, o.max_refine);
+      k_resid<double, double, F64A, kNoAllocChunk><<<gs, kThreads, smem_na, stream>>>(cm, fl, co, kr, o.tol, o.inner_tol, o.max_refine);
       SG_CUDA(cudaGetLastError());
       if (r == o.max_refine - 1) break;
       SG_CUDA(cudaMemcpyAsync(&hctl, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, stream));
       SG_CUDA(cudaStreamSynchronize(stream));
       if (hctl.n_outer == 0) break;
       for (int it = 0; it < o.max_iters; ++it) {
-        k_bicg1<double><<<gs, kThreads, smem_na, stream>>>(cm, co, kr);
-        k_bicg2<double><<<gs, kThreads, smem_na, stream>>>(cm, co, kr);
-        k_bicg3<double><<<gs, kThreads, 0, stream>>>(cm, kr, o.max_iters);
+        k_bicg1<double, kNoAllocChunk><<<gs, kThreads, smem_na, stream>>>(cm, co, kr);
+        k_bicg2<double, kNoAllocChunk><<<gs, kThreads, smem_na, stream>>>(cm, co, kr);
+        k_bicg3<double, kNoAllocChunk><<<gs, kThreads, 0, stream>>>(cm, kr, o.max_iters);
         SG_CUDA(cudaGetLastError());
         if (it < 4 || (it & 3) == 3) {
           SG_CUDA(cudaMemcpyAsync(&hctl, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, stream));
@@ -1601,7 +1712,7 @@ extern "C" int sayram_step_noalloc(const sayram_problem* pd, const sayram_option
         }
       }
     }
-    k_polish<double, F64A><<<gs, kThreads, smem_na, stream>>>(cm, fl, co);
+    k_polish<double, F64A, kNoAllocChunk><<<gs, kThreads, smem_na, stream>>>(cm, fl, co);
     SG_CUDA(cudaGetLastError());
   }
   k_field_out<F64A><<<gt, 256, 0, stream>>>(cm, f_out, fl.f);

@@ -561,13 +561,15 @@ struct Slot {
   long long K;
   bool valid;
 };
+template <int CH>
 __device__ __forceinline__ long long chunk_start(int c, const InstDev& I) {
-  return I.base + (long long)(c - I.chunk0) * kChunk;
+  return I.base + (long long)(c - I.chunk0) * CH;
 }
 __device__ __forceinline__ long long inst_end(const InstDev& I) { return I.base + (long long)I.ny * I.pitch; }
+template <int CH>
 __device__ __forceinline__ Slot slot_of(int c, const InstDev& I, int g) {
   Slot s;
-  s.K = chunk_start(c, I) + 4 * (threadIdx.x + g * kThreads);
+  s.K = chunk_start<CH>(c, I) + 4 * (threadIdx.x + g * kThreads);
   s.valid = s.K < inst_end(I);
   return s;
 }
@@ -664,7 +666,7 @@ __device__ __forceinline__ Q4<typename A::V> stencilW(const Q4<typename A::V>& c
 // ------------------------------------------------------------------------------ outer residual
 // r = R - A~ (y + x) in the wide arithmetic; writes y + x to the other y buffer and r (T precision).
 // Partials: ||r||^2, ||R||^2.
-template <typename T, typename C, typename A>
+template <typename T, typename C, typename A, int CH>
 __global__ void __launch_bounds__(kThreads, 3) k_resid(Common cm, Fields fl, Coef<C> co, Kry<T> kr,
                                                         double tol, double inner_tol, int max_refine) {
   using V = typename A::V;
@@ -682,8 +684,8 @@ __global__ void __launch_bounds__(kThreads, 3) k_resid(Common cm, Fields fl, Coe
     const float sc = rhs_scale(st.rmax_bits);  // r is handed over as r * sc
     const float isc = 1.0f / sc;                // exact: sc is a power of two
     const int P = I.pitch;
-    const long long c0 = chunk_start(c, I);
-    const long long c1 = min(c0 + (long long)kChunk, inst_end(I));
+    const long long c0 = chunk_start<CH>(c, I);
+    const long long c1 = min(c0 + (long long)CH, inst_end(I));
     const long long e0 = c0 - P;
     // y + x (the last Krylov correction, in scaled units) over the chunk and one row each side
     stage_rows<V>(sm, e0, (c1 - c0) + 2LL * P, [&](long long k) {
@@ -698,7 +700,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_resid(Common cm, Fields fl, Coe
     __syncthreads();
     typename A::Acc q0 = 0, q1 = 0;
 #pragma unroll 1
-    for (int g = 0; g < kGroups; ++g) {
+    for (int g = 0; g < CH / (4 * kThreads); ++g) {
       const long long K = c0 + 4 * (threadIdx.x + g * kThreads);
       if (K < c1) {
         const long long o = K - e0;
@@ -761,7 +763,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_resid(Common cm, Fields fl, Coe
 // k1: p = r + beta (p_old - omega v_old)  (p = r on a restart, which also sets r^ = r);
 //     v = A~ p;  partial (r^, v). p is computed once per cell into shared memory (chunk plus one
 //     row above and below) and the stencil reads it there.
-template <typename T>
+template <typename T, int CH>
 __global__ void __launch_bounds__(kThreads) k_bicg1(Common cm, Coef<T> co, Kry<T> kr) {
   count_launch(cm.ctl);
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -780,8 +782,8 @@ __global__ void __launch_bounds__(kThreads) k_bicg1(Common cm, Coef<T> co, Kry<T
     T* __restrict__ pn = kr.p[pc ^ 1];
     T* __restrict__ vn = kr.v[pc ^ 1];
     const int P = I.pitch;
-    const long long c0 = chunk_start(c, I);
-    const long long c1 = min(c0 + (long long)kChunk, inst_end(I));
+    const long long c0 = chunk_start<CH>(c, I);
+    const long long c1 = min(c0 + (long long)CH, inst_end(I));
     const long long e0 = c0 - P;
     stage_rows<T>(sm, e0, (c1 - c0) + 2LL * P, [&](long long k) {
       Q4<T> x = ld4(r + k);
@@ -795,7 +797,7 @@ __global__ void __launch_bounds__(kThreads) k_bicg1(Common cm, Coef<T> co, Kry<T
     __syncthreads();
     T q[1] = {(T)0};
 #pragma unroll 2
-    for (int g = 0; g < kGroups; ++g) {
+    for (int g = 0; g < CH / (4 * kThreads); ++g) {
       const long long K = c0 + 4 * (threadIdx.x + g * kThreads);
       if (K < c1) {
         const long long o = K - e0;
@@ -834,7 +836,7 @@ __global__ void __launch_bounds__(kThreads) k_bicg1(Common cm, Coef<T> co, Kry<T
 }
 
 // k2: s = r - alpha v;  t = A~ s;  partials (t, s), (t, t). s is staged like p in k1.
-template <typename T>
+template <typename T, int CH>
 __global__ void __launch_bounds__(kThreads) k_bicg2(Common cm, Coef<T> co, Kry<T> kr) {
   count_launch(cm.ctl);
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -848,8 +850,8 @@ __global__ void __launch_bounds__(kThreads) k_bicg2(Common cm, Coef<T> co, Kry<T
     const T* __restrict__ r = kr.r;
     const T* __restrict__ vv = kr.v[st.pcur];
     const int P = I.pitch;
-    const long long c0 = chunk_start(c, I);
-    const long long c1 = min(c0 + (long long)kChunk, inst_end(I));
+    const long long c0 = chunk_start<CH>(c, I);
+    const long long c1 = min(c0 + (long long)CH, inst_end(I));
     const long long e0 = c0 - P;
     stage_rows<T>(sm, e0, (c1 - c0) + 2LL * P, [&](long long k) {
       Q4<T> x = ld4(r + k);
@@ -861,7 +863,7 @@ __global__ void __launch_bounds__(kThreads) k_bicg2(Common cm, Coef<T> co, Kry<T
     __syncthreads();
     T q[2] = {(T)0, (T)0};
 #pragma unroll 2
-    for (int g = 0; g < kGroups; ++g) {
+    for (int g = 0; g < CH / (4 * kThreads); ++g) {
       const long long K = c0 + 4 * (threadIdx.x + g * kThreads);
       if (K < c1) {
         const long long o = K - e0;
@@ -890,7 +892,7 @@ __global__ void __launch_bounds__(kThreads) k_bicg2(Common cm, Coef<T> co, Kry<T
 
 // k3: x += alpha p + omega s (x starts at 0 on the first iteration of a solve);
 //     r = s - omega t;  partials (r^, r), (r, r); convergence test.
-template <typename T>
+template <typename T, int CH>
 __global__ void __launch_bounds__(kThreads) k_bicg3(Common cm, Kry<T> kr, int max_iters) {
   count_launch(cm.ctl);
   for (int c = blockIdx.x, nc_ = n_chunks(cm); c < nc_; c += gridDim.x) {
@@ -904,8 +906,8 @@ __global__ void __launch_bounds__(kThreads) k_bicg3(Common cm, Kry<T> kr, int ma
     const T* vv = kr.v[st.pcur];
     T q[2] = {(T)0, (T)0};
 #pragma unroll 2
-    for (int g = 0; g < kGroups; ++g) {
-    const Slot s = slot_of(c, I, g);
+    for (int g = 0; g < CH / (4 * kThreads); ++g) {
+    const Slot s = slot_of<CH>(c, I, g);
     if (s.valid) {
       const long long K = s.K;
       const Q4<T> r = ld4(kr.r + K), v = ld4(vv + K), p = ld4(pp + K), t = ld4(kr.t + K);
@@ -955,7 +957,7 @@ __global__ void __launch_bounds__(kThreads) k_bicg3(Common cm, Kry<T> kr, int ma
 // ------------------------------------------------------------------------------ polish + checks
 // y' = R + (I - A~) max(y, 0) >= 0 (R >= 0, fractions >= 0), f = y' / D; partials: sum colsum*f,
 // sum R, clamped count; the chunk minimum of f travels in part slot 3.
-template <typename C, typename A>
+template <typename C, typename A, int CH>
 __global__ void __launch_bounds__(kThreads, 3) k_polish(Common cm, Fields fl, Coef<C> co) {
   using V = typename A::V;
   count_launch(cm.ctl);
@@ -969,8 +971,8 @@ __global__ void __launch_bounds__(kThreads, 3) k_polish(Common cm, Fields fl, Co
     if (!I.enabled) continue;
     const double* y = fl.y64[st.ycur];
     const int P = I.pitch;
-    const long long c0 = chunk_start(c, I);
-    const long long c1 = min(c0 + (long long)kChunk, inst_end(I));
+    const long long c0 = chunk_start<CH>(c, I);
+    const long long c1 = min(c0 + (long long)CH, inst_end(I));
     const long long e0 = c0 - P;
     stage_rows<V>(sm, e0, (c1 - c0) + 2LL * P, [&](long long k) {
       Q4<V> v = A::ld4(y + k);
@@ -983,7 +985,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_polish(Common cm, Fields fl, Co
     float clamp = 0.0f;
     float mn = 3.0e38f;
 #pragma unroll 1
-    for (int g = 0; g < kGroups; ++g) {
+    for (int g = 0; g < CH / (4 * kThreads); ++g) {
       const long long K = c0 + 4 * (threadIdx.x + g * kThreads);
       if (K < c1) {
         const long long o = K - e0;

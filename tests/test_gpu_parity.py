@@ -217,3 +217,28 @@ def test_graph_equals_host_loop(capi, prec):
         assert sg["total_refinements"] == sh["total_refinements"]
     g.close()
     h.close()
+
+
+@pytest.mark.parametrize("prec", [0, 2])
+def test_autotune_restores_state(capi, oracle, prec):
+    """The autotuner runs steps under every launch shape and puts the state back: after it the
+    batch is at step 0 with its initial f, and the tuned launch shape solves to the same accuracy
+    as the oracle (reduction order changes with the chunk size, so not bit for bit)."""
+    probs = cases.batch_problems(6, seed=31, dt=1e-2, lo=20, hi=120)
+    b = capi.Batch(probs, precision=prec)
+    f0 = [b.f(k).copy() for k in range(len(probs))]
+    chunk, grid = b.autotune(2)
+    assert chunk in (1024, 2048, 4096) and grid in (8, 16, 32)
+    log = b.tuning_log()
+    assert len(log) == 9 and all(e["ms_per_step"] > 0 for e in log)
+    assert min(log, key=lambda e: e["ms_per_step"])["chunk"] == chunk
+    for k in range(len(probs)):
+        assert np.array_equal(b.f(k), f0[k])
+        assert b.stats(k)["steps"] == 0
+    b.step(3)
+    tol = TOL64 if prec == 0 else TOL32
+    for k, p in enumerate(probs):
+        f = oracle.step(p, None, 3)
+        assert rel(b.f(k), f) <= tol, (prec, k, rel(b.f(k), f))
+        assert b.f(k).min() >= 0.0
+    b.close()
