@@ -119,6 +119,10 @@ struct F64A {
   __device__ static V rcp(V a) { return 1.0 / a; }
   __device__ static V div(V a, V b) { return a / b; }
   __device__ static V abs(V a) { return fabs(a); }
+  __device__ static V neg(V a) { return -a; }
+  // D (2 f - f_prev): the extrapolated starting point of the solve
+  __device__ static V extrap(V D, V f, V fp) { return D * (f + f - fp); }
+  __device__ static V rsub1(V a) { return 1.0 - a; }
   __device__ static V max0(V a) { return fmax(a, 0.0); }
   __device__ static V k(double c) { return c; }
   __device__ static bool lt0(V a) { return a < 0.0; }
@@ -173,6 +177,11 @@ struct DWA {
   __device__ static V rcp(V a) { return dw_rcp(a); }
   __device__ static V div(V a, V b) { return dw_div(a, b); }
   __device__ static V abs(V a) { return dw_abs(a); }
+  __device__ static V neg(V a) { return dw_neg(a); }
+  // the starting point only steers the iteration (the converged answer does not depend on it),
+  // so 2 f - f_prev is formed in FP32
+  __device__ static V extrap(V D, V f, V fp) { return dw_mul_f(D, fmaf(2.0f, f.hi, -fp.hi)); }
+  __device__ static V rsub1(V a) { return dw_add_f(dw_neg(a), 1.0f); }  // 1 - a (DWPlusFP)
   __device__ static V max0(V a) { return dw_max0(a); }
   __device__ static V k(double c) { return dw_from_double(c); }
   __device__ static bool lt0(V a) { return a.hi < 0.0f; }
@@ -370,10 +379,10 @@ __device__ __forceinline__ void inner_face(typename A::V aK, typename A::V SK, t
   const V absK = A::abs(aK), absL = A::abs(aL);
   const V denom = A::addp(A::addp(absK, absL), A::k(2 * kEps));
   const V muK = A::div(A::addp(absL, A::k(kEps)), denom);
-  const V muL = A::sub(A::k(1.0), muK);
+  const V muL = A::rsub1(muK);
   const V B = A::sub(A::mul(muL, aL), A::mul(muK, aK));
   const V Bp = A::max0(B);             // (|B| + B) / 2
-  const V Bm = A::max0(A::sub(A::k(0.0), B));  // (|B| - B) / 2
+  const V Bm = A::max0(A::neg(B));     // (|B| - B) / 2
   *AK = A::fmap(Bp, invK, A::mul(muK, SK));  // all terms >= 0
   *AL = A::fmap(Bm, invL, A::mul(muL, SL));
 }
@@ -382,7 +391,7 @@ __device__ __forceinline__ void inner_face(typename A::V aK, typename A::V SK, t
 template <typename A>
 __device__ __forceinline__ void dirichlet_face(typename A::V aK, typename A::V SK, typename A::V invK,
                                                typename A::V* Aout, typename A::V* Bm) {
-  *Aout = A::fmap(A::max0(A::sub(A::k(0.0), aK)), invK, SK);
+  *Aout = A::fmap(A::max0(A::neg(aK)), invK, SK);
   *Bm = A::max0(aK);
 }
 
@@ -541,8 +550,7 @@ __global__ void __launch_bounds__(kAsmThreads) k_assemble(Common cm, Geo geo, Fi
       A::st(fl.colsum, K, A::addp(sd, dir));
       // start the solve from the linear extrapolation 2 f^n - f^(n-1) (only the starting point of
       // the iteration; the converged answer does not depend on it)
-      const V g0 = has_prev ? A::sub(A::add(fK, fK), A::ld(fl.fprev, K)) : fK;
-      A::st(fl.y64[cm.st[b].ycur], K, A::mul(D, g0));
+      A::st(fl.y64[cm.st[b].ycur], K, has_prev ? A::extrap(D, fK, A::ld(fl.fprev, K)) : A::mul(D, fK));
       if (wIn) AsmOut<C, A>::put(co, 1, K - 1, A::mul(Aw, inv));  // row K-1, east entry
       if (eIn) AsmOut<C, A>::put(co, 0, K + 1, A::mul(Ae, inv));  // row K+1, west entry
       if (sIn) AsmOut<C, A>::put(co, 3, K - P, A::mul(As, inv));  // row K-P, north entry
