@@ -445,7 +445,7 @@ int sayram_batch_s::place(int b, const sayram_problem& p, long long base, int xe
   return upload_instance(b, p, true, true);
 }
 
-// Work lists of the enabled instances, in slot order: 1024-cell chunks and 32x16 tiles.
+// Work lists of the enabled instances, in slot order: chunks of `chunk` cells and 32x16 tiles.
 int sayram_batch_s::rebuild_lists() {
   h_chunk.clear();
   h_tile.clear();

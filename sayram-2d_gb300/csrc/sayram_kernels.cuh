@@ -15,9 +15,9 @@
 //   column-diagonally-dominant M-matrix), which keeps FP32 storage well scaled and makes the
 //   positivity polish y' = R + (I - A~) max(y, 0) a 1-norm contraction.
 //
-// Reductions are deterministic: every chunk (1024 cells) writes its partial sums, and the last
-// block to finish an instance's chunks (counted with one atomic per chunk) adds them in chunk
-// order and updates that instance's Krylov scalars.  No kernel waits on another block.
+// Reductions are deterministic: every chunk (1024, 2048 or 4096 cells, chosen per batch) writes
+// its partial sums, and the last block to finish an instance's chunks (counted with one atomic
+// per chunk) adds them in chunk order and updates that instance's Krylov scalars.  No kernel waits on another block.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -26,9 +26,7 @@
 
 namespace sg {
 
-constexpr int kChunk = 4096;   // cells per chunk of the streaming kernels
 constexpr int kThreads = 256;  // threads per block of the streaming kernels
-constexpr int kGroups = kChunk / (4 * kThreads);  // 4-cell groups per thread and chunk
 constexpr int kTX = 32;        // assembly tile width (alpha0, contiguous)
 constexpr int kTY = 16;        // assembly tile height (log E)
 constexpr int kAsmThreads = 256;

@@ -564,7 +564,8 @@ __global__ void __launch_bounds__(kAsmThreads) k_assemble(Common cm, Geo geo, Fi
 }
 
 // ------------------------------------------------------------------------------ streaming helpers
-// Locates 4-cell group g (0..kGroups-1) of this thread in chunk c of instance I.
+// Locates 4-cell group g (0 .. CH/(4*kThreads) - 1) of this thread in chunk c (CH cells) of
+// instance I.
 struct Slot {
   long long K;
   bool valid;
