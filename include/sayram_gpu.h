@@ -19,6 +19,10 @@
  *   sayram_set_dirichlet / sayram_set_coeffs
  *       -> the per-step re-reads after eq.update(t) (Solver.cc:286-289: update_Lambda and
  *          fill_vertex_from_bcs), for cases whose coefficients or boundary values change.
+ *   sayram_dtable / sayram_set_dtable / sayram_batch_set_dtable
+ *       -> Albert_Young(_LC)::constructD (source/Cases/Albert_Young.cc:112-134) with locate
+ *          (Albert_Young.cc:94-110), calWeight and interp2D (source/utils.h:24-58): the D fields
+ *          interpolated from the case's HDF5 D table (Albert_Young_IO.cc:17-36), on the device.
  *   sayram_batch_*   -> no counterpart (many independent Solver instances advanced together).
  *   sayram_server_*  -> no counterpart (continuous-batching service of solve requests).
  *
@@ -136,6 +140,23 @@ int sayram_set_coeffs(sayram_solver s, const double* G, const double* Dxx, const
 int sayram_get_stats(sayram_solver s, sayram_stats* out);
 void sayram_destroy(sayram_solver s);
 
+/* A diffusion-coefficient table as the Albert_Young cases read it from D/<dID>.h5
+ * (Albert_Young_IO::read_D): the datasets /alpha0 (degrees), /E, /Daa, /Dap, /Dpp. */
+typedef struct sayram_dtable {
+  int n_alpha, n_energy;          /* nodes along alpha0 and E, both >= 2 */
+  const double* alpha0_deg;       /* n_alpha pitch angles in degrees (/alpha0) */
+  const double* energy;           /* n_energy energies (/E), > 0 */
+  const double *Daa, *Dap, *Dpp;  /* n_alpha x n_energy, row-major (alpha0-major), as stored */
+} sayram_dtable;
+/* Replaces Dxx, Dxy, Dyy by the table interpolated at the cell centres, on the device, as the
+ * reference's constructD does: positions from the axes' end points (uniform in alpha0 and in
+ * log E assumed), bilinear weights, the last node beyond the table's upper ends, then
+ * Dxx = Daa k / p^2, Dxy = Dap k (dlogE/dp) / p, Dyy = Dpp k (dlogE/dp)^2 with k = gME^2 gC^2 *
+ * 86400 and p = e2p(E) at the cell's E. A centre below the table's first node takes the first
+ * node (the reference's own calWeight branch for that case; its size_t conversion there is
+ * undefined). G, 1/tau, f and the boundary values stay. Only the table crosses to the device. */
+int sayram_set_dtable(sayram_solver s, const sayram_dtable* t);
+
 /* ---- batches: many independent instances advanced by the same launches ------------------- */
 typedef struct sayram_batch_s* sayram_batch;
 
@@ -155,6 +176,8 @@ int sayram_batch_set_f(sayram_batch b, int idx, const double* f);
 int sayram_batch_set_dirichlet(sayram_batch b, int idx, int side, const double* v, int n);
 int sayram_batch_set_coeffs(sayram_batch b, int idx, const double* G, const double* Dxx,
                             const double* Dxy, const double* Dyy, const double* inv_tau);
+/* As sayram_set_dtable for instance idx, or for every instance when idx < 0 (one launch). */
+int sayram_batch_set_dtable(sayram_batch b, int idx, const sayram_dtable* t);
 int sayram_batch_stats(sayram_batch b, int idx, sayram_stats* out);
 /* Assembles instance idx's linear system from its current f (without stepping) and returns it
  * in the reference's unscaled form M f = R (the M_ and R_ members of Solver, Solver.h:37-41),
@@ -180,6 +203,11 @@ int sayram_batch_kernel_times(sayram_batch b, const char** names, double* total_
  * fastest. The instances' state is restored afterwards, so tuning does not advance the
  * simulation. Writes the choice if the pointers are not NULL. */
 int sayram_batch_autotune(sayram_batch b, int steps, int* chunk_out, int* blocks_per_sm_out);
+/* Sets the launch shape directly (chunk 1024, 2048 or 4096 cells; 1..64 blocks per SM), or reads
+ * it back. The default is chosen from the batch size; results do not depend on it beyond the
+ * order of the reductions. */
+int sayram_batch_set_launch_shape(sayram_batch b, int chunk, int blocks_per_sm);
+int sayram_batch_get_launch_shape(sayram_batch b, int* chunk, int* blocks_per_sm);
 /* The timings of the last autotune: up to cap (chunk, blocks per SM, ms per step) entries;
  * returns the number of candidates measured. */
 int sayram_batch_tuning_log(sayram_batch b, int* chunks, int* blocks_per_sm, double* ms_per_step, int cap);

@@ -25,11 +25,13 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libppfv_oracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libsayram_ref.so")
+REF_CASE_PATH = os.path.join(HERE, "_ref", "libsayram_case_ref.so")
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _lock = threading.Lock()
 _lib = None
 _ref = None
+_ref_case = None
 
 
 class _OrcProblem(ctypes.Structure):
@@ -41,6 +43,11 @@ class _OrcProblem(ctypes.Structure):
         ("G", _dp), ("Dxx", _dp), ("Dxy", _dp), ("Dyy", _dp), ("inv_tau", _dp),
         ("dir", _dp * 4),
     ]
+
+
+class _OrcDTable(ctypes.Structure):
+    _fields_ = [("na", ctypes.c_int), ("ne", ctypes.c_int), ("alpha0_deg", _dp), ("E", _dp),
+                ("Daa", _dp), ("Dap", _dp), ("Dpp", _dp)]
 
 
 def build(force: bool = False) -> str:
@@ -72,6 +79,9 @@ def lib():
             L.orc_assemble_bound.restype = ctypes.c_int
             L.orc_solve.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]
             L.orc_step.argtypes = [P, _dp, ctypes.c_int]
+            L.orc_dtable_fields.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, ctypes.POINTER(_OrcDTable),
+                                            _dp, _dp, _dp]
+            L.orc_dtable_fields.restype = ctypes.c_int
             for fn in (L.orc_vertex_f, L.orc_face_coeffs, L.orc_assemble, L.orc_solve, L.orc_step):
                 fn.restype = ctypes.c_int
             _lib = L
@@ -234,3 +244,65 @@ def ref_run(prob, nsteps):
     if rc != 0:
         raise RuntimeError("reference run failed: " + L.ref_last_error().decode())
     return M5, R, f
+
+
+# ----------------------------------------------------------------------------- D table
+def _pack_table(t):
+    c = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    keep = [c(t.alpha0_deg), c(t.E), c(t.Daa), c(t.Dap), c(t.Dpp)]
+    s = _OrcDTable(len(keep[0]), len(keep[1]), *[_ptr(a) for a in keep])
+    return s, keep
+
+
+def dtable_fields(x_edges, y_edges, table):
+    """Dxx, Dxy, Dyy (alpha-major) interpolated from a D table at the cell centres, as the
+    Albert_Young cases' constructD does (orc_dtable_fields)."""
+    xe = np.ascontiguousarray(x_edges, dtype=np.float64)
+    ye = np.ascontiguousarray(y_edges, dtype=np.float64)
+    nx, ny = len(xe) - 1, len(ye) - 1
+    s, keep = _pack_table(table)
+    out = [np.empty((nx, ny)) for _ in range(3)]
+    _check(lib().orc_dtable_fields(nx, ny, _ptr(xe), _ptr(ye), ctypes.byref(s), *[_ptr(o) for o in out]),
+           "dtable_fields")
+    return tuple(out)
+
+
+def ref_case_lib():
+    global _ref_case
+    with _lock:
+        if _ref_case is None:
+            if not os.path.exists(REF_CASE_PATH):
+                return None
+            L = ctypes.CDLL(REF_CASE_PATH)
+            L.ref_case.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp, ctypes.c_double,
+                                   ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, _dp, _dp,
+                                   _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
+                                   ctypes.POINTER(ctypes.c_int), _dp]
+            L.ref_case.restype = ctypes.c_int
+            L.ref_case_last_error.restype = ctypes.c_char_p
+            _ref_case = L
+    return _ref_case
+
+
+def ref_case(which, x_edges, y_edges, dt, Emin, Emax, table):
+    """Runs the reference's own Albert_Young (which=0) or Albert_Young_LC (1) case on the grid and
+    D table (oracle/_ref). Returns G, Dxx, Dxy, Dyy, inv_tau, f0 (alpha-major), bc[4] and the
+    Dirichlet vertex values per side (None for zero-flux sides)."""
+    L = ref_case_lib()
+    if L is None:
+        raise RuntimeError("reference case build not available (make -C oracle ref)")
+    xe = np.ascontiguousarray(x_edges, dtype=np.float64)
+    ye = np.ascontiguousarray(y_edges, dtype=np.float64)
+    nx, ny = len(xe) - 1, len(ye) - 1
+    s, keep = _pack_table(table)
+    out = {k: np.empty((nx, ny)) for k in ("G", "Dxx", "Dxy", "Dyy", "inv_tau", "f0")}
+    bc = (ctypes.c_int * 4)()
+    dirv = np.zeros(2 * (ny + 1) + 2 * (nx + 1))
+    rc = L.ref_case(int(which), nx, ny, _ptr(xe), _ptr(ye), float(dt), float(Emin), float(Emax), s.na, s.ne,
+                    s.alpha0_deg, s.E, s.Daa, s.Dap, s.Dpp, *[_ptr(out[k]) for k in out], bc, _ptr(dirv))
+    if rc != 0:
+        raise RuntimeError("reference case failed: " + L.ref_case_last_error().decode())
+    out["bc"] = [int(b) for b in bc]
+    offs = np.cumsum([0, ny + 1, ny + 1, nx + 1, nx + 1])
+    out["dirichlet"] = [dirv[offs[k]:offs[k + 1]].copy() if out["bc"][k] == 0 else None for k in range(4)]
+    return out

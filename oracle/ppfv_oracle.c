@@ -448,3 +448,84 @@ int orc_step(const orc_problem* p, double* f, int nsteps) {
   free(M5); free(R); free(x);
   return rc;
 }
+
+/* ---------------------------------------------------------------------------- D table
+ * The Albert_Young cases build Dxx, Dxy, Dyy by bilinear interpolation in a table read from
+ * HDF5 (Albert_Young_IO::read_D, Albert_Young_IO.cc:17-36), then convert the units:
+ *   locate      Albert_Young.cc:94-110   position in a table assumed uniform in alpha0 and in
+ *                                        log E, from the end points only
+ *   calWeight   utils.h:44-58            weight of the lower node; beyond the last node the
+ *                                        last node is used with weight 1
+ *   interp2D    utils.h:24-41
+ *   constructD  Albert_Young.cc:112-134  (the same in Albert_Young_LC.cc)
+ *   e2p, dlogE_dp  utils.h:12-20;  gE0, gME, gC, gPI: common.h:38-43
+ * The table's alpha0 axis is in degrees, as in the file (read_D converts it with * gPI / 180).
+ * A position below the first node makes the reference convert a negative floor() to size_t,
+ * which C++ leaves undefined; calWeight's own `i < 0` branch (first node, weight 1) states the
+ * intent, and that is what is done here. */
+typedef struct {
+  int na, ne;                      /* nodes along alpha0 and E (both >= 2) */
+  const double* alpha0_deg;        /* na: /alpha0 (degrees) */
+  const double* E;                 /* ne: /E */
+  const double *Daa, *Dap, *Dpp;   /* (na, ne) row-major: /Daa, /Dap, /Dpp */
+} orc_dtable;
+
+#define ORC_PI 3.141592653589793238462 /* gPI */
+#define ORC_C 1.0                      /* gC */
+#define ORC_E0 0.511875                /* gE0, MeV */
+
+static double orc_e2p(double E, double E0) { return sqrt(E * (E + 2 * E0)) / ORC_C; }
+static double orc_dlogE_dp(double logE, double E0) {
+  const double E = exp(logE);
+  return orc_e2p(E, ORC_E0) * ORC_C * ORC_C / (E * (E + E0));
+}
+
+static void orc_calweight(long* i, double* w, long n, double pos) {
+  if (pos < 0.0) { /* see the note above */
+    *i = 0;
+    *w = 1.0;
+  } else if (*i < n) {
+    *w = 1.0 - (pos - (double)*i);
+  } else {
+    *i = n - 1;
+    *w = 0.0;
+  }
+}
+
+/* (nx, ny) alpha-major Dxx, Dxy, Dyy at the cell centres of the grid given by its edges. */
+int orc_dtable_fields(int nx, int ny, const double* xe, const double* ye, const orc_dtable* t, double* Dxx,
+                      double* Dxy, double* Dyy) {
+  if (nx < 1 || ny < 1 || !t || t->na < 2 || t->ne < 2) return -1;
+  const double xmin = t->alpha0_deg[0] * ORC_PI / 180, xmax = t->alpha0_deg[t->na - 1] * ORC_PI / 180;
+  const double lymin = log(t->E[0]), lymax = log(t->E[t->ne - 1]);
+  const double gme = ORC_E0 / (ORC_C * ORC_C);
+  const double denorm = gme * gme * ORC_C * ORC_C;
+  const double s2d = 3600 * 24;
+  const long na1 = t->na - 1, ne1 = t->ne - 1;
+  for (int i = 0; i < nx; ++i) {
+    const double alpha0 = 0.5 * (xe[i] + xe[i + 1]);
+    for (int j = 0; j < ny; ++j) {
+      const double logE = 0.5 * (ye[j] + ye[j + 1]);
+      const double p = orc_e2p(exp(logE), ORC_E0);
+      const double px = (alpha0 - xmin) / (xmax - xmin) * (double)na1;
+      const double py = (logE - lymin) / (lymax - lymin) * (double)ne1;
+      long i0 = px >= 0.0 ? (long)floor(px) : 0, j0 = py >= 0.0 ? (long)floor(py) : 0;
+      double wi, wj;
+      orc_calweight(&i0, &wi, na1, px);
+      orc_calweight(&j0, &wj, ne1, py);
+      const double* raw[3] = {t->Daa, t->Dap, t->Dpp};
+      double v[3];
+      for (int k = 0; k < 3; ++k) {
+        const double* r = raw[k];
+        const long e = t->ne;
+        v[k] = r[i0 * e + j0] * wi * wj + r[(i0 + 1) * e + j0] * (1 - wi) * wj +
+               r[(i0 + 1) * e + j0 + 1] * (1 - wi) * (1 - wj) + r[i0 * e + j0 + 1] * wi * (1 - wj);
+      }
+      const long c = (long)i * ny + j;
+      Dxx[c] = v[0] * denorm * s2d / (p * p);
+      Dxy[c] = v[1] * denorm * s2d * orc_dlogE_dp(logE, ORC_E0) / p;
+      Dyy[c] = v[2] * denorm * s2d * pow(orc_dlogE_dp(logE, ORC_E0), 2);
+    }
+  }
+  return 0;
+}

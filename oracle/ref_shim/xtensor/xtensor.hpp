@@ -1,5 +1,6 @@
 // TEST INFRASTRUCTURE: a project-written stand-in for the xtensor containers that Sayram-2D's
-// Solver/Mesh/Equation headers use (row-major 2-D storage, resize(shape), operator()(i,j), fill).
+// Solver/Mesh/Equation headers and its Albert_Young cases use (row-major 2-D storage,
+// resize(shape), operator()(i,j), fill; a 1-D array with size(), [] and element-wise scaling).
 #pragma once
 #include <array>
 #include <cstddef>
@@ -34,6 +35,21 @@ struct xtensor {
 template <typename T>
 struct xarray {
   std::vector<T> data_;
+  std::size_t size() const { return data_.size(); }
+  T& operator[](std::size_t i) { return data_[i]; }
+  const T& operator[](std::size_t i) const { return data_[i]; }
 };
+
+// element-wise a * s and a / s, each element rounded once (as xtensor evaluates them)
+inline xarray<double> operator*(const xarray<double>& a, double s) {
+  xarray<double> r = a;
+  for (auto& x : r.data_) x = x * s;
+  return r;
+}
+inline xarray<double> operator/(const xarray<double>& a, double s) {
+  xarray<double> r = a;
+  for (auto& x : r.data_) x = x / s;
+  return r;
+}
 
 }  // namespace xt

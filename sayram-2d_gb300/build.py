@@ -11,7 +11,7 @@ CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT_DIR, "libsayram_gpu.so")
 SOURCES = ["sayram_engine.cu"]
-DEPS = ["sayram_kernels.cuh", "sayram_ops.cuh"]
+DEPS = ["sayram_kernels.cuh", "sayram_ops.cuh", "dword.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -36,7 +36,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     tmp = LIB + ".tmp"
-    cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
+    # host code: no fused multiply-adds, so host-side values (grid weights, D-table row factors)
+    # are the same separately rounded operations on x86-64 and aarch64
+    cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-shared",
            "-I", os.path.join(ROOT, "include"), "-o", tmp] + [os.path.join(CSRC, s) for s in SOURCES]
     if verbose:
         print(" ".join(cmd))

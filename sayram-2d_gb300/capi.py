@@ -57,6 +57,11 @@ class sayram_stats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class sayram_dtable(ctypes.Structure):
+    _fields_ = [("n_alpha", ctypes.c_int), ("n_energy", ctypes.c_int), ("alpha0_deg", _dp), ("energy", _dp),
+                ("Daa", _dp), ("Dap", _dp), ("Dpp", _dp)]
+
+
 class sayram_server_config(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_double), ("max_slots", ctypes.c_int), ("max_side", ctypes.c_int)]
 
@@ -109,6 +114,10 @@ SIGNATURES = {
     "sayram_batch_enable_timing": (ctypes.c_int, [_P, ctypes.c_int]),
     "sayram_batch_kernel_times": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_char_p), _dp, ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
     "sayram_batch_autotune": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
+    "sayram_batch_set_dtable": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(sayram_dtable)]),
+    "sayram_set_dtable": (ctypes.c_int, [_P, ctypes.POINTER(sayram_dtable)]),
+    "sayram_batch_set_launch_shape": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),
+    "sayram_batch_get_launch_shape": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
     "sayram_batch_tuning_log": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), _dp, ctypes.c_int]),
     "sayram_batch_launches": (ctypes.c_longlong, [_P]),
     "sayram_batch_destroy": (None, [_P]),
@@ -304,6 +313,24 @@ class Batch:
         check(self._L.sayram_batch_autotune(self.h, int(steps), ctypes.byref(ch), ctypes.byref(gm)), "sayram_batch_autotune")
         return ch.value, gm.value
 
+    def set_dtable(self, idx: int, table) -> None:
+        """D fields of instance idx (every instance if idx < 0) interpolated on the device from a
+        table with fields alpha0_deg, E, Daa, Dap, Dpp (cases.DTable), as constructD does."""
+        keep = [_f64(table.alpha0_deg), _f64(table.E), _f64(table.Daa), _f64(table.Dap), _f64(table.Dpp)]
+        na, ne = len(keep[0]), len(keep[1])
+        if any(a.shape != (na, ne) for a in keep[2:]):
+            raise ValueError("Daa, Dap, Dpp must have shape (len(alpha0_deg), len(E))")
+        t = sayram_dtable(na, ne, *[_ptr(a) for a in keep])
+        check(self._L.sayram_batch_set_dtable(self.h, int(idx), ctypes.byref(t)), "sayram_batch_set_dtable")
+
+    def set_launch_shape(self, chunk: int, blocks_per_sm: int) -> None:
+        check(self._L.sayram_batch_set_launch_shape(self.h, int(chunk), int(blocks_per_sm)), "sayram_batch_set_launch_shape")
+
+    def launch_shape(self):
+        ch, gm = ctypes.c_int(), ctypes.c_int()
+        check(self._L.sayram_batch_get_launch_shape(self.h, ctypes.byref(ch), ctypes.byref(gm)), "sayram_batch_get_launch_shape")
+        return ch.value, gm.value
+
     def tuning_log(self):
         cap = 32
         c, g, m = (ctypes.c_int * cap)(), (ctypes.c_int * cap)(), (ctypes.c_double * cap)()
@@ -338,6 +365,9 @@ class Solver(Batch):
 
     def set_coeffs(self, G, Dxx, Dxy, Dyy, inv_tau) -> None:
         super().set_coeffs(0, G, Dxx, Dxy, Dyy, inv_tau)
+
+    def set_dtable(self, table, idx: int = 0) -> None:  # constructD on the device
+        super().set_dtable(idx, table)
 
     def get_stats(self) -> dict:
         return self.stats(0)

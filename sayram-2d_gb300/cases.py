@@ -196,9 +196,11 @@ def synthetic_problem(
 
 
 def albert_young_problem(nalpha: int, nE: int, dt: float, seed: int = 0, rho: float = 0.5,
-                         alpha0_min_deg: float = 5.0, Emin: float = 0.2, Emax: float = 5.0) -> Problem:
-    """Albert_Young's G, f0 and BCs (Albert_Young.h:37-62, Albert_Young.cc:42-92); the D table
-    (read from HDF5 in the reference) is replaced by seeded synthetic fields."""
+                         alpha0_min_deg: float = 5.0, Emin: float = 0.2, Emax: float = 5.0,
+                         D=None) -> Problem:
+    """Albert_Young's G, f0 and BCs (Albert_Young.h:37-62, Albert_Young.cc:42-92). D is
+    (Dxx, Dxy, Dyy) at the cell centres if given (for example interpolated from a
+    :class:`DTable`); otherwise seeded synthetic fields stand in for the HDF5 table."""
     rng = np.random.default_rng(seed)
     xe = uniform_edges(nalpha, alpha0_min_deg * PI / 180, 90.0 * PI / 180)
     ye = uniform_edges(nE, math.log(Emin), math.log(Emax))
@@ -208,7 +210,7 @@ def albert_young_problem(nalpha: int, nE: int, dt: float, seed: int = 0, rho: fl
         p = e2p(np.exp(logE))
         return np.exp(-(np.exp(logE) - 0.2) / 0.1) * (np.sin(a) - np.sin(5 * PI / 180)) / (p * p) + EPS
 
-    Dxx, Dxy, Dyy = synthetic_D(rng, A, Y, rho)
+    Dxx, Dxy, Dyy = synthetic_D(rng, A, Y, rho) if D is None else (np.asarray(d, dtype=np.float64) for d in D)
     dirichlet = [np.zeros(nE + 1), None, init_f(xe, math.log(Emin)), np.zeros(nalpha + 1)]
     prob = Problem(nalpha, nE, xe, ye, float(dt), [DIRICHLET, ZEROFLUX, DIRICHLET, DIRICHLET],
                    _ay_G(A, Y), Dxx, Dxy, Dyy, np.zeros((nalpha, nE)), init_f(A, Y), dirichlet,
@@ -226,9 +228,10 @@ def bounce_period(a0, p, L):
 
 
 def albert_young_lc_problem(nalpha: int, nE: int, dt: float, seed: int = 0, rho: float = 0.5,
-                            Emin: float = 0.2, Emax: float = 5.0) -> Problem:
+                            Emin: float = 0.2, Emax: float = 5.0, D=None) -> Problem:
     """The loss-cone case (Albert_Young_LC.{h,cc}): alpha0 from 0 deg, zero flux at both alpha0
-    sides, inv_tau = 4/bounce period inside the loss cone (L = 4.5), Dirichlet in E; seeded D."""
+    sides, inv_tau = 4/bounce period inside the loss cone (L = 4.5), Dirichlet in E; D as in
+    :func:`albert_young_problem`."""
     rng = np.random.default_rng(seed)
     xe = uniform_edges(nalpha, 0.0, 90.0 * PI / 180)
     ye = uniform_edges(nE, math.log(Emin), math.log(Emax))
@@ -242,13 +245,44 @@ def albert_young_lc_problem(nalpha: int, nE: int, dt: float, seed: int = 0, rho:
     alpha0lc = math.asin((L ** 5 * (4 * L - 3)) ** -0.25)
     p = e2p(np.exp(Y))
     inv_tau = np.where(A < alpha0lc, 4.0 / bounce_period(A, p, L), 0.0)
-    Dxx, Dxy, Dyy = synthetic_D(rng, A, Y, rho)
+    Dxx, Dxy, Dyy = synthetic_D(rng, A, Y, rho) if D is None else (np.asarray(d, dtype=np.float64) for d in D)
     dirichlet = [None, None, init_f(xe, math.log(Emin)), np.zeros(nalpha + 1)]
     prob = Problem(nalpha, nE, xe, ye, float(dt), [ZEROFLUX, ZEROFLUX, DIRICHLET, DIRICHLET],
                    _ay_G(A, Y), Dxx, Dxy, Dyy, inv_tau, init_f(A, Y), dirichlet,
                    name=f"albert-young-lc-{nalpha}x{nE}")
     prob.validate()
     return prob
+
+
+@dataclasses.dataclass
+class DTable:
+    """A diffusion-coefficient table as the Albert_Young cases read it from D/<dID>.h5
+    (Albert_Young_IO.cc:17-36): /alpha0 in degrees, /E, and /Daa, /Dap, /Dpp of shape
+    (len(alpha0), len(E)). The cases interpolate it bilinearly in alpha0 and log E, assuming both
+    axes uniform (only the end points are used, Albert_Young.cc:94-110)."""
+
+    alpha0_deg: np.ndarray
+    E: np.ndarray
+    Daa: np.ndarray
+    Dap: np.ndarray
+    Dpp: np.ndarray
+
+
+def synthetic_dtable(seed: int, n_alpha: int = 46, n_E: int = 31, alpha0_max_deg: float = 90.0,
+                     Emin: float = 0.1, Emax: float = 10.0, rho: float = 0.6) -> DTable:
+    """Seeded stand-in for an Albert-Young D file: smooth positive Daa, Dpp whose converted
+    values (x 22643/p^2 etc.) land near 1e-6..1e-2 per day, and Dap = rho' sqrt(Daa Dpp) with a
+    smooth |rho'| <= |rho| < 1, so every interpolated D stays positive definite."""
+    rng = np.random.default_rng([seed, 91])
+    a = np.linspace(0.0, alpha0_max_deg, n_alpha)
+    E = np.exp(np.linspace(math.log(Emin), math.log(Emax), n_E))
+    A, LE = np.meshgrid(a * PI / 180, np.log(E), indexing="ij")
+    xi = A / max(A.max(), 1e-300)
+    eta = (LE - LE.min()) / max(LE.max() - LE.min(), 1e-300)
+    Daa = 10.0 ** (-9.0 + 3.0 * _smooth_field(rng, xi, eta)) * (0.05 + np.sin(A))
+    Dpp = 10.0 ** (-9.5 + 3.0 * _smooth_field(rng, xi, eta)) * (0.05 + np.sin(A))
+    Dap = rho * (0.5 + 0.5 * _smooth_field(rng, xi, eta)) * np.sqrt(Daa * Dpp)
+    return DTable(a, E, Daa, Dap, Dpp)
 
 
 def stretched_edges(n: int, lo: float, hi: float, a: float) -> np.ndarray:

@@ -73,6 +73,10 @@ struct sayram_batch_s {
   double *d_xe = nullptr, *d_ye = nullptr, *d_wx = nullptr, *d_wy = nullptr, *d_dirv = nullptr;
   double* d_part = nullptr;
   double* d_stage = nullptr;   // 6 * max instance cells (setup) / packed field (get/set)
+  long long ycap_ = 0;         // y-edge table length
+  double* d_tab = nullptr;     // D table (3 * n_alpha * n_energy), grown on demand
+  long long tab_cap = 0;
+  double* d_rows = nullptr;    // D-table row factors p, dlogE/dp, its square (3 * ycap_)
   long long stage_cells = 0;
   sg::Geo geo{};
   sg::Fields fl{};
@@ -105,6 +109,10 @@ struct sayram_batch_s {
     graph = nullptr;
     for (void* p : allocs) cudaFree(p);
     allocs.clear();
+    if (d_tab) cudaFree(d_tab);
+    if (d_rows) cudaFree(d_rows);
+    d_tab = d_rows = nullptr;
+    tab_cap = 0;
     if (h_ctl) cudaFreeHost(h_ctl);
     h_ctl = nullptr;
     for (auto e : evpool) cudaEventDestroy(e);
@@ -217,6 +225,7 @@ struct sayram_batch_s {
     graph = nullptr;
   }
   int autotune(int steps, int* best_chunk, int* best_grid);
+  int set_dtable(int idx, const sayram_dtable* t);
   struct Tuned {
     int chunk, gmult;
     double ms_per_step;
@@ -327,13 +336,14 @@ int sayram_batch_s::alloc_storage(long long cells, int slots, int chunks_cap, in
   SG_ALLOC(d_tile, tiles_cap);
   SG_ALLOC(d_xe, xcap);
   SG_ALLOC(d_ye, ycap);
+  ycap_ = ycap;
   SG_ALLOC(d_wx, 2 * xcap);
   SG_ALLOC(d_wy, 2 * ycap);
   SG_ALLOC(d_dirv, std::max<long long>(dcap, 1));
   SG_ALLOC(d_part, 4LL * chunks_cap);
   SG_ALLOC(d_stage, stage_cap);
   cell_arrays.clear();
-  double** geos[8] = {&geo.aAx, &geo.aBx, &geo.Sx, &geo.aAy, &geo.aBy, &geo.Sy, &geo.ukk, &geo.sdiag};
+  double** geos[9] = {&geo.aAx, &geo.aBx, &geo.Sx, &geo.aAy, &geo.aBy, &geo.Sy, &geo.ukk, &geo.sdiag, &geo.G};
   for (auto g : geos) {
     SG_ALLOC(*g, cells);
     cell_arrays.push_back({*g, 8});
@@ -694,6 +704,101 @@ int sayram_batch_s::launch_steps(int nsteps) {
   return SAYRAM_OK;
 }
 
+namespace {
+// Albert_Young's unit conversion (utils.h:12-20, common.h:41-43), host libm: the device kernel
+// reads these per-row values so that its arithmetic is a fixed sequence of IEEE operations.
+constexpr double kC = 1.0;          // gC
+constexpr double kE0 = 0.511875;    // gE0 [MeV]
+constexpr double kPi = 3.141592653589793238462;  // gPI
+double host_e2p(double E, double E0) { return std::sqrt(E * (E + 2 * E0)) / kC; }
+double host_dlogE_dp(double logE, double E0) {
+  const double E = std::exp(logE);
+  return host_e2p(E, kE0) * kC * kC / (E * (E + E0));
+}
+}  // namespace
+
+// Interpolates Dxx, Dxy, Dyy from a D table at every cell centre of instance idx (all instances
+// when idx < 0), as Albert_Young(_LC)::constructD does, and re-derives the face factors from them
+// and the stored G. The step graph reads the factors from memory, so it stays valid.
+int sayram_batch_s::set_dtable(int idx, const sayram_dtable* t) {
+  if (!t || t->n_alpha < 2 || t->n_energy < 2 || !t->alpha0_deg || !t->energy || !t->Daa || !t->Dap || !t->Dpp)
+    return fail(SAYRAM_ERR_ARG, "D table: needs n_alpha, n_energy >= 2 and all five arrays");
+  if (idx >= n) return fail(SAYRAM_ERR_ARG, "instance index out of range");
+  if (idx >= 0 && !hinst[idx].enabled) return fail(SAYRAM_ERR_STATE, "instance slot is empty");
+  const int na = t->n_alpha, ne = t->n_energy;
+  const double a0 = t->alpha0_deg[0], a1 = t->alpha0_deg[na - 1];
+  const double e0 = t->energy[0], e1 = t->energy[ne - 1];
+  if (!(a1 > a0) || !(e0 > 0.0) || !(e1 > e0) || !std::isfinite(a0) || !std::isfinite(a1) || !std::isfinite(e1))
+    return fail(SAYRAM_ERR_ARG, "D table: alpha0 and energy axes must increase from end to end, energies > 0");
+  SG_CUDA(cudaSetDevice(dev));
+  SG_CUDA(cudaStreamSynchronize(stream));
+  const long long nt = 3LL * na * ne;
+  if (nt > tab_cap) {
+    double* q = nullptr;
+    if (cudaMalloc(&q, sizeof(double) * nt) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(SAYRAM_ERR_OOM, "D table: no device memory for the table");
+    }
+    if (d_tab) cudaFree(d_tab);
+    d_tab = q;
+    tab_cap = nt;
+  }
+  if (!d_rows) {
+    if (cudaMalloc(&d_rows, sizeof(double) * 3 * std::max<long long>(ycap_, 1)) != cudaSuccess) {
+      cudaGetLastError();
+      d_rows = nullptr;
+      return fail(SAYRAM_ERR_OOM, "D table: no device memory for the row factors");
+    }
+  }
+  const size_t tb = sizeof(double) * (size_t)na * ne;
+  SG_CUDA(cudaMemcpyAsync(d_tab, t->Daa, tb, cudaMemcpyHostToDevice, stream));
+  SG_CUDA(cudaMemcpyAsync(d_tab + (long long)na * ne, t->Dap, tb, cudaMemcpyHostToDevice, stream));
+  SG_CUDA(cudaMemcpyAsync(d_tab + 2LL * na * ne, t->Dpp, tb, cudaMemcpyHostToDevice, stream));
+  // row factors of the selected instances, from their y edges
+  std::vector<double> ye(ycap_), rows(3 * ycap_, 0.0);
+  SG_CUDA(cudaMemcpyAsync(ye.data(), d_ye, sizeof(double) * ycap_, cudaMemcpyDeviceToHost, stream));
+  SG_CUDA(cudaStreamSynchronize(stream));
+  for (int b = (idx < 0 ? 0 : idx); b < (idx < 0 ? n : idx + 1); ++b) {
+    const InstDev& I = hinst[b];
+    if (!I.enabled) continue;
+    for (int j = 0; j < I.ny; ++j) {
+      const double logE = 0.5 * (ye[I.ye + j] + ye[I.ye + j + 1]);
+      const double dl = host_dlogE_dp(logE, kE0);
+      rows[I.ye + j] = host_e2p(std::exp(logE), kE0);
+      rows[ycap_ + I.ye + j] = dl;
+      rows[2 * ycap_ + I.ye + j] = std::pow(dl, 2);
+    }
+  }
+  SG_CUDA(cudaMemcpyAsync(d_rows, rows.data(), sizeof(double) * rows.size(), cudaMemcpyHostToDevice, stream));
+  sg::DTab dt{};
+  dt.na = na;
+  dt.ne = ne;
+  dt.xmin = a0 * kPi / 180;
+  dt.xmax = a1 * kPi / 180;
+  dt.lymin = std::log(e0);
+  dt.lymax = std::log(e1);
+  const double gme = kE0 / (kC * kC);
+  dt.denorm = gme * gme * kC * kC;
+  dt.Daa = d_tab;
+  dt.Dap = d_tab + (long long)na * ne;
+  dt.Dpp = d_tab + 2LL * na * ne;
+  dt.rp = d_rows;
+  dt.rdl = d_rows + ycap_;
+  dt.rdl2 = d_rows + 2 * ycap_;
+  const int t0 = idx < 0 ? 0 : hinst[idx].tile0;
+  const int t1 = idx < 0 ? ntiles : hinst[idx].tile0 + hinst[idx].ntx * hinst[idx].nty;
+  if (t1 > t0) {
+    const int blocks = std::min(t1 - t0, nsm * 8);
+    if (dwm)
+      sg::k_dtable<sg::DWA><<<blocks, 256, 0, stream>>>(cm, geo, dt, d_xe, d_ye, t0, t1);
+    else
+      sg::k_dtable<sg::F64A><<<blocks, 256, 0, stream>>>(cm, geo, dt, d_xe, d_ye, t0, t1);
+    SG_CUDA(cudaGetLastError());
+  }
+  SG_CUDA(cudaStreamSynchronize(stream));
+  return SAYRAM_OK;
+}
+
 // Times `steps` steps of every launch shape (cells per chunk x blocks per SM) from the same
 // state and keeps the fastest; f, the previous f and the per-instance state are restored
 // afterwards, so tuning does not advance the simulation.
@@ -1047,6 +1152,32 @@ int sayram_batch_autotune(sayram_batch b, int steps, int* chunk_out, int* blocks
   return b->autotune(steps, chunk_out, blocks_per_sm_out);
 }
 
+int sayram_batch_set_dtable(sayram_batch b, int idx, const sayram_dtable* t) {
+  if (!b) return fail(SAYRAM_ERR_ARG, "null handle");
+  return b->set_dtable(idx, t);
+}
+
+int sayram_set_dtable(sayram_solver s, const sayram_dtable* t) { return sayram_batch_set_dtable(s, 0, t); }
+
+int sayram_batch_set_launch_shape(sayram_batch b, int chunk, int blocks_per_sm) {
+  if (!b) return fail(SAYRAM_ERR_ARG, "null handle");
+  if (chunk != 1024 && chunk != 2048 && chunk != 4096) return fail(SAYRAM_ERR_ARG, "chunk must be 1024, 2048 or 4096");
+  if (blocks_per_sm < 1 || blocks_per_sm > 64) return fail(SAYRAM_ERR_ARG, "blocks_per_sm must be in [1, 64]");
+  SG_CUDA(cudaSetDevice(b->dev));
+  SG_CUDA(cudaStreamSynchronize(b->stream));
+  b->chunk = chunk;
+  b->gmult = blocks_per_sm;
+  b->drop_graph();
+  return b->rebuild_lists();
+}
+
+int sayram_batch_get_launch_shape(sayram_batch b, int* chunk, int* blocks_per_sm) {
+  if (!b) return fail(SAYRAM_ERR_ARG, "null handle");
+  if (chunk) *chunk = b->chunk;
+  if (blocks_per_sm) *blocks_per_sm = b->gmult;
+  return SAYRAM_OK;
+}
+
 int sayram_batch_tuning_log(sayram_batch b, int* chunks, int* blocks_per_sm, double* ms_per_step, int cap) {
   if (!b) return fail(SAYRAM_ERR_ARG, "null handle");
   const int m = (int)b->tune_log.size();
@@ -1072,7 +1203,7 @@ void sayram_batch_destroy(sayram_batch b) { delete b; }
 size_t sayram_instance_bytes(int nx, int ny, int precision) {
   const long long pitch = round_up(nx, 4);
   const long long cells = round_up((long long)(ny + 2) * pitch, 32);
-  const long long per = 15 * 8 + (precision != SAYRAM_FP64 ? 8 * 4 + 8 * 4 : 4 * 8 + 8 * 8) + 8;
+  const long long per = 16 * 8 + (precision != SAYRAM_FP64 ? 8 * 4 + 8 * 4 : 4 * 8 + 8 * 8) + 8;
   return (size_t)(cells * per + 4096);
 }
 

@@ -1,6 +1,7 @@
 // sayram_ops.cuh -- the kernels of one backward-Euler step (see sayram_kernels.cuh for layout).
 //
 //   k_setup      once per instance: coefficients -> per-cell face factors, UKK, loss diagonal
+//   k_dtable     on demand: D fields interpolated from a D table -> the face factors again
 //   k_begin      per step: resets the per-instance solver state
 //   k_assemble   fused vertex interpolation + PPFV face fluxes + diagonal/RHS + Jacobi scaling
 //   k_resid      outer residual r = R - A~ y (adds the last Krylov correction first)
@@ -23,6 +24,7 @@ namespace sg {
 // ------------------------------------------------------------------------------ arguments
 struct Geo {  // per-cell face factors (time independent while the coefficients are)
   double *aAx, *aBx, *Sx, *aAy, *aBy, *Sy, *ukk, *sdiag;
+  double* G;  // G per cell, FP64 (kept so that new D fields can re-derive the face factors)
 };
 
 struct Common {
@@ -246,6 +248,24 @@ __device__ __forceinline__ void face_pair(double Kx, double Ky, double Ax, doubl
                   __dadd_rn(__dmul_rn(vkb0, rvka0), __dmul_rn(vkb1, rvka1)));
 }
 
+// Face factors of cell K from G and D (Solver::update_Lambda, Solver.cc:57-65, then the general
+// a_sigma formula on the XNEG and YNEG edges), stored in the policy's wide format.
+template <typename A>
+__device__ __forceinline__ void setup_faces(const Geo& geo, long long K, double xl, double xr, double yb,
+                                            double yt, double g, double dxx, double dxy, double dyy) {
+  const double Kx = __dmul_rn(0.5, __dadd_rn(xl, xr)), Ky = __dmul_rn(0.5, __dadd_rn(yb, yt));
+  const double L[4] = {__dmul_rn(dxx, g), __dmul_rn(dxy, g), __dmul_rn(dxy, g), __dmul_rn(dyy, g)};
+  double aa, ab;
+  face_pair(Kx, Ky, xl, yt, xl, yb, -1.0, 0.0, L, &aa, &ab);  // XNEG: A=(i,j+1) B=(i,j)
+  A::st(geo.aAx, K, A::from_d(aa));
+  A::st(geo.aBx, K, A::from_d(ab));
+  A::st(geo.Sx, K, A::from_d(__dadd_rn(aa, ab)));
+  face_pair(Kx, Ky, xl, yb, xr, yb, 0.0, -1.0, L, &aa, &ab);  // YNEG: A=(i,j) B=(i+1,j)
+  A::st(geo.aAy, K, A::from_d(aa));
+  A::st(geo.aBy, K, A::from_d(ab));
+  A::st(geo.Sy, K, A::from_d(__dadd_rn(aa, ab)));
+}
+
 // One instance: stage holds alpha-major G, Dxx, Dxy, Dyy, inv_tau, f0 (each nx*ny). mask bits
 // 0-4 select the coefficient sections (all five together), bit 5 the initial state. Values are
 // computed in FP64 and stored in the policy's wide format.
@@ -268,25 +288,91 @@ __global__ void k_setup(Common cm, Geo geo, double* f, const double* stage, cons
       const double xl = xe[I.xe + i], xr = xe[I.xe + i + 1];
       const double yb = ye[I.ye + j], yt = ye[I.ye + j + 1];
       const double dx = __dadd_rn(xr, -xl), dy = __dadd_rn(yt, -yb);
-      const double Kx = __dmul_rn(0.5, __dadd_rn(xl, xr)), Ky = __dmul_rn(0.5, __dadd_rn(yb, yt));
       const double g = G[c];
-      const double L[4] = {__dmul_rn(Dxx[c], g), __dmul_rn(Dxy[c], g), __dmul_rn(Dxy[c], g),
-                           __dmul_rn(Dyy[c], g)};
-      double aa, ab;
-      face_pair(Kx, Ky, xl, yt, xl, yb, -1.0, 0.0, L, &aa, &ab);  // XNEG: A=(i,j+1) B=(i,j)
-      A::st(geo.aAx, K, A::from_d(aa));
-      A::st(geo.aBx, K, A::from_d(ab));
-      A::st(geo.Sx, K, A::from_d(__dadd_rn(aa, ab)));
-      face_pair(Kx, Ky, xl, yb, xr, yb, 0.0, -1.0, L, &aa, &ab);  // YNEG: A=(i,j) B=(i+1,j)
-      A::st(geo.aAy, K, A::from_d(aa));
-      A::st(geo.aBy, K, A::from_d(ab));
-      A::st(geo.Sy, K, A::from_d(__dadd_rn(aa, ab)));
+      setup_faces<A>(geo, K, xl, xr, yb, yt, g, Dxx[c], Dxy[c], Dyy[c]);
+      if (geo.G) geo.G[K] = g;
       // UKK = G * (dx*dy/dt); diagonal UKK*(1 + dt/tau) (Solver.cc:190-199, Mesh.h:61-63)
       const double ukk = __dmul_rn(g, __ddiv_rn(__dmul_rn(dx, dy), I.dt));
       A::st(geo.ukk, K, A::from_d(ukk));
       A::st(geo.sdiag, K, A::from_d(__dmul_rn(ukk, __dadd_rn(1.0, __dmul_rn(I.dt, itau[c])))));
     }
     if (mask & 32) A::st(f, K, A::from_d(f0[c]));
+  }
+}
+
+// A diffusion-coefficient table on the device and the host-side values it is read with (see
+// k_dtable). Row factors are per E row of each instance, at the instance's y-edge offset.
+struct DTab {
+  int na, ne;
+  double xmin, xmax;      // alpha0 of the first and last node (radians)
+  double lymin, lymax;    // log E of the first and last node
+  double denorm;          // gME^2 gC^2
+  const double *Daa, *Dap, *Dpp;        // (na, ne) row-major
+  const double *rp, *rdl, *rdl2;        // per row: p, dlogE/dp, (dlogE/dp)^2
+};
+
+// calWeight (utils.h:44-58): weight of the lower node; past the last node, the last node with
+// weight 1 (i = n-1, w = 0). Below the first node the reference converts a negative floor() to
+// size_t (undefined in C++); its own i < 0 branch (first node, weight 1) is what is done here.
+__device__ __forceinline__ void cal_weight(long long* i, double* w, long long n, double pos) {
+  if (pos < 0.0) {
+    *i = 0;
+    *w = 1.0;
+  } else if (*i < n) {
+    *w = __dadd_rn(1.0, -__dadd_rn(pos, -(double)*i));
+  } else {
+    *i = n - 1;
+    *w = 0.0;
+  }
+}
+
+// D fields of Albert_Young(_LC)::constructD (Albert_Young.cc:112-134) at the cell centres, then
+// the face factors of those cells. locate (Albert_Young.cc:94-110) places a centre in the table
+// from its end points (uniform in alpha0 and log E); interp2D (utils.h:24-41) is bilinear. The
+// transcendental row factors p = e2p(exp(log E)), dlogE/dp and its square (utils.h:12-20), the
+// logs of the table's energy bounds and the unit factor come from the host's libm, so every
+// operation here is a separately rounded IEEE add, multiply or divide in the reference's order.
+// Tiles [t0, t1) of the tile list.
+template <typename A>
+__global__ void k_dtable(Common cm, Geo geo, DTab t, const double* xe, const double* ye, int t0, int t1) {
+  const double s2d = 86400.0;  // 3600 * 24
+  for (int tl = t0 + blockIdx.x; tl < t1; tl += gridDim.x) {
+    const int b = cm.tile_inst[tl];
+    const InstDev I = cm.inst[b];
+    if (!I.enabled) continue;
+    const int lt = tl - I.tile0, i0t = (lt % I.ntx) * kTX, j0t = (lt / I.ntx) * kTY;
+    for (int q = threadIdx.x; q < kTX * kTY; q += blockDim.x) {
+      const int i = i0t + (q % kTX), j = j0t + (q / kTX);
+      if (i >= I.nx || j >= I.ny) continue;
+      const long long K = I.base + (long long)j * I.pitch + i;
+      const double xl = xe[I.xe + i], xr = xe[I.xe + i + 1];
+      const double yb = ye[I.ye + j], yt = ye[I.ye + j + 1];
+      const double alpha0 = __dmul_rn(0.5, __dadd_rn(xl, xr)), logE = __dmul_rn(0.5, __dadd_rn(yb, yt));
+      const double px = __dmul_rn(__ddiv_rn(__dadd_rn(alpha0, -t.xmin), __dadd_rn(t.xmax, -t.xmin)), (double)(t.na - 1));
+      const double py = __dmul_rn(__ddiv_rn(__dadd_rn(logE, -t.lymin), __dadd_rn(t.lymax, -t.lymin)), (double)(t.ne - 1));
+      long long ia = px >= 0.0 ? (long long)floor(px) : 0, je = py >= 0.0 ? (long long)floor(py) : 0;
+      double wi, wj;
+      cal_weight(&ia, &wi, t.na - 1, px);
+      cal_weight(&je, &wj, t.ne - 1, py);
+      const double ui = __dadd_rn(1.0, -wi), uj = __dadd_rn(1.0, -wj);
+      const long long r00 = ia * t.ne + je, r10 = r00 + t.ne;
+      const double* raw[3] = {t.Daa, t.Dap, t.Dpp};
+      double v[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const double* r = raw[k];
+        const double s1 = __dmul_rn(__dmul_rn(r[r00], wi), wj);
+        const double s2 = __dmul_rn(__dmul_rn(r[r10], ui), wj);
+        const double s3 = __dmul_rn(__dmul_rn(r[r10 + 1], ui), uj);
+        const double s4 = __dmul_rn(__dmul_rn(r[r00 + 1], wi), uj);
+        v[k] = __dadd_rn(__dadd_rn(__dadd_rn(s1, s2), s3), s4);
+      }
+      const double p = t.rp[I.ye + j], dl = t.rdl[I.ye + j], dl2 = t.rdl2[I.ye + j];
+      const double dxx = __ddiv_rn(__dmul_rn(__dmul_rn(v[0], t.denorm), s2d), __dmul_rn(p, p));
+      const double dxy = __ddiv_rn(__dmul_rn(__dmul_rn(__dmul_rn(v[1], t.denorm), s2d), dl), p);
+      const double dyy = __dmul_rn(__dmul_rn(__dmul_rn(v[2], t.denorm), s2d), dl2);
+      setup_faces<A>(geo, K, xl, xr, yb, yt, geo.G[K], dxx, dxy, dyy);
+    }
   }
 }
 

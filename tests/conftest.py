@@ -64,3 +64,37 @@ def c0_problem():
 
     rp = cases.read_ini(os.path.join(ROOT, "sayram-2d_gb300", "configs", "c0.ini"))
     return rp, cases.problem_from_params(rp)
+
+
+def load_table_cases():
+    """The reference-generated Albert_Young / Albert_Young_LC fixtures: name -> dict with which,
+    x_edges, y_edges, dt, Emin, Emax, table (cases.DTable) and the reference's outputs (G, Dxx,
+    Dxy, Dyy, inv_tau, f0, bc, dirichlet)."""
+    import numpy as np
+    from sayram2d_gb300 import cases
+
+    z = np.load(os.path.join(GOLDEN, "ref_cases.npz"))
+    out = {}
+    for name in sorted({k.split("/")[0] for k in z.files}):
+        g = lambda k: z[f"{name}/{k}"]
+        which, dt, Emin, Emax = g("meta")
+        bc = [int(v) for v in g("bc")]
+        out[name] = {
+            "which": int(which), "dt": float(dt), "Emin": float(Emin), "Emax": float(Emax),
+            "x_edges": g("x_edges"), "y_edges": g("y_edges"),
+            "table": cases.DTable(*[g("table_" + k) for k in ("alpha0_deg", "E", "Daa", "Dap", "Dpp")]),
+            **{k: g(k) for k in ("G", "Dxx", "Dxy", "Dyy", "inv_tau", "f0")},
+            "bc": bc, "dirichlet": [g(f"dir{s}") if bc[s] == cases.DIRICHLET else None for s in range(4)],
+        }
+    return out
+
+
+def case_problem(c):
+    """A cases.Problem for a table fixture, built by the host case generators with the
+    reference's interpolated D (the generators' G, f0 and inv_tau are compared separately)."""
+    from sayram2d_gb300 import cases
+
+    nx, ny = len(c["x_edges"]) - 1, len(c["y_edges"]) - 1
+    mk = cases.albert_young_problem if c["which"] == 0 else cases.albert_young_lc_problem
+    kw = {"alpha0_min_deg": 5.0} if c["which"] == 0 else {}
+    return mk(nx, ny, c["dt"], Emin=c["Emin"], Emax=c["Emax"], D=(c["Dxx"], c["Dxy"], c["Dyy"]), **kw)

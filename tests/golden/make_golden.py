@@ -7,7 +7,14 @@ diagonals, system order) and right-hand side R that the reference assembles from
 1 and ``nsteps`` updates. The config-0 case (90 x 90, 1000 steps) stores only outputs; its inputs
 are regenerated from the seeded generator (an input checksum guards against drift).
 
-Run here (where the reference sources exist):  python tests/golden/make_golden.py
+The case fixtures (ref_cases.npz) come from the reference's own Albert_Young, Albert_Young_LC
+and Albert_Young_IO sources, compiled the same way (oracle/_ref/libsayram_case_ref.so, driven by
+oracle/ref_case_harness.cc): for each grid and seeded D table, the fields a Solver reads from the
+case -- G, Dxx, Dxy, Dyy (interpolated from the table), inv_tau, init_f, the BC types and the
+Dirichlet vertex values.
+
+Run here (where the reference sources exist):  python tests/golden/make_golden.py [cases]
+("cases" regenerates only ref_cases.npz)
 """
 import hashlib
 import os
@@ -68,10 +75,49 @@ def input_digest(p):
     return h.hexdigest()
 
 
+def table_cases():
+    """(which, x_edges, y_edges, dt, Emin, Emax, table) per fixture; which 0 = Albert_Young,
+    1 = Albert_Young_LC. The grids follow main.cc:20-37; the tables are seeded stand-ins for the
+    HDF5 D files, one of them ending below the grid's upper alpha0 and E (the clamped branch of
+    calWeight), one of them the smallest table (2 x 2)."""
+    d2r = PI / 180
+    lE = lambda lo, hi, n: cases.uniform_edges(n, np.log(lo), np.log(hi))
+    return {
+        "ay_24x20": (0, cases.uniform_edges(24, 5 * d2r, 90 * d2r), lE(0.2, 5.0, 20), 1e-2, 0.2, 5.0,
+                     cases.synthetic_dtable(1)),
+        "ay_16x12_clamped": (0, cases.uniform_edges(16, 5 * d2r, 90 * d2r), lE(0.2, 5.0, 12), 1e-2, 0.2, 5.0,
+                             cases.synthetic_dtable(2, n_alpha=31, n_E=17, alpha0_max_deg=60.0, Emax=2.0)),
+        "lc_20x16": (1, cases.uniform_edges(20, 0.0, 90 * d2r), lE(0.2, 5.0, 16), 1e-2, 0.2, 5.0,
+                     cases.synthetic_dtable(3)),
+        "ay_13x9_table2x2": (0, cases.uniform_edges(13, 5 * d2r, 90 * d2r), lE(0.2, 5.0, 9), 1e-3, 0.2, 5.0,
+                             cases.synthetic_dtable(4, n_alpha=2, n_E=2)),
+    }
+
+
+def write_case_fixtures():
+    data = {}
+    for name, (which, xe, ye, dt, Emin, Emax, t) in table_cases().items():
+        r = oracle.ref_case(which, xe, ye, dt, Emin, Emax, t)
+        data[name + "/meta"] = np.array([which, dt, Emin, Emax], dtype=np.float64)
+        data[name + "/x_edges"], data[name + "/y_edges"] = xe, ye
+        for k in ("alpha0_deg", "E", "Daa", "Dap", "Dpp"):
+            data[name + "/table_" + k] = getattr(t, k)
+        for k in ("G", "Dxx", "Dxy", "Dyy", "inv_tau", "f0"):
+            data[name + "/" + k] = r[k]
+        data[name + "/bc"] = np.array(r["bc"], dtype=np.float64)
+        for s in range(4):
+            data[name + f"/dir{s}"] = r["dirichlet"][s] if r["dirichlet"][s] is not None else np.zeros(0)
+    np.savez_compressed(os.path.join(HERE, "ref_cases.npz"), **data)
+
+
 def main():
     oracle.build()
     if oracle.build_ref() is None:
         raise SystemExit("the reference sources are needed to generate fixtures")
+    write_case_fixtures()
+    if sys.argv[1:] == ["cases"]:
+        print("wrote ref_cases.npz")
+        return
     nsteps = 10
     data = {}
     for name, p in small_cases().items():

@@ -68,6 +68,11 @@ def test_null_handles_rejected(capi):
     assert L.sayram_batch_step(None, 1) == capi.ERR_ARG
     assert L.sayram_batch_get_f(None, 0, None) == capi.ERR_ARG
     assert L.sayram_batch_size(None) == 0
+    assert L.sayram_batch_autotune(None, 1, None, None) == capi.ERR_ARG
+    assert L.sayram_batch_set_dtable(None, 0, None) == capi.ERR_ARG
+    assert L.sayram_set_dtable(None, None) == capi.ERR_ARG
+    assert L.sayram_batch_set_launch_shape(None, 1024, 8) == capi.ERR_ARG
+    assert L.sayram_batch_get_launch_shape(None, None, None) == capi.ERR_ARG
 
 
 def test_instance_bytes_monotone(capi):

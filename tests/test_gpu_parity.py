@@ -242,3 +242,24 @@ def test_autotune_restores_state(capi, oracle, prec):
         assert rel(b.f(k), f) <= tol, (prec, k, rel(b.f(k), f))
         assert b.f(k).min() >= 0.0
     b.close()
+
+
+def test_launch_shape_setter(capi):
+    """Every launch shape gives the same FP64 answer up to the order of the reductions; shapes
+    outside the supported set are refused."""
+    probs = cases.batch_problems(4, seed=41, dt=1e-2, lo=30, hi=140)
+    ref = capi.Batch(probs, precision=capi.FP64)
+    ref.step(2)
+    for chunk, blocks in ((1024, 8), (2048, 16), (4096, 32), (4096, 1)):
+        b = capi.Batch(probs, precision=capi.FP64)
+        b.set_launch_shape(chunk, blocks)
+        assert b.launch_shape() == (chunk, blocks)
+        b.step(2)
+        for k in range(len(probs)):
+            assert rel(b.f(k), ref.f(k)) <= 1e-12, (chunk, blocks, k)
+        b.close()
+    with pytest.raises(RuntimeError, match="chunk must be"):
+        ref.set_launch_shape(3000, 8)
+    with pytest.raises(RuntimeError, match="blocks_per_sm"):
+        ref.set_launch_shape(1024, 0)
+    ref.close()

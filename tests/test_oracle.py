@@ -140,3 +140,48 @@ def test_forward_error_scale(oracle, name):
     M5, R, B5 = oracle.assemble_bound(p, p.f0)
     assert np.array_equal(M5, Z[f"{name}/M5"])
     assert (B5 >= np.abs(M5) * (1 - 1e-12)).all()
+
+
+# ------------------------------------------------------------------ D table and the reference cases
+from conftest import case_problem, load_table_cases  # noqa: E402
+
+TABLE_CASES = load_table_cases()
+
+
+@pytest.mark.parametrize("name", sorted(TABLE_CASES))
+def test_dtable_restatement_bit_exact(oracle, name):
+    """locate / calWeight / interp2D / constructD restated in C reproduce the reference's
+    Albert_Young(_LC)::constructD bit for bit, including the clamped branch past the table's
+    last node and the smallest (2 x 2) table."""
+    c = TABLE_CASES[name]
+    D = oracle.dtable_fields(c["x_edges"], c["y_edges"], c["table"])
+    for k, d in zip(("Dxx", "Dxy", "Dyy"), D):
+        assert np.array_equal(d, c[k]), (name, k)
+
+
+@pytest.mark.parametrize("name", sorted(TABLE_CASES))
+def test_case_generators_match_reference(name):
+    """The host case generators give the reference cases' G, f0 (numpy's transcendentals: a few
+    ulps), inv_tau, BC types and Dirichlet vertex values."""
+    c = TABLE_CASES[name]
+    p = case_problem(c)
+    assert np.array_equal(p.x_edges, c["x_edges"]) and np.array_equal(p.y_edges, c["y_edges"])
+    for k in ("G", "f0", "inv_tau"):
+        a, b = getattr(p, k), c[k]
+        assert np.allclose(a, b, rtol=1e-14, atol=0.0), (name, k, np.max(np.abs(a - b) / np.abs(b)))
+    assert list(p.bc) == c["bc"]
+    for s in range(4):
+        if c["dirichlet"][s] is None:
+            assert p.dirichlet[s] is None
+        else:
+            assert np.allclose(p.dirichlet[s], c["dirichlet"][s], rtol=1e-14, atol=0.0)
+
+
+def test_case_fixture_regenerates(oracle):
+    """Where the reference sources are present, its case build reproduces the stored fixture."""
+    if oracle.build_ref() is None:
+        pytest.skip("reference sources absent")
+    c = TABLE_CASES["lc_20x16"]
+    r = oracle.ref_case(c["which"], c["x_edges"], c["y_edges"], c["dt"], c["Emin"], c["Emax"], c["table"])
+    for k in ("G", "Dxx", "Dxy", "Dyy", "inv_tau", "f0"):
+        assert np.array_equal(r[k], c[k]), k
