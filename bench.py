@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--serve-rate", type=float, default=30.0, help="Poisson arrival rate (requests/s)")
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
     ap.add_argument("--serve-only", action="store_true")
+    ap.add_argument("--launch-shape", default="",
+                    help="CHUNK,BLOCKS_PER_SM instead of the autotuner (e.g. 4096,32; for profiling)")
     ap.add_argument("--no-graph", action="store_true",
                     help="host-driven loops instead of the per-step CUDA graph (for ncu, which cannot profile "
                          "kernels inside graphs with conditional nodes)")
@@ -321,7 +323,11 @@ def run_ours(a):
     other = capi.FP32_REFINE if a.precision == "dw" else capi.FP32_REFINE_DW
     b = capi.Batch(probs, precision=prec, use_graph=0 if a.no_graph else 1)
     t0 = time.perf_counter()
-    shape = b.autotune(2)
+    if a.launch_shape:
+        b.set_launch_shape(*[int(v) for v in a.launch_shape.split(",")])
+        shape = b.launch_shape()
+    else:
+        shape = b.autotune(2)
     tune_s = time.perf_counter() - t0
     for _ in range(a.warmup):
         b.step(1, allow_not_converged=True)
