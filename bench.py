@@ -223,6 +223,12 @@ BYTES32 = {
 }
 
 
+# DRAM bytes per processed cell measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the
+# 256-instance case of the same kernels (profiles/*_dw_256instances.md); traffic grows with the
+# cells processed, so a launch's traffic is this figure times the cells it processed.
+TRAFFIC32 = {"assemble": 146.2, "bicg1": 40.3, "bicg2": 27.9, "resid": 60.9, "polish": 92.9}
+
+
 def kernel_roofline(b, probs, peak, steps=2):
     """Per-kernel event timing over `steps` steps; bytes from the cells each kernel processed."""
     cells = np.array([p.nx * p.ny for p in probs], dtype=np.float64)
@@ -250,9 +256,10 @@ def kernel_roofline(b, probs, peak, steps=2):
     dom = max((k for k in out if k in BYTES32), key=lambda k: out[k]["ms"])
     d = out[dom]
     ach = d["GBps"]
-    traffic = None
+    traffic = TRAFFIC32[dom] * d["bytes"] / BYTES32[dom] / d["launches"] if dom in TRAFFIC32 else None
     roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak[0], "unit": "GB/s",
             "frac": ach / peak[0], "peak_source": peak[1], "traffic": traffic,
+            "traffic_source": "ncu dram bytes per cell on 256 instances, scaled by the cells processed",
             "bytes_per_launch": d["bytes"] / d["launches"], "avg_launch_ms": d["ms"] / d["launches"]}
     return roof, out
 

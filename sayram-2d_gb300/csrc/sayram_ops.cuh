@@ -128,6 +128,7 @@ struct F64A {
   __device__ static V max0(V a) { return fmax(a, 0.0); }
   __device__ static V k(double c) { return c; }
   __device__ static bool lt0(V a) { return a < 0.0; }
+  __device__ static bool gt0(V a) { return a > 0.0; }
   __device__ static float f32(V a) { return (float)a; }
   __device__ static float sq32(V a) { return (float)(a * a); }
   __device__ static double to_d(V a) { return a; }
@@ -187,6 +188,7 @@ struct DWA {
   __device__ static V max0(V a) { return dw_max0(a); }
   __device__ static V k(double c) { return dw_from_double(c); }
   __device__ static bool lt0(V a) { return a.hi < 0.0f; }
+  __device__ static bool gt0(V a) { return a.hi > 0.0f; }
   __device__ static float f32(V a) { return a.hi; }
   __device__ static float sq32(V a) { return a.hi * a.hi; }
   __device__ static double to_d(V a) { return dw_to_double(a); }
@@ -467,10 +469,14 @@ __device__ __forceinline__ void inner_face(typename A::V aK, typename A::V SK, t
   const V muK = A::div(A::addp(absL, A::k(kEps)), denom);
   const V muL = A::rsub1(muK);
   const V B = A::sub(A::mul(muL, aL), A::mul(muK, aK));
-  const V Bp = A::max0(B);             // (|B| + B) / 2
-  const V Bm = A::max0(A::neg(B));     // (|B| - B) / 2
-  *AK = A::fmap(Bp, invK, A::mul(muK, SK));  // all terms >= 0
-  *AL = A::fmap(Bm, invL, A::mul(muL, SL));
+  // B+ = (|B| + B)/2 goes to K's coefficient, B- = (|B| - B)/2 to L's; at most one is nonzero,
+  // so only that one is multiplied by its 1/(f + eps) and added (all terms >= 0)
+  const V mK = A::mul(muK, SK), mL = A::mul(muL, SL);
+  const bool pos = A::gt0(B);
+  const V T = A::mul(pos ? B : A::max0(A::neg(B)), pos ? invK : invL);
+  const V X = A::addp(pos ? mK : mL, T);
+  *AK = pos ? X : mK;
+  *AL = pos ? mL : X;
 }
 
 // Dirichlet face (Solver.cc:143-164): B = -a_sigma; A = S + B+/(f+eps); R += B-.
