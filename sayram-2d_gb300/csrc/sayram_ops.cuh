@@ -675,6 +675,32 @@ __device__ __forceinline__ Slot slot_of(int c, const InstDev& I, int g) {
   return s;
 }
 
+// Runs body(c) for every chunk c of this block (c = blockIdx.x + k*gridDim.x) whose instance
+// passes want(instance). The instance checks run in parallel, one chunk per thread, and the
+// passing chunks are compacted in shared memory: a launch in which most instances have finished
+// costs one round of checks per block instead of two dependent loads per chunk. Chunks are
+// independent, so the order in which a block takes them does not change any result.
+template <typename W, typename Body>
+__device__ __forceinline__ void for_active_chunks(const Common& cm, W&& want, Body&& body) {
+  __shared__ int s_list[kThreads];
+  __shared__ int s_cnt;
+  const int nc = n_chunks(cm);
+  const int per = (int)blockIdx.x < nc ? (nc - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  for (int r0 = 0; r0 < per; r0 += kThreads) {
+    if (threadIdx.x == 0) s_cnt = 0;
+    __syncthreads();
+    const int k = r0 + (int)threadIdx.x;
+    if (k < per) {
+      const int c = (int)blockIdx.x + k * (int)gridDim.x;
+      if (want(cm.chunk_inst[c])) s_list[atomicAdd(&s_cnt, 1)] = c;
+    }
+    __syncthreads();
+    const int m = s_cnt;
+    for (int q = 0; q < m; ++q) body(s_list[q]);
+    __syncthreads();
+  }
+}
+
 // Fills smem[0 .. n) with a 4-aligned stretch [e0, e0 + n) of a vector computed cell-wise by
 // f(k) -> Q4<T> (k a multiple of 4): the chunk plus one row above and below, so that the stencil
 // of every cell in the chunk reads shared memory only.
@@ -774,10 +800,9 @@ __global__ void __launch_bounds__(kThreads, 3) k_resid(Common cm, Fields fl, Coe
   count_launch(cm.ctl);
   extern __shared__ __align__(16) unsigned char smraw[];
   V* sm = reinterpret_cast<V*>(smraw);
-  for (int c = blockIdx.x, nc_ = n_chunks(cm); c < nc_; c += gridDim.x) {
+  for_active_chunks(cm, [&](int b_) { return cm.st[b_].outer_active != 0; }, [&](int c) {
     const int b = cm.chunk_inst[c];
     InstState& st = cm.st[b];
-    if (!st.outer_active) continue;
     const InstDev I = cm.inst[b];
     const double* yin = fl.y64[st.ycur];
     double* yout = fl.y64[st.ycur ^ 1];
@@ -856,7 +881,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_resid(Common cm, Fields fl, Coe
         atomicAdd(&cm.ctl->n_inner, 1);
       }
     }
-  }
+  });
   loop_epilogue(cm, 0);
 }
 
@@ -869,10 +894,9 @@ __global__ void __launch_bounds__(kThreads) k_bicg1(Common cm, Coef<T> co, Kry<T
   count_launch(cm.ctl);
   extern __shared__ __align__(16) unsigned char smraw[];
   T* sm = reinterpret_cast<T*>(smraw);
-  for (int c = blockIdx.x, nc_ = n_chunks(cm); c < nc_; c += gridDim.x) {
+  for_active_chunks(cm, [&](int b_) { return cm.st[b_].inner_active != 0; }, [&](int c) {
     const int b = cm.chunk_inst[c];
     InstState& st = cm.st[b];
-    if (!st.inner_active) continue;
     const InstDev I = cm.inst[b];
     const int pc = st.pcur;
     const bool rs = st.restart != 0;
@@ -933,7 +957,7 @@ __global__ void __launch_bounds__(kThreads) k_bicg1(Common cm, Coef<T> co, Kry<T
         st.restart = 1;
       }
     }
-  }
+  });
 }
 
 // k2: s = r - alpha v;  t = A~ s;  partials (t, s), (t, t). s is staged like p in k1.
@@ -942,10 +966,9 @@ __global__ void __launch_bounds__(kThreads) k_bicg2(Common cm, Coef<T> co, Kry<T
   count_launch(cm.ctl);
   extern __shared__ __align__(16) unsigned char smraw[];
   T* sm = reinterpret_cast<T*>(smraw);
-  for (int c = blockIdx.x, nc_ = n_chunks(cm); c < nc_; c += gridDim.x) {
+  for_active_chunks(cm, [&](int b_) { return cm.st[b_].inner_active != 0; }, [&](int c) {
     const int b = cm.chunk_inst[c];
     InstState& st = cm.st[b];
-    if (!st.inner_active) continue;
     const InstDev I = cm.inst[b];
     const T alpha = (T)st.alpha;
     const T* __restrict__ r = kr.r;
@@ -988,7 +1011,7 @@ __global__ void __launch_bounds__(kThreads) k_bicg2(Common cm, Coef<T> co, Kry<T
       }
       if (st.omega == 0.0) st.restart = 1;
     }
-  }
+  });
 }
 
 // k3: x += alpha p + omega s (x starts at 0 on the first iteration of a solve);
@@ -996,10 +1019,9 @@ __global__ void __launch_bounds__(kThreads) k_bicg2(Common cm, Coef<T> co, Kry<T
 template <typename T, int CH>
 __global__ void __launch_bounds__(kThreads) k_bicg3(Common cm, Kry<T> kr, int max_iters) {
   count_launch(cm.ctl);
-  for (int c = blockIdx.x, nc_ = n_chunks(cm); c < nc_; c += gridDim.x) {
+  for_active_chunks(cm, [&](int b_) { return cm.st[b_].inner_active != 0; }, [&](int c) {
     const int b = cm.chunk_inst[c];
     InstState& st = cm.st[b];
-    if (!st.inner_active) continue;
     const InstDev I = cm.inst[b];
     const T alpha = (T)st.alpha, omega = (T)st.omega;
     const bool fresh = st.fresh != 0;
@@ -1051,7 +1073,7 @@ __global__ void __launch_bounds__(kThreads) k_bicg3(Common cm, Kry<T> kr, int ma
         }
       }
     }
-  }
+  });
   loop_epilogue(cm, 1);
 }
 
@@ -1065,11 +1087,10 @@ __global__ void __launch_bounds__(kThreads, 3) k_polish(Common cm, Fields fl, Co
   extern __shared__ __align__(16) unsigned char smraw[];
   V* sm = reinterpret_cast<V*>(smraw);
   __shared__ float smin[kThreads / 32];
-  for (int c = blockIdx.x, nc_ = n_chunks(cm); c < nc_; c += gridDim.x) {
+  for_active_chunks(cm, [&](int b_) { return cm.inst[b_].enabled != 0; }, [&](int c) {
     const int b = cm.chunk_inst[c];
     InstState& st = cm.st[b];
     const InstDev I = cm.inst[b];
-    if (!I.enabled) continue;
     const double* y = fl.y64[st.ycur];
     const int P = I.pitch;
     const long long c0 = chunk_start<CH>(c, I);
@@ -1141,7 +1162,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_polish(Common cm, Fields fl, Co
       if (!(gmin >= 0.0)) st.status = ST_NEGATIVE;
     }
     __syncthreads();
-  }
+  });
 }
 
 }  // namespace sg
