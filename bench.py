@@ -214,12 +214,12 @@ def run_reference(a):
 # Algorithmic bytes per real cell per launch (FP32+refine path): reads + writes of the arrays
 # each kernel must touch once (neighbour re-reads served by cache are not counted).
 BYTES32 = {
-    "assemble": 2 * 8 + 8 * 8 + 4 * (4 + 4) + 4 * 8,  # f, f_prev, 8 factors -> 4 hi+lo coefs, invD/R/colsum/y
+    "assemble": 4 * 8 + 8 * 8 + 4 * (4 + 4) + 4 * 8,  # f + 3 earlier states, 8 factors -> 4 hi+lo coefs, invD/R/colsum/y
     "resid": 8 + 4 + 8 + 4 * (4 + 4) + 8 + 4,     # y, x, R, hi+lo coefs -> y', r
     "bicg1": 4 * 4 + 4 * 4 + 2 * 4,               # r, p, v, r^, 4 coefs -> p', v'
     "bicg2": 2 * 4 + 4 * 4 + 4,                   # r, v, 4 coefs -> t
     "bicg3": 6 * 4 + 2 * 4,                       # r, v, p, t, r^, x -> x, r
-    "polish": 8 + 4 * (4 + 4) + 3 * 8 + 8 + 2 * 8,  # y, hi+lo coefs, R, invD, colsum -> f; f -> f_prev
+    "polish": 8 + 4 * (4 + 4) + 3 * 8 + 8 + 2 * 8,  # y, hi+lo coefs, R, invD, colsum -> f; f -> history
 }
 
 

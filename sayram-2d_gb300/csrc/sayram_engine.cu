@@ -348,7 +348,7 @@ int sayram_batch_s::alloc_storage(long long cells, int slots, int chunks_cap, in
     SG_ALLOC(*g, cells);
     cell_arrays.push_back({*g, 8});
   }
-  double** fs[7] = {&fl.f, &fl.fprev, &fl.invD, &fl.R, &fl.colsum, &fl.y64[0], &fl.y64[1]};
+  double** fs[9] = {&fl.f, &fl.fh[0], &fl.fh[1], &fl.fh[2], &fl.invD, &fl.R, &fl.colsum, &fl.y64[0], &fl.y64[1]};
   for (auto f : fs) {
     SG_ALLOC(*f, cells);
     cell_arrays.push_back({*f, 8});
@@ -391,6 +391,7 @@ int sayram_batch_s::alloc_storage(long long cells, int slots, int chunks_cap, in
   cm.dirv = d_dirv;
   cm.part = d_part;
   cm.dyn = d_dyn;
+  cm.hist_cap = 3;
   return SAYRAM_OK;
 }
 
@@ -800,25 +801,25 @@ int sayram_batch_s::set_dtable(int idx, const sayram_dtable* t) {
 }
 
 // Times `steps` steps of every launch shape (cells per chunk x blocks per SM) from the same
-// state and keeps the fastest; f, the previous f and the per-instance state are restored
-// afterwards, so tuning does not advance the simulation.
+// state and keeps the fastest; f, the history of earlier states and the per-instance state are
+// restored afterwards, so tuning does not advance the simulation.
 int sayram_batch_s::autotune(int steps, int* best_chunk, int* best_grid) {
   if (steps < 1) steps = 1;
   SG_CUDA(cudaSetDevice(dev));
-  double *bf = nullptr, *bp = nullptr;
-  if (cudaMalloc(&bf, sizeof(double) * ncell) != cudaSuccess || cudaMalloc(&bp, sizeof(double) * ncell) != cudaSuccess) {
+  double* snap = nullptr;  // f, fh[0], fh[1], fh[2]
+  if (cudaMalloc(&snap, sizeof(double) * 4 * ncell) != cudaSuccess) {
     cudaGetLastError();
-    if (bf) cudaFree(bf);
     return fail(SAYRAM_ERR_OOM, "autotune: no room for the state snapshot");
   }
+  double* const saved[4] = {fl.f, fl.fh[0], fl.fh[1], fl.fh[2]};
   std::vector<InstState> hs(cap_slots);
-  SG_CUDA(cudaMemcpyAsync(bf, fl.f, sizeof(double) * ncell, cudaMemcpyDeviceToDevice, stream));
-  SG_CUDA(cudaMemcpyAsync(bp, fl.fprev, sizeof(double) * ncell, cudaMemcpyDeviceToDevice, stream));
+  for (int k = 0; k < 4; ++k)
+    SG_CUDA(cudaMemcpyAsync(snap + k * ncell, saved[k], sizeof(double) * ncell, cudaMemcpyDeviceToDevice, stream));
   SG_CUDA(cudaMemcpyAsync(hs.data(), d_st, sizeof(InstState) * cap_slots, cudaMemcpyDeviceToHost, stream));
   SG_CUDA(cudaStreamSynchronize(stream));
   auto restore = [&]() -> int {
-    SG_CUDA(cudaMemcpyAsync(fl.f, bf, sizeof(double) * ncell, cudaMemcpyDeviceToDevice, stream));
-    SG_CUDA(cudaMemcpyAsync(fl.fprev, bp, sizeof(double) * ncell, cudaMemcpyDeviceToDevice, stream));
+    for (int k = 0; k < 4; ++k)
+      SG_CUDA(cudaMemcpyAsync(saved[k], snap + k * ncell, sizeof(double) * ncell, cudaMemcpyDeviceToDevice, stream));
     SG_CUDA(cudaMemcpyAsync(d_st, hs.data(), sizeof(InstState) * cap_slots, cudaMemcpyHostToDevice, stream));
     SG_CUDA(cudaStreamSynchronize(stream));
     return SAYRAM_OK;
@@ -861,8 +862,7 @@ int sayram_batch_s::autotune(int steps, int* best_chunk, int* best_grid) {
   if (!rc2) rc2 = restore();
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  cudaFree(bf);
-  cudaFree(bp);
+  cudaFree(snap);
   timing = timing_was;
   if (rc) return rc;
   if (rc2) return rc2;
@@ -950,7 +950,7 @@ int sayram_batch_step_host(sayram_batch b, int nsteps, const double* f_in, doubl
   if (f_in) {
     SG_CUDA(cudaMemcpyAsync(b->d_stage, f_in, sizeof(double) * b->nreal, cudaMemcpyHostToDevice, b->stream));
     // a replaced state has no previous step to extrapolate from
-    SG_CUDA(cudaMemset2DAsync((char*)b->d_st + offsetof(InstState, has_prev), sizeof(InstState), 0, sizeof(int),
+    SG_CUDA(cudaMemset2DAsync((char*)b->d_st + offsetof(InstState, nhist), sizeof(InstState), 0, sizeof(int),
                               (size_t)b->n, b->stream));
     b->launch("field_in", [&] {
       if (b->dwm)
@@ -996,7 +996,7 @@ int sayram_batch_set_f(sayram_batch b, int idx, const double* f) {
   for (int i = 0; i < I.nx; ++i)
     for (int j = 0; j < I.ny; ++j) rows[(size_t)j * I.pitch + i] = b->wide(f[(size_t)i * I.ny + j]);
   SG_CUDA(cudaMemcpyAsync(b->fl.f + I.base, rows.data(), sizeof(double) * rows.size(), cudaMemcpyHostToDevice, b->stream));
-  SG_CUDA(cudaMemsetAsync((char*)(b->d_st + idx) + offsetof(InstState, has_prev), 0, sizeof(int), b->stream));
+  SG_CUDA(cudaMemsetAsync((char*)(b->d_st + idx) + offsetof(InstState, nhist), 0, sizeof(int), b->stream));
   SG_CUDA(cudaStreamSynchronize(b->stream));
   return SAYRAM_OK;
 }
@@ -1203,7 +1203,7 @@ void sayram_batch_destroy(sayram_batch b) { delete b; }
 size_t sayram_instance_bytes(int nx, int ny, int precision) {
   const long long pitch = round_up(nx, 4);
   const long long cells = round_up((long long)(ny + 2) * pitch, 32);
-  const long long per = 16 * 8 + (precision != SAYRAM_FP64 ? 8 * 4 + 8 * 4 : 4 * 8 + 8 * 8) + 8;
+  const long long per = 18 * 8 + (precision != SAYRAM_FP64 ? 8 * 4 + 8 * 4 : 4 * 8 + 8 * 8) + 8;
   return (size_t)(cells * per + 4096);
 }
 
@@ -1750,13 +1750,14 @@ extern "C" int sayram_step_noalloc(const sayram_problem* pd, const sayram_option
   Coef<double> co{};
   Kry<double> kr{};
   double** cellarrs[27] = {&geo.aAx, &geo.aBx, &geo.Sx, &geo.aAy, &geo.aBy, &geo.Sy, &geo.ukk, &geo.sdiag,
-                           &fl.f, &fl.fprev, &fl.invD, &fl.R, &fl.colsum, &fl.y64[0], &fl.y64[1],
+                           &fl.f, &fl.fh[0], &fl.invD, &fl.R, &fl.colsum, &fl.y64[0], &fl.y64[1],
                            &co.cw, &co.ce, &co.cs, &co.cn,
                            &kr.r, &kr.rh, &kr.t, &kr.x, &kr.p[0], &kr.p[1], &kr.v[0], &kr.v[1]};
   for (auto a : cellarrs) {
     *a = lay.take<double>(kNoAllocCells);
     if (!*a) return fail(SAYRAM_ERR_ARG, "cell arrays exceed the scratch");
   }
+  fl.fh[1] = fl.fh[2] = fl.fh[0];  // one history buffer: linear extrapolation (Common::hist_cap = 1)
   unsigned char* used_end = lay.cur;
 
   // ---- every call starts from zero: padding, pad rows, state and counters must be 0
@@ -1795,6 +1796,7 @@ extern "C" int sayram_step_noalloc(const sayram_problem* pd, const sayram_option
   cm.inst = d_inst;
   cm.st = d_st;
   cm.ctl = d_ctl;
+  cm.hist_cap = 1;
   cm.chunk_inst = d_chunk;
   cm.nchunks = I.nchunks;
   cm.tile_inst = d_tile;

@@ -48,6 +48,7 @@ struct Common {
   unsigned long long h_outer, h_inner;  // cudaGraphConditionalHandle of the two WHILE nodes
   int use_cond;
   int guard_refine, guard_iters;  // hard caps on loop trips, whatever the bookkeeping says
+  int hist_cap;  // history depth used for the starting point (3; 1 when the three buffers alias)
 };
 
 __device__ __forceinline__ int n_chunks(const Common& cm) { return cm.dyn ? cm.dyn[0] : cm.nchunks; }
@@ -90,7 +91,7 @@ struct Coef {  // row-oriented scaled off-diagonal magnitudes (hi parts when spl
 
 struct Fields {
   double* f;       // state, padded system order
-  double* fprev;   // state of the previous step
+  double* fh[3];   // earlier states f^(n-1), f^(n-2), f^(n-3), rotated per instance (InstState::hslot)
   double* invD;    // 1 / diag(M)
   double* R;       // right-hand side
   double* colsum;  // 1^T M per column (conservation check)
@@ -122,8 +123,17 @@ struct F64A {
   __device__ static V div(V a, V b) { return a / b; }
   __device__ static V abs(V a) { return fabs(a); }
   __device__ static V neg(V a) { return -a; }
-  // D (2 f - f_prev): the extrapolated starting point of the solve
-  __device__ static V extrap(V D, V f, V fp) { return D * (f + f - fp); }
+  // D g with g the polynomial extrapolation in time through f and n earlier states (n = 1..3):
+  // f + d1, f + 2 d1 - d2, f + 3 (d1 - d2) + d3 with d1 = f - h1, d2 = h1 - h2, d3 = h2 - h3
+  __device__ static V start(V D, V f, V h1, V h2, V h3, int n) {
+    const double d1 = f - h1;
+    double c = d1;
+    if (n >= 2) {
+      const double d2 = h1 - h2;
+      c = n == 2 ? 2.0 * d1 - d2 : 3.0 * (d1 - d2) + (h2 - h3);
+    }
+    return D * (f + c);
+  }
   __device__ static V rsub1(V a) { return 1.0 - a; }
   __device__ static V max0(V a) { return fmax(a, 0.0); }
   __device__ static V k(double c) { return c; }
@@ -181,9 +191,19 @@ struct DWA {
   __device__ static V div(V a, V b) { return dw_div(a, b); }
   __device__ static V abs(V a) { return dw_abs(a); }
   __device__ static V neg(V a) { return dw_neg(a); }
-  // the starting point only steers the iteration (the converged answer does not depend on it),
-  // so 2 f - f_prev is formed in FP32
-  __device__ static V extrap(V D, V f, V fp) { return dw_mul_f(D, fmaf(2.0f, f.hi, -fp.hi)); }
+  // as F64A::start. The increments are small against f, so they are formed in FP32 (differences
+  // of the hi parts are exact when the states are within a factor of 2) and added to f in
+  // double-word; the starting point only steers the iteration, the converged answer does not
+  // depend on it
+  __device__ static V start(V D, V f, V h1, V h2, V h3, int n) {
+    const float d1 = (f.hi - h1.hi) + (f.lo - h1.lo);
+    float c = d1;
+    if (n >= 2) {
+      const float d2 = (h1.hi - h2.hi) + (h1.lo - h2.lo);
+      c = n == 2 ? fmaf(2.0f, d1, -d2) : fmaf(3.0f, d1 - d2, (h2.hi - h3.hi) + (h2.lo - h3.lo));
+    }
+    return dw_mul(D, dw_add_f(f, c));
+  }
   __device__ static V rsub1(V a) { return dw_add_f(dw_neg(a), 1.0f); }  // 1 - a (DWPlusFP)
   __device__ static V max0(V a) { return dw_max0(a); }
   __device__ static V k(double c) { return dw_from_double(c); }
@@ -508,7 +528,10 @@ __global__ void __launch_bounds__(kAsmThreads) k_assemble(Common cm, Geo geo, Fi
     const int i0 = (lt % I.ntx) * kTX, j0 = (lt / I.ntx) * kTY;
     const int nx = I.nx, ny = I.ny, P = I.pitch;
     const long long base = I.base;
-    const bool has_prev = cm.st[b].has_prev != 0;
+    const int nh = min(cm.st[b].nhist, cm.hist_cap), hs = cm.st[b].hslot;
+    const double* h1p = fl.fh[hs];
+    const double* h2p = fl.fh[hs == 0 ? 2 : hs - 1];
+    const double* h3p = fl.fh[hs == 2 ? 0 : hs + 1];
     // 1) f and 1/(f+eps) on the tile plus a one-cell halo
     for (int q = threadIdx.x; q < HX * HY; q += blockDim.x) {
       const int hx = q % HX, hy = q / HX;
@@ -640,9 +663,17 @@ __global__ void __launch_bounds__(kAsmThreads) k_assemble(Common cm, Geo geo, Fi
       A::st(fl.invD, K, inv);
       A::st(fl.R, K, Rv);
       A::st(fl.colsum, K, A::addp(sd, dir));
-      // start the solve from the linear extrapolation 2 f^n - f^(n-1) (only the starting point of
-      // the iteration; the converged answer does not depend on it)
-      A::st(fl.y64[cm.st[b].ycur], K, has_prev ? A::extrap(D, fK, A::ld(fl.fprev, K)) : A::mul(D, fK));
+      // start the solve from the polynomial extrapolation in time through f^n and up to three
+      // earlier states (only the starting point of the iteration; the converged answer does not
+      // depend on it)
+      V y0;
+      if (nh == 0) {
+        y0 = A::mul(D, fK);
+      } else {
+        const V h1 = A::ld(h1p, K), h2 = nh >= 2 ? A::ld(h2p, K) : h1, h3 = nh >= 3 ? A::ld(h3p, K) : h2;
+        y0 = A::start(D, fK, h1, h2, h3, nh);
+      }
+      A::st(fl.y64[cm.st[b].ycur], K, y0);
       if (wIn) AsmOut<C, A>::put(co, 1, K - 1, A::mul(Aw, inv));  // row K-1, east entry
       if (eIn) AsmOut<C, A>::put(co, 0, K + 1, A::mul(Ae, inv));  // row K+1, west entry
       if (sIn) AsmOut<C, A>::put(co, 3, K - P, A::mul(As, inv));  // row K-P, north entry
@@ -1130,7 +1161,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_polish(Common cm, Fields fl, Co
             mn = fminf(mn, A::f32(fv));
           }
         }
-        A::st4(fl.fprev + K, A::ld4(fl.f + K));
+        A::st4(fl.fh[st.hslot == 2 ? 0 : st.hslot + 1] + K, A::ld4(fl.f + K));  // f^n into the oldest slot
         A::st4(fl.f + K, fo);
       }
     }
@@ -1158,7 +1189,8 @@ __global__ void __launch_bounds__(kThreads, 3) k_polish(Common cm, Fields fl, Co
       st.clamped = (long long)tot[2];
       st.mass_drift = tot[1] != 0.0 ? fabs(tot[0] - tot[1]) / fabs(tot[1]) : 0.0;
       st.steps += 1;
-      st.has_prev = 1;
+      st.hslot = st.hslot == 2 ? 0 : st.hslot + 1;
+      st.nhist = min(st.nhist + 1, 3);
       if (!(gmin >= 0.0)) st.status = ST_NEGATIVE;
     }
     __syncthreads();
