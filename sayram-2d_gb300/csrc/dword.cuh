@@ -6,10 +6,11 @@
 // form. The building blocks are the published error-free transformations and double-word
 // algorithms:
 //   2Sum (Knuth, TAOCP vol. 2), Fast2Sum (Dekker 1971), Fast2Mult with FMA,
-//   AccurateDWPlusDW (Alg. 6), DWPlusFP (Alg. 4), DWTimesFP3 (Alg. 9) and DWTimesDW3 (Alg. 12) of
-//   M. Joldes, J.-M. Muller, V. Popescu, "Tight and rigorous error bounds for basic building
-//   blocks of double-word arithmetic", ACM TOMS 44(2), 2017 -- relative errors <= 3u^2, 2u^2,
-//   2u^2, 4u^2 with u = 2^-24;
+//   AccurateDWPlusDW (Alg. 6), SloppyDWPlusDW (Alg. 5), DWPlusFP (Alg. 4), DWTimesFP3 (Alg. 9)
+//   and DWTimesDW3 (Alg. 12) of M. Joldes, J.-M. Muller, V. Popescu, "Tight and rigorous error
+//   bounds for basic building blocks of double-word arithmetic", ACM TOMS 44(2), 2017 -- relative
+//   errors <= 3u^2, (3u^2 of the operands' magnitudes), 2u^2, 2u^2, 4u^2 with u = 2^-24;
+//   a fused multiply-add x*y + z built from the same transformations (6u^2 of |x y| + |z|);
 //   the reciprocal is one Newton-Raphson step r = t + t(1 - y t) from the FP32 reciprocal t.
 // Values below ~2^-100 lose low-part bits to FP32 underflow; the solver only needs them to
 // absolute accuracy.
@@ -61,8 +62,9 @@ SG_HD dw dw_add(dw x, dw y) {
   return fast2sum(v.hi, w);
 }
 
-// SloppyDWPlusDW (Alg. 5 of Joldes, Muller, Popescu 2017): fewer operations; its relative error
-// stays within ~3u^2 when x and y have the same sign (no cancellation), the only use here.
+// SloppyDWPlusDW (Alg. 5 of Joldes, Muller, Popescu 2017): fewer operations. Its error is
+// within ~3u^2 (|x| + |y|) for any signs, and so within ~3u^2 of the result when x and y have the
+// same sign (no cancellation).
 SG_HD dw dw_add_same(dw x, dw y) {
   const dw s = two_sum(x.hi, y.hi);
   const float v = x.lo + y.lo;
@@ -72,6 +74,18 @@ SG_HD dw dw_add_same(dw x, dw y) {
 
 SG_HD dw dw_neg(dw x) { return dw{-x.hi, -x.lo}; }
 SG_HD dw dw_sub(dw x, dw y) { return dw_add(x, dw_neg(y)); }
+
+// x*y + z in one renormalisation: the exact product of the high parts (Fast2Mult), its low part
+// and the cross terms folded by FMA, then 2Sum with z's high part. Error within 6u^2 (|x y| +
+// |z|): enough wherever the accuracy needed is relative to the operands' magnitudes rather than
+// to a result that cancels (x.lo*y.lo, below u^2 |x y|, is left out).
+SG_HD dw dw_fma(dw x, dw y, dw z) {
+  const dw p = two_prod(x.hi, y.hi);
+  const float t = fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, p.lo));
+  const dw s = two_sum(p.hi, z.hi);
+  const float w = (t + z.lo) + s.lo;
+  return fast2sum(s.hi, w);
+}
 
 // DWPlusFP
 SG_HD dw dw_add_f(dw x, float y) {

@@ -107,6 +107,7 @@ struct Kry {
 // ------------------------------------------------------------------------------ arithmetic
 struct F64A {
   using V = double;
+  static constexpr int kAsmBlocks = 4;  // k_assemble: resident blocks (64 registers)
   __device__ static V ld(const double* p, long long i) { return p[i]; }
   __device__ static void st(double* p, long long i, V v) { p[i] = v; }
   __device__ static Q4<V> ld4(const double* p) { return sg::ld4(p); }
@@ -166,6 +167,7 @@ struct F64A {
 
 struct DWA {
   using V = dw;
+  static constexpr int kAsmBlocks = 5;  // k_assemble: latency bound, 5 resident blocks (48 registers)
   __device__ static V ld(const double* p, long long i) {
     const float2 q = reinterpret_cast<const float2*>(p)[i];
     return dw{q.x, q.y};
@@ -180,29 +182,31 @@ struct DWA {
     reinterpret_cast<float4*>(p)[0] = make_float4(q.a[0].hi, q.a[0].lo, q.a[1].hi, q.a[1].lo);
     reinterpret_cast<float4*>(p)[1] = make_float4(q.a[2].hi, q.a[2].lo, q.a[3].hi, q.a[3].lo);
   }
-  __device__ static V add(V a, V b) { return dw_add(a, b); }
-  __device__ static V sub(V a, V b) { return dw_sub(a, b); }
+  // Sums and multiply-adds are accurate to a few u^2 of their operands' magnitudes (SloppyDWPlusDW,
+  // dw_fma), which is the accuracy every use needs: matrix entries against their forward-error
+  // scale, residuals against |R|, increments against |f|.
+  __device__ static V add(V a, V b) { return dw_add_same(a, b); }
+  __device__ static V sub(V a, V b) { return dw_add_same(a, dw_neg(b)); }
   __device__ static V mul(V a, V b) { return dw_mul(a, b); }
-  __device__ static V fma(V a, V b, V c) { return dw_add(dw_mul(a, b), c); }
+  __device__ static V fma(V a, V b, V c) { return dw_fma(a, b, c); }
   __device__ static V addp(V a, V b) { return dw_add_same(a, b); }
-  __device__ static V fmap(V a, V b, V c) { return dw_add_same(dw_mul(a, b), c); }
+  __device__ static V fmap(V a, V b, V c) { return dw_fma(a, b, c); }
   __device__ static V addf(V a, float b) { return dw_add_f(a, b); }
   __device__ static V rcp(V a) { return dw_rcp(a); }
   __device__ static V div(V a, V b) { return dw_div(a, b); }
   __device__ static V abs(V a) { return dw_abs(a); }
   __device__ static V neg(V a) { return dw_neg(a); }
-  // as F64A::start. The increments are small against f, so they are formed in FP32 (differences
-  // of the hi parts are exact when the states are within a factor of 2) and added to f in
-  // double-word; the starting point only steers the iteration, the converged answer does not
-  // depend on it
+  // as F64A::start, in double-word: with loss rates up to 10 per day an increment is ~10 % of f,
+  // so FP32 increments would leave ~1e-8 of f in the start, above what the cubic achieves; the
+  // starting point only steers the iteration, the converged answer does not depend on it
   __device__ static V start(V D, V f, V h1, V h2, V h3, int n) {
-    const float d1 = (f.hi - h1.hi) + (f.lo - h1.lo);
-    float c = d1;
+    const dw d1 = sub(f, h1);
+    dw c = d1;
     if (n >= 2) {
-      const float d2 = (h1.hi - h2.hi) + (h1.lo - h2.lo);
-      c = n == 2 ? fmaf(2.0f, d1, -d2) : fmaf(3.0f, d1 - d2, (h2.hi - h3.hi) + (h2.lo - h3.lo));
+      const dw d2 = sub(h1, h2);
+      c = n == 2 ? sub(dw{2.0f * d1.hi, 2.0f * d1.lo}, d2) : add(dw_mul_f(sub(d1, d2), 3.0f), sub(h2, h3));
     }
-    return dw_mul(D, dw_add_f(f, c));
+    return dw_mul(D, add(f, c));
   }
   __device__ static V rsub1(V a) { return dw_add_f(dw_neg(a), 1.0f); }  // 1 - a (DWPlusFP)
   __device__ static V max0(V a) { return dw_max0(a); }
@@ -510,7 +514,7 @@ __device__ __forceinline__ void dirichlet_face(typename A::V aK, typename A::V S
 // One tile of kTX x kTY cells per iteration; vertices and faces are computed once per tile
 // (plus a one-cell halo), in shared memory.
 template <typename C, typename A>
-__global__ void __launch_bounds__(kAsmThreads) k_assemble(Common cm, Geo geo, Fields fl, Coef<C> co) {
+__global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common cm, Geo geo, Fields fl, Coef<C> co) {
   using V = typename A::V;
   count_launch(cm.ctl);
   constexpr int HX = kTX + 2, HY = kTY + 2, VX = kTX + 1, VY = kTY + 1;
@@ -532,6 +536,19 @@ __global__ void __launch_bounds__(kAsmThreads) k_assemble(Common cm, Geo geo, Fi
     const double* h1p = fl.fh[hs];
     const double* h2p = fl.fh[hs == 0 ? 2 : hs - 1];
     const double* h3p = fl.fh[hs == 2 ? 0 : hs + 1];
+    // the per-cell data of step 4 is only needed after three barriers: start its trip to L2 now
+#pragma unroll
+    for (int q = threadIdx.x; q < kTX * kTY; q += kAsmThreads) {
+      const int i = i0 + (q % kTX), j = j0 + (q / kTX);
+      if (i < nx && j < ny) {
+        const long long K = base + (long long)j * P + i;
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(geo.sdiag + K));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(geo.ukk + K));
+        if (nh > 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(h1p + K));
+        if (nh > 1) asm volatile("prefetch.global.L2 [%0];" ::"l"(h2p + K));
+        if (nh > 2) asm volatile("prefetch.global.L2 [%0];" ::"l"(h3p + K));
+      }
+    }
     // 1) f and 1/(f+eps) on the tile plus a one-cell halo
     for (int q = threadIdx.x; q < HX * HY; q += blockDim.x) {
       const int hx = q % HX, hy = q / HX;
@@ -637,7 +654,8 @@ __global__ void __launch_bounds__(kAsmThreads) k_assemble(Common cm, Geo geo, Fi
     __syncthreads();
     // 4) per cell: diagonal in the reference's triplet order, RHS, scaling, scatter
     float rmax = 0.0f;
-    for (int q = threadIdx.x; q < kTX * kTY; q += blockDim.x) {
+#pragma unroll
+    for (int q = threadIdx.x; q < kTX * kTY; q += kAsmThreads) {
       const int cx = q % kTX, cy = q / kTX;
       const int i = i0 + cx, j = j0 + cy;
       if (i >= nx || j >= ny) continue;
