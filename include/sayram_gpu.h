@@ -169,7 +169,9 @@ int sayram_batch_step(sayram_batch b, int nsteps);
 /* The end-to-end form: if f_in is not NULL it first replaces every instance's f from the packed
  * host array (instances concatenated, each alpha-major), then steps, then, if f_out is not
  * NULL, writes every instance's f back the same way. Pinned buffers (sayram_host_alloc) copy
- * fastest. */
+ * fastest. The first guess of each step's solve is extrapolated from the last few states; an
+ * instance whose f_in differs from the state it holds restarts that history, one given back its
+ * own f_out unchanged keeps it (results never depend on the guess, only the iteration count). */
 int sayram_batch_step_host(sayram_batch b, int nsteps, const double* f_in, double* f_out);
 int sayram_batch_get_f(sayram_batch b, int idx, double* f_out);
 int sayram_batch_set_f(sayram_batch b, int idx, const double* f);

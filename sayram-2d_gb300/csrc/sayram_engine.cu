@@ -949,14 +949,13 @@ int sayram_batch_step_host(sayram_batch b, int nsteps, const double* f_in, doubl
   SG_CUDA(cudaSetDevice(b->dev));
   if (f_in) {
     SG_CUDA(cudaMemcpyAsync(b->d_stage, f_in, sizeof(double) * b->nreal, cudaMemcpyHostToDevice, b->stream));
-    // a replaced state has no previous step to extrapolate from
-    SG_CUDA(cudaMemset2DAsync((char*)b->d_st + offsetof(InstState, nhist), sizeof(InstState), 0, sizeof(int),
-                              (size_t)b->n, b->stream));
+    // an instance whose state changed restarts its extrapolation history; one given back its
+    // own current state (a host round trip) keeps it
     b->launch("field_in", [&] {
       if (b->dwm)
-        sg::k_field_in<sg::DWA><<<b->grid_tiles(), 256, 0, b->stream>>>(b->cm, b->fl.f, b->d_stage);
+        sg::k_field_in<sg::DWA><<<b->grid_tiles(), 256, 0, b->stream>>>(b->cm, b->fl.f, b->d_stage, 1);
       else
-        sg::k_field_in<sg::F64A><<<b->grid_tiles(), 256, 0, b->stream>>>(b->cm, b->fl.f, b->d_stage);
+        sg::k_field_in<sg::F64A><<<b->grid_tiles(), 256, 0, b->stream>>>(b->cm, b->fl.f, b->d_stage, 1);
     });
   }
   int rc = b->run_steps(nsteps);
@@ -1814,7 +1813,7 @@ extern "C" int sayram_step_noalloc(const sayram_problem* pd, const sayram_option
   SG_CUDA(cudaGetLastError());
   const int gt = std::max(1, std::min(cm.ntiles, nsm * 8));
   const int gs = std::max(1, std::min(cm.nchunks, nsm * 16));
-  k_field_in<F64A><<<gt, 256, 0, stream>>>(cm, fl.f, f_in);
+  k_field_in<F64A><<<gt, 256, 0, stream>>>(cm, fl.f, f_in, 0);
   const size_t smem_na = (size_t)(kNoAllocChunk + 2 * pitch) * sizeof(double);
   SG_CUDA(cudaFuncSetAttribute(k_bicg1<double, kNoAllocChunk>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_na));
   SG_CUDA(cudaFuncSetAttribute(k_bicg2<double, kNoAllocChunk>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_na));

@@ -402,20 +402,31 @@ __global__ void k_dtable(Common cm, Geo geo, DTab t, const double* xe, const dou
   }
 }
 
-// alpha-major FP64 (packed at hoff) -> padded system order in the wide format (tile grid)
+// alpha-major FP64 (packed at hoff) -> padded system order in the wide format (tile grid).
+// When `restart` is set, a cell given back exactly the double it would be read out as keeps its
+// stored value (in the double-word format that value can carry low bits a double does not), and
+// an instance with any other cell loses its history of earlier states (the extrapolated start
+// restarts from the new state). An instance given back its own state is left exactly as it was.
 template <typename A>
-__global__ void k_field_in(Common cm, double* dst, const double* src) {
+__global__ void k_field_in(Common cm, double* dst, const double* src, int restart) {
   count_launch(cm.ctl);
   for (int t = blockIdx.x, nt_ = n_tiles(cm); t < nt_; t += gridDim.x) {
     const int b = cm.tile_inst[t];
     const InstDev I = cm.inst[b];
     if (!I.enabled) continue;
     const int lt = t - I.tile0, i0 = (lt % I.ntx) * kTX, j0 = (lt / I.ntx) * kTY;
+    int changed = 0;
     for (int q = threadIdx.x; q < kTX * kTY; q += blockDim.x) {
       const int i = i0 + (q / kTY), j = j0 + (q % kTY);  // j fastest: reads contiguous in j
-      if (i < I.nx && j < I.ny)
-        A::st(dst, I.base + (long long)j * I.pitch + i, A::from_d(src[I.hoff + (long long)i * I.ny + j]));
+      if (i < I.nx && j < I.ny) {
+        const long long K = I.base + (long long)j * I.pitch + i;
+        const double v = src[I.hoff + (long long)i * I.ny + j];
+        if (restart && __double_as_longlong(A::to_d(A::ld(dst, K))) == __double_as_longlong(v)) continue;
+        changed = 1;
+        A::st(dst, K, A::from_d(v));
+      }
     }
+    if (__syncthreads_or(restart && changed) && threadIdx.x == 0) cm.st[b].nhist = 0;
   }
 }
 

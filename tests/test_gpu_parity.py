@@ -263,3 +263,34 @@ def test_launch_shape_setter(capi):
     with pytest.raises(RuntimeError, match="blocks_per_sm"):
         ref.set_launch_shape(1024, 0)
     ref.close()
+
+
+@pytest.mark.parametrize("prec", [0, 2])
+def test_step_host_round_trips_keep_history(capi, prec):
+    """Stepping through host buffers that carry each step's output back in gives bit for bit the
+    device-resident trajectory (the extrapolation history is kept); an instance whose state was
+    changed on the host restarts its history, exactly as set_f on that instance does."""
+    probs = cases.batch_problems(4, seed=21, dt=1e-2, lo=30, hi=90)
+    a = capi.Batch(probs, precision=prec)
+    b = capi.Batch(probs, precision=prec)
+    fin = np.concatenate([p.f0.ravel() for p in probs])
+    fout = np.empty_like(fin)
+    a.step_host(1, fin.ctypes.data, fout.ctypes.data)
+    b.step(1)
+    for _ in range(4):
+        fin[:] = fout
+        a.step_host(1, fin.ctypes.data, fout.ctypes.data)
+        b.step(1)
+    for k in range(len(probs)):
+        assert np.array_equal(a.f(k), b.f(k)), k
+    off = probs[0].nx * probs[0].ny
+    n1 = probs[1].nx * probs[1].ny
+    fin[:] = fout
+    fin[off:off + n1] *= 1.0 + 1e-9
+    a.step_host(1, fin.ctypes.data, fout.ctypes.data)
+    b.set_f(1, fin[off:off + n1].reshape(probs[1].nx, probs[1].ny))
+    b.step(1)
+    for k in range(len(probs)):
+        assert np.array_equal(a.f(k), b.f(k)), k
+    a.close()
+    b.close()
