@@ -402,25 +402,34 @@ __global__ void k_dtable(Common cm, Geo geo, DTab t, const double* xe, const dou
   }
 }
 
-// alpha-major FP64 (packed at hoff) -> padded system order in the wide format (tile grid).
+// alpha-major FP64 (packed at hoff) -> padded system order in the wide format, for tiles
+// [t0, t1) of the tile list (t1 < 0: all), one 32x16 tile at a time: read along j (contiguous on the host side), transposed through shared memory,
+// written along i (contiguous on the device side).
 // When `restart` is set, a cell given back exactly the double it would be read out as keeps its
 // stored value (in the double-word format that value can carry low bits a double does not), and
 // an instance with any other cell loses its history of earlier states (the extrapolated start
 // restarts from the new state). An instance given back its own state is left exactly as it was.
 template <typename A>
-__global__ void k_field_in(Common cm, double* dst, const double* src, int restart) {
+__global__ void k_field_in(Common cm, double* dst, const double* src, int restart, int t0, int t1) {
   count_launch(cm.ctl);
-  for (int t = blockIdx.x, nt_ = n_tiles(cm); t < nt_; t += gridDim.x) {
+  __shared__ double tile[kTY][kTX + 1];
+  if (t1 < 0) t1 = n_tiles(cm);
+  for (int t = t0 + blockIdx.x; t < t1; t += gridDim.x) {
     const int b = cm.tile_inst[t];
     const InstDev I = cm.inst[b];
     if (!I.enabled) continue;
     const int lt = t - I.tile0, i0 = (lt % I.ntx) * kTX, j0 = (lt / I.ntx) * kTY;
+    for (int q = threadIdx.x; q < kTX * kTY; q += blockDim.x) {
+      const int i = i0 + (q / kTY), j = j0 + (q % kTY);  // j fastest
+      if (i < I.nx && j < I.ny) tile[j - j0][i - i0] = src[I.hoff + (long long)i * I.ny + j];
+    }
+    __syncthreads();
     int changed = 0;
     for (int q = threadIdx.x; q < kTX * kTY; q += blockDim.x) {
-      const int i = i0 + (q / kTY), j = j0 + (q % kTY);  // j fastest: reads contiguous in j
+      const int i = i0 + (q % kTX), j = j0 + (q / kTX);  // i fastest
       if (i < I.nx && j < I.ny) {
         const long long K = I.base + (long long)j * I.pitch + i;
-        const double v = src[I.hoff + (long long)i * I.ny + j];
+        const double v = tile[j - j0][i - i0];
         if (restart && __double_as_longlong(A::to_d(A::ld(dst, K))) == __double_as_longlong(v)) continue;
         changed = 1;
         A::st(dst, K, A::from_d(v));
@@ -430,19 +439,28 @@ __global__ void k_field_in(Common cm, double* dst, const double* src, int restar
   }
 }
 
+// padded system order in the wide format -> alpha-major FP64, transposed like k_field_in (tiles
+// [t0, t1) of the tile list; t1 < 0: all)
 template <typename A>
-__global__ void k_field_out(Common cm, double* dst, const double* src) {
+__global__ void k_field_out(Common cm, double* dst, const double* src, int t0, int t1) {
   count_launch(cm.ctl);
-  for (int t = blockIdx.x, nt_ = n_tiles(cm); t < nt_; t += gridDim.x) {
+  __shared__ double tile[kTY][kTX + 1];
+  if (t1 < 0) t1 = n_tiles(cm);
+  for (int t = t0 + blockIdx.x; t < t1; t += gridDim.x) {
     const int b = cm.tile_inst[t];
     const InstDev I = cm.inst[b];
     if (!I.enabled) continue;
     const int lt = t - I.tile0, i0 = (lt % I.ntx) * kTX, j0 = (lt / I.ntx) * kTY;
     for (int q = threadIdx.x; q < kTX * kTY; q += blockDim.x) {
-      const int i = i0 + (q / kTY), j = j0 + (q % kTY);
-      if (i < I.nx && j < I.ny)
-        dst[I.hoff + (long long)i * I.ny + j] = A::to_d(A::ld(src, I.base + (long long)j * I.pitch + i));
+      const int i = i0 + (q % kTX), j = j0 + (q / kTX);  // i fastest
+      if (i < I.nx && j < I.ny) tile[j - j0][i - i0] = A::to_d(A::ld(src, I.base + (long long)j * I.pitch + i));
     }
+    __syncthreads();
+    for (int q = threadIdx.x; q < kTX * kTY; q += blockDim.x) {
+      const int i = i0 + (q / kTY), j = j0 + (q % kTY);  // j fastest
+      if (i < I.nx && j < I.ny) dst[I.hoff + (long long)i * I.ny + j] = tile[j - j0][i - i0];
+    }
+    __syncthreads();
   }
 }
 

@@ -265,16 +265,26 @@ def test_launch_shape_setter(capi):
     ref.close()
 
 
+@pytest.mark.parametrize("pinned", [False, True])
 @pytest.mark.parametrize("prec", [0, 2])
-def test_step_host_round_trips_keep_history(capi, prec):
+def test_step_host_round_trips_keep_history(capi, prec, pinned):
     """Stepping through host buffers that carry each step's output back in gives bit for bit the
     device-resident trajectory (the extrapolation history is kept); an instance whose state was
-    changed on the host restarts its history, exactly as set_f on that instance does."""
+    changed on the host restarts its history, exactly as set_f on that instance does. Both
+    pageable and page-locked (sayram_host_alloc) host buffers."""
+    import ctypes
+
     probs = cases.batch_problems(4, seed=21, dt=1e-2, lo=30, hi=90)
     a = capi.Batch(probs, precision=prec)
     b = capi.Batch(probs, precision=prec)
-    fin = np.concatenate([p.f0.ravel() for p in probs])
-    fout = np.empty_like(fin)
+    f0 = np.concatenate([p.f0.ravel() for p in probs])
+    L = capi.load()
+    if pinned:
+        hp = [L.sayram_host_alloc(8 * f0.size) for _ in range(2)]
+        fin, fout = [np.ctypeslib.as_array((ctypes.c_double * f0.size).from_address(h)) for h in hp]
+        fin[:] = f0
+    else:
+        fin, fout = f0.copy(), np.empty_like(f0)
     a.step_host(1, fin.ctypes.data, fout.ctypes.data)
     b.step(1)
     for _ in range(4):
@@ -294,3 +304,6 @@ def test_step_host_round_trips_keep_history(capi, prec):
         assert np.array_equal(a.f(k), b.f(k)), k
     a.close()
     b.close()
+    if pinned:
+        for h in hp:
+            L.sayram_host_free(h)
