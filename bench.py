@@ -226,7 +226,7 @@ BYTES32 = {
 # DRAM bytes per processed cell measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the
 # 256-instance case of the same kernels (profiles/*_dw_256instances.md); traffic grows with the
 # cells processed, so a launch's traffic is this figure times the cells it processed.
-TRAFFIC32 = {"assemble": 164.6, "bicg1": 40.3, "bicg2": 27.9, "resid": 60.9, "polish": 92.9}
+TRAFFIC32 = {"assemble": 168.2, "bicg1": 40.3, "bicg2": 27.9, "resid": 60.9, "polish": 92.9}
 
 
 def kernel_roofline(b, probs, peak, steps=2):
@@ -315,6 +315,28 @@ def run_serving(capi, arrivals, probs, steps, precision, budget_gb):
             "requests_per_s": nreq / wall, "ticks": info["ticks"], "busy_s": info["busy_seconds"],
             "tick_split_s": {k: info[k + "_seconds"] for k in ("admit", "lists", "step", "collect")},
             "min_f": min_f, "not_converged": not_conv, "device_gb": info["device_bytes"] / 1e9}
+
+
+def run_1024(capi):
+    """The single-instance 1024 x 1024 configuration (dt = 1e-2): device-timed steps/s of the
+    plain FP64 drop-in and of the double-word path, and their agreement."""
+    p = cases.synthetic_problem(1024, 1024, DT, seed=11)
+    out = {"grid": "1024 x 1024", "dt": DT}
+    fs = {}
+    for name, prec in (("fp64", capi.FP64), ("fp32_refine_dw", capi.FP32_REFINE_DW)):
+        s = capi.Solver(p, precision=prec)
+        s.step(4)
+        s.record_event(0)
+        s.step(10)
+        s.record_event(1)
+        ms = s.elapsed_ms(0, 1) / 10
+        st = s.get_stats()
+        fs[name] = s.f()
+        out[name] = {"steps_per_s": 1e3 / ms, "ms_per_step": ms, "iterations_last_step": st["iterations"],
+                     "rel_residual": st["rel_residual"]}
+        s.close()
+    out["rel_err_dw_vs_fp64"] = float(np.linalg.norm(fs["fp32_refine_dw"] - fs["fp64"]) / np.linalg.norm(fs["fp64"]))
+    return out
 
 
 def run_ours(a):
@@ -437,6 +459,7 @@ def run_ours(a):
                               "sample": f"first {ns} instances, 2 steps each, one sayram_create per instance"}
         line["speedup_vs_plain_fp64"] = value / plain
         line["cpu_baseline"] = cpu_baseline_single(a.seed, a.instances, a.cpu_seconds)
+        line["config_1024"] = run_1024(capi)
     else:
         b.close()
     if a.serve_requests > 0:

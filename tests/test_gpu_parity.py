@@ -182,6 +182,28 @@ def test_large_grid_properties(capi, oracle):
     assert f.min() >= 0.0 and st["mass_drift"] <= 1e-9
 
 
+def test_config1_size_1024(capi, oracle):
+    """The single-instance configuration at full size (1024 x 1024, dt = 1e-2): one step of the
+    FP64 path against SuperLU, then size-independent properties over further steps -- the
+    double-word path within 1e-8 of the FP64 path, conservation, positivity, residual."""
+    p = cases.synthetic_problem(1024, 1024, 1e-2, seed=11)
+    s64 = capi.Solver(p, precision=capi.FP64)
+    s64.step(1)
+    ref = oracle.step(p, None, 1, solver="splu")
+    assert rel(s64.f(), ref) <= TOL64, rel(s64.f(), ref)
+    sdw = capi.Solver(p, precision=capi.FP32_REFINE_DW)
+    sdw.step(1)
+    s64.step(3)
+    sdw.step(3)
+    f64, fdw = s64.f(), sdw.f()
+    assert rel(fdw, f64) <= TOL32, rel(fdw, f64)
+    for st, tol in ((s64.get_stats(), 1e-12), (sdw.get_stats(), 1e-11)):
+        assert st["rel_residual"] <= tol and st["mass_drift"] <= 1e-9 and st["status"] == 0
+    assert f64.min() >= 0.0 and fdw.min() >= 0.0
+    s64.close()
+    sdw.close()
+
+
 def test_tiny_magnitudes(capi, oracle):
     """f0 and the Dirichlet values scaled by 2^-100 (~1e-30): the FP32 inner solves see residuals
     scaled by a power of two near max|R| (no FP32 underflow), so every mode still matches the
