@@ -350,7 +350,8 @@ int sayram_batch_s::alloc_storage(long long cells, int slots, int chunks_cap, in
   SG_ALLOC(d_part, 4LL * chunks_cap);
   SG_ALLOC(d_stage, stage_cap);
   cell_arrays.clear();
-  double** geos[9] = {&geo.aAx, &geo.aBx, &geo.Sx, &geo.aAy, &geo.aBy, &geo.Sy, &geo.ukk, &geo.sdiag, &geo.G};
+  double** geos[10] = {&geo.aAx, &geo.aBx, &geo.Sx, &geo.aAy, &geo.aBy, &geo.Sy, &geo.ukk, &geo.sdiag, &geo.G,
+                       &geo.decay};
   for (auto g : geos) {
     SG_ALLOC(*g, cells);
     cell_arrays.push_back({*g, 8});
@@ -1254,7 +1255,7 @@ void sayram_batch_destroy(sayram_batch b) { delete b; }
 size_t sayram_instance_bytes(int nx, int ny, int precision) {
   const long long pitch = round_up(nx, 4);
   const long long cells = round_up((long long)(ny + 2) * pitch, 32);
-  const long long per = 18 * 8 + (precision != SAYRAM_FP64 ? 8 * 4 + 8 * 4 : 4 * 8 + 8 * 8) + 8;
+  const long long per = 19 * 8 + (precision != SAYRAM_FP64 ? 8 * 4 + 8 * 4 : 4 * 8 + 8 * 8) + 8;
   return (size_t)(cells * per + 4096);
 }
 

@@ -25,6 +25,7 @@ namespace sg {
 struct Geo {  // per-cell face factors (time independent while the coefficients are)
   double *aAx, *aBx, *Sx, *aAy, *aBy, *Sy, *ukk, *sdiag;
   double* G;  // G per cell, FP64 (kept so that new D fields can re-derive the face factors)
+  double* decay;  // 1 / (1 + dt/tau): one step of pure loss (extrapolated start); null: 1
 };
 
 struct Common {
@@ -124,16 +125,20 @@ struct F64A {
   __device__ static V div(V a, V b) { return a / b; }
   __device__ static V abs(V a) { return fabs(a); }
   __device__ static V neg(V a) { return -a; }
-  // D g with g the polynomial extrapolation in time through f and n earlier states (n = 1..3):
-  // f + d1, f + 2 d1 - d2, f + 3 (d1 - d2) + d3 with d1 = f - h1, d2 = h1 - h2, d3 = h2 - h3
-  __device__ static V start(V D, V f, V h1, V h2, V h3, int n) {
-    const double d1 = f - h1;
+  // D g with g the polynomial extrapolation in time through f and n earlier states (n = 1..3) of
+  // the loss-compensated sequence c_k = h_k r^k (r = 1/(1 + dt/tau), one step of pure loss), times
+  // r: g = r (c0 + d1), r (c0 + 2 d1 - d2), r (c0 + 3 (d1 - d2) + d3) with d1 = c0 - c1,
+  // d2 = c1 - c2, d3 = c2 - c3, c0 = f. Exact for pure loss; r = 1 gives the plain polynomial.
+  __device__ static V start(V D, V f, V h1, V h2, V h3, int n, V r) {
+    const double c1 = h1 * r;
+    const double d1 = f - c1;
     double c = d1;
     if (n >= 2) {
-      const double d2 = h1 - h2;
-      c = n == 2 ? 2.0 * d1 - d2 : 3.0 * (d1 - d2) + (h2 - h3);
+      const double r2 = r * r, c2 = h2 * r2;
+      const double d2 = c1 - c2;
+      c = n == 2 ? 2.0 * d1 - d2 : 3.0 * (d1 - d2) + (c2 - h3 * (r2 * r));
     }
-    return D * (f + c);
+    return D * (r * (f + c));
   }
   __device__ static V rsub1(V a) { return 1.0 - a; }
   __device__ static V max0(V a) { return fmax(a, 0.0); }
@@ -199,14 +204,17 @@ struct DWA {
   // as F64A::start, in double-word: with loss rates up to 10 per day an increment is ~10 % of f,
   // so FP32 increments would leave ~1e-8 of f in the start, above what the cubic achieves; the
   // starting point only steers the iteration, the converged answer does not depend on it
-  __device__ static V start(V D, V f, V h1, V h2, V h3, int n) {
-    const dw d1 = sub(f, h1);
+  __device__ static V start(V D, V f, V h1, V h2, V h3, int n, V r) {
+    const dw c1 = dw_mul(h1, r);
+    const dw d1 = sub(f, c1);
     dw c = d1;
     if (n >= 2) {
-      const dw d2 = sub(h1, h2);
-      c = n == 2 ? sub(dw{2.0f * d1.hi, 2.0f * d1.lo}, d2) : add(dw_mul_f(sub(d1, d2), 3.0f), sub(h2, h3));
+      const dw r2 = dw_mul(r, r), c2 = dw_mul(h2, r2);
+      const dw d2 = sub(c1, c2);
+      c = n == 2 ? sub(dw{2.0f * d1.hi, 2.0f * d1.lo}, d2)
+                 : add(dw_mul_f(sub(d1, d2), 3.0f), sub(c2, dw_mul(h3, dw_mul(r2, r))));
     }
-    return dw_mul(D, add(f, c));
+    return dw_mul(D, dw_mul(r, add(f, c)));
   }
   __device__ static V rsub1(V a) { return dw_add_f(dw_neg(a), 1.0f); }  // 1 - a (DWPlusFP)
   __device__ static V max0(V a) { return dw_max0(a); }
@@ -320,7 +328,9 @@ __global__ void k_setup(Common cm, Geo geo, double* f, const double* stage, cons
       // UKK = G * (dx*dy/dt); diagonal UKK*(1 + dt/tau) (Solver.cc:190-199, Mesh.h:61-63)
       const double ukk = __dmul_rn(g, __ddiv_rn(__dmul_rn(dx, dy), I.dt));
       A::st(geo.ukk, K, A::from_d(ukk));
-      A::st(geo.sdiag, K, A::from_d(__dmul_rn(ukk, __dadd_rn(1.0, __dmul_rn(I.dt, itau[c])))));
+      const double lossd = __dadd_rn(1.0, __dmul_rn(I.dt, itau[c]));
+      A::st(geo.sdiag, K, A::from_d(__dmul_rn(ukk, lossd)));
+      if (geo.decay) A::st(geo.decay, K, A::from_d(__ddiv_rn(1.0, lossd)));
     }
     if (mask & 32) A::st(f, K, A::from_d(f0[c]));
   }
@@ -576,6 +586,7 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
         if (nh > 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(h1p + K));
         if (nh > 1) asm volatile("prefetch.global.L2 [%0];" ::"l"(h2p + K));
         if (nh > 2) asm volatile("prefetch.global.L2 [%0];" ::"l"(h3p + K));
+        if (nh > 0 && geo.decay) asm volatile("prefetch.global.L2 [%0];" ::"l"(geo.decay + K));
       }
     }
     // 1) f and 1/(f+eps) on the tile plus a one-cell halo
@@ -718,7 +729,7 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
         y0 = A::mul(D, fK);
       } else {
         const V h1 = A::ld(h1p, K), h2 = nh >= 2 ? A::ld(h2p, K) : h1, h3 = nh >= 3 ? A::ld(h3p, K) : h2;
-        y0 = A::start(D, fK, h1, h2, h3, nh);
+        y0 = A::start(D, fK, h1, h2, h3, nh, geo.decay ? A::ld(geo.decay, K) : A::k(1.0));
       }
       A::st(fl.y64[cm.st[b].ycur], K, y0);
       if (wIn) AsmOut<C, A>::put(co, 1, K - 1, A::mul(Aw, inv));  // row K-1, east entry
