@@ -1809,7 +1809,8 @@ extern "C" int sayram_step_noalloc(const sayram_problem* pd, const sayram_option
     *a = lay.take<double>(kNoAllocCells);
     if (!*a) return fail(SAYRAM_ERR_ARG, "cell arrays exceed the scratch");
   }
-  fl.fh[1] = fl.fh[2] = fl.fh[0];  // one history buffer: linear extrapolation (Common::hist_cap = 1)
+  fl.fh[1] = fl.fh[2] = fl.fh[0];  // one history buffer: linear extrapolation (Common::hist_cap = 1);
+                                    // geo.decay stays null (no loss compensation on this path)
   unsigned char* used_end = lay.cur;
 
   // ---- every call starts from zero: padding, pad rows, state and counters must be 0

@@ -7,7 +7,7 @@
 //   k_resid      outer residual r = R - A~ y (adds the last Krylov correction first)
 //   k_bicg1/2/3  one BiCGSTAB iteration in T precision (FP64 or FP32) with fused SpMV + dots
 //   k_polish     positivity polish y' = R + (I - A~) y+, f = y'/D, min / clamp / mass checks
-//   k_field_*    alpha-major FP64 <-> padded system order copies for get_f / set_f
+//   k_field_*    alpha-major FP64 <-> padded system order transposes for the host-buffer step
 //
 // The assembly, residual, polish and state are written once over an arithmetic policy A:
 //   F64A  IEEE binary64 (the FP64 drop-in and the FP32 + FP64-residual mode)
@@ -721,9 +721,9 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
       A::st(fl.invD, K, inv);
       A::st(fl.R, K, Rv);
       A::st(fl.colsum, K, A::addp(sd, dir));
-      // start the solve from the polynomial extrapolation in time through f^n and up to three
-      // earlier states (only the starting point of the iteration; the converged answer does not
-      // depend on it)
+      // start the solve from the loss-compensated polynomial extrapolation in time through f^n and
+      // up to three earlier states (only the starting point of the iteration; the converged
+      // answer does not depend on it)
       V y0;
       if (nh == 0) {
         y0 = A::mul(D, fK);
