@@ -264,18 +264,24 @@ def kernel_roofline(b, probs, peak, steps=2):
     return roof, out
 
 
+SERVE_POOL = 1024  # distinct request problems at most; longer streams reuse them in turn
+
+
 def serving_requests(nreq, rate, seed):
     """Seeded request stream: Poisson arrivals at `rate`, n log-uniform in [32, 512] (n x n grid),
-    steps log-uniform in [10, 2000], seeded D fields, rho and tau per request."""
+    steps log-uniform in [10, 2000], seeded D fields, rho and tau per request. Streams longer
+    than SERVE_POOL requests draw their problems from SERVE_POOL distinct ones in turn (each
+    request keeps its own step count and arrival time), which bounds host memory."""
     rng = np.random.default_rng([seed, 4242])
     arrivals = np.cumsum(rng.exponential(1.0 / rate, size=nreq))
     n = np.rint(np.exp(rng.uniform(np.log(32), np.log(512), size=nreq))).astype(int)
     steps = np.rint(np.exp(rng.uniform(np.log(10), np.log(2000), size=nreq))).astype(int)
-    probs = []
-    for k in range(nreq):
+    pool = []
+    for k in range(min(nreq, SERVE_POOL)):
         r = np.random.default_rng([seed, k, 99])
-        probs.append(cases.synthetic_problem(int(n[k]), int(n[k]), DT, seed=seed * 104729 + k,
-                                             tau=float(10.0 ** r.uniform(-1, 1)), rho=float(r.uniform(-0.9, 0.9))))
+        pool.append(cases.synthetic_problem(int(n[k]), int(n[k]), DT, seed=seed * 104729 + k,
+                                            tau=float(10.0 ** r.uniform(-1, 1)), rho=float(r.uniform(-0.9, 0.9))))
+    probs = [pool[k % len(pool)] for k in range(nreq)]
     return arrivals, probs, steps
 
 
@@ -474,6 +480,27 @@ def run_ours(a):
     print(json.dumps(line))
 
 
+def run_serve_only(a):
+    """Only the serving measurement (one JSON line): both precisions, the request stream of
+    --serve-requests / --serve-rate / --serve-budget-gb."""
+    from sayram2d_gb300 import build, capi
+
+    build.build()
+    capi.load()
+    arr, sprobs, ssteps = serving_requests(a.serve_requests, a.serve_rate, a.seed)
+    cfg = (f"{a.serve_requests} Poisson requests at {a.serve_rate}/s, n~logU[32,512] (n x n), "
+           f"steps~logU[10,2000], dt={DT} day, HBM budget {a.serve_budget_gb} GB, "
+           f"{min(a.serve_requests, SERVE_POOL)} distinct problems")
+    line = {"metric": "serving latency p50/p99 (ms) and throughput", "unit": "ms", "n_gpus": 1,
+            "data": "synthetic (seeded)", "config": {"workload": cfg}}
+    line["serving"] = {"precision": "fp32_refine_dw",
+                       **run_serving(capi, arr, sprobs, ssteps, capi.FP32_REFINE_DW, a.serve_budget_gb)}
+    if not a.quick:
+        line["serving_plain_fp64"] = {"precision": "fp64",
+                                      **run_serving(capi, arr, sprobs, ssteps, capi.FP64, a.serve_budget_gb)}
+    print(json.dumps(line))
+
+
 def main():
     a = parse()
     if a.gpus != 1 or int(os.environ.get("WORLD_SIZE", "1")) != 1:
@@ -483,6 +510,8 @@ def main():
         a.warmup = 3
     if a.impl == "reference":
         run_reference(a)
+    elif a.serve_only:
+        run_serve_only(a)
     else:
         run_ours(a)
 
