@@ -745,6 +745,12 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
 }
 
 // ------------------------------------------------------------------------------ streaming helpers
+// Resident blocks per SM the Krylov kernels are compiled for: in FP32, 6 (registers capped at
+// 40; their shared memory allows 6, and the extra blocks in flight raised their bandwidth by
+// 8-14 %); in FP64, 4 (a cap of 40 registers spills).
+template <typename T>
+constexpr int krylov_blocks() { return sizeof(T) == 4 ? 6 : 4; }
+
 // Locates 4-cell group g (0 .. CH/(4*kThreads) - 1) of this thread in chunk c (CH cells) of
 // instance I.
 struct Slot {
@@ -883,7 +889,7 @@ __device__ __forceinline__ Q4<typename A::V> stencilW(const Q4<typename A::V>& c
 // r = R - A~ (y + x) in the wide arithmetic; writes y + x to the other y buffer and r (T precision).
 // Partials: ||r||^2, ||R||^2.
 template <typename T, typename C, typename A, int CH>
-__global__ void __launch_bounds__(kThreads, 3) k_resid(Common cm, Fields fl, Coef<C> co, Kry<T> kr,
+__global__ void __launch_bounds__(kThreads, 4) k_resid(Common cm, Fields fl, Coef<C> co, Kry<T> kr,
                                                         double tol, double inner_tol, int max_refine) {
   using V = typename A::V;
   count_launch(cm.ctl);
@@ -979,7 +985,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_resid(Common cm, Fields fl, Coe
 //     v = A~ p;  partial (r^, v). p is computed once per cell into shared memory (chunk plus one
 //     row above and below) and the stencil reads it there.
 template <typename T, int CH>
-__global__ void __launch_bounds__(kThreads) k_bicg1(Common cm, Coef<T> co, Kry<T> kr) {
+__global__ void __launch_bounds__(kThreads, krylov_blocks<T>()) k_bicg1(Common cm, Coef<T> co, Kry<T> kr) {
   count_launch(cm.ctl);
   extern __shared__ __align__(16) unsigned char smraw[];
   T* sm = reinterpret_cast<T*>(smraw);
@@ -1051,7 +1057,7 @@ __global__ void __launch_bounds__(kThreads) k_bicg1(Common cm, Coef<T> co, Kry<T
 
 // k2: s = r - alpha v;  t = A~ s;  partials (t, s), (t, t). s is staged like p in k1.
 template <typename T, int CH>
-__global__ void __launch_bounds__(kThreads) k_bicg2(Common cm, Coef<T> co, Kry<T> kr) {
+__global__ void __launch_bounds__(kThreads, krylov_blocks<T>()) k_bicg2(Common cm, Coef<T> co, Kry<T> kr) {
   count_launch(cm.ctl);
   extern __shared__ __align__(16) unsigned char smraw[];
   T* sm = reinterpret_cast<T*>(smraw);
@@ -1106,7 +1112,7 @@ __global__ void __launch_bounds__(kThreads) k_bicg2(Common cm, Coef<T> co, Kry<T
 // k3: x += alpha p + omega s (x starts at 0 on the first iteration of a solve);
 //     r = s - omega t;  partials (r^, r), (r, r); convergence test.
 template <typename T, int CH>
-__global__ void __launch_bounds__(kThreads) k_bicg3(Common cm, Kry<T> kr, int max_iters) {
+__global__ void __launch_bounds__(kThreads, krylov_blocks<T>()) k_bicg3(Common cm, Kry<T> kr, int max_iters) {
   count_launch(cm.ctl);
   for_active_chunks(cm, [&](int b_) { return cm.st[b_].inner_active != 0; }, [&](int c) {
     const int b = cm.chunk_inst[c];
