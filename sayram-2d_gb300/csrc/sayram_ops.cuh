@@ -560,8 +560,10 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
   __shared__ V fS[HY][HX];
   __shared__ V iS[HY][HX];
   __shared__ V vS[VY][VX];
-  __shared__ V xL[kTY][VX], xR[kTY][VX], xB[kTY][VX];  // x-faces: left/right outflow, R part
-  __shared__ V yB[VY][kTX], yT[VY][kTX], yR[VY][kTX];  // y-faces: below/above outflow, R part
+  // x-faces: outflow to the left / right cell; y-faces: to the cell below / above. On a Dirichlet
+  // side the slot of the missing outside cell holds the face's RHS part instead.
+  __shared__ V xL[kTY][VX], xR[kTY][VX];
+  __shared__ V yB[VY][kTX], yT[VY][kTX];
   const V zero = A::k(0.0);
   for (int t = blockIdx.x, nt_ = n_tiles(cm); t < nt_; t += gridDim.x) {
     const int b = cm.tile_inst[t];
@@ -660,9 +662,8 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
                             iS[ry + 1][vx], &aL, &bm);
         }
       }
-      xL[ry][vx] = aL;
-      xR[ry][vx] = aR;
-      xB[ry][vx] = bm;
+      xL[ry][vx] = Iv == 0 ? bm : aL;
+      xR[ry][vx] = Iv == nx ? bm : aR;
     }
     // 3b) y-faces (vertex row Jv between cells Jv-1 and Jv)
     for (int q = threadIdx.x; q < VY * kTX; q += blockDim.x) {
@@ -687,9 +688,8 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
                             iS[vy][cx + 1], &aB, &bm);
         }
       }
-      yB[vy][cx] = aB;
-      yT[vy][cx] = aT;
-      yR[vy][cx] = bm;
+      yB[vy][cx] = Jv == 0 ? bm : aB;
+      yT[vy][cx] = Jv == ny ? bm : aT;
     }
     __syncthreads();
     // 4) per cell: diagonal in the reference's triplet order, RHS, scaling, scatter
@@ -708,10 +708,10 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
       if (eIn) D = A::addp(D, Ae);
       if (sIn) D = A::addp(D, As);
       if (nIn) D = A::addp(D, An);
-      if (!wIn && I.bc[XMIN] == DIRICHLET) { D = A::addp(D, Aw); dir = A::addp(dir, Aw); Rv = A::addp(Rv, xB[cy][cx]); }
-      if (!eIn && I.bc[XMAX] == DIRICHLET) { D = A::addp(D, Ae); dir = A::addp(dir, Ae); Rv = A::addp(Rv, xB[cy][cx + 1]); }
-      if (!sIn && I.bc[YMIN] == DIRICHLET) { D = A::addp(D, As); dir = A::addp(dir, As); Rv = A::addp(Rv, yR[cy][cx]); }
-      if (!nIn && I.bc[YMAX] == DIRICHLET) { D = A::addp(D, An); dir = A::addp(dir, An); Rv = A::addp(Rv, yR[cy + 1][cx]); }
+      if (!wIn && I.bc[XMIN] == DIRICHLET) { D = A::addp(D, Aw); dir = A::addp(dir, Aw); Rv = A::addp(Rv, xL[cy][cx]); }
+      if (!eIn && I.bc[XMAX] == DIRICHLET) { D = A::addp(D, Ae); dir = A::addp(dir, Ae); Rv = A::addp(Rv, xR[cy][cx + 1]); }
+      if (!sIn && I.bc[YMIN] == DIRICHLET) { D = A::addp(D, As); dir = A::addp(dir, As); Rv = A::addp(Rv, yB[cy][cx]); }
+      if (!nIn && I.bc[YMAX] == DIRICHLET) { D = A::addp(D, An); dir = A::addp(dir, An); Rv = A::addp(Rv, yT[cy + 1][cx]); }
       const V sd = A::ld(geo.sdiag, K);
       D = A::addp(D, sd);
       const V fK = fS[cy + 1][cx + 1];

@@ -329,3 +329,23 @@ def test_step_host_round_trips_keep_history(capi, prec, pinned):
     if pinned:
         for h in hp:
             L.sayram_host_free(h)
+
+
+@pytest.mark.parametrize("prec", [0, 1, 2])
+def test_stiff_steps(capi, oracle, prec):
+    """Stiff settings: dt = 1 day (100 times the benchmark's), loss time 0.01 to 100 days, cross
+    terms at |rho| = 0.99; six steps, so the extrapolated start runs at every order and through
+    fast loss. Each mode still meets its tolerance against the oracle, stays non-negative and
+    conserves mass."""
+    probs = [cases.synthetic_problem(40 + 7 * k, 36 + 5 * k, 1.0, seed=90 + k, tau=tau, rho=rho)
+             for k, (tau, rho) in enumerate(((0.01, 0.99), (100.0, -0.99), (0.3, 0.5), (None, -0.9)))]
+    b = capi.Batch(probs, precision=prec)
+    b.step(6)
+    tol = TOL64 if prec == 0 else TOL32
+    for k, p in enumerate(probs):
+        ref = oracle.step(p, None, 6)
+        f = b.f(k)
+        st = b.stats(k)
+        assert rel(f, ref) <= tol, (prec, k, rel(f, ref))
+        assert f.min() >= 0.0 and st["status"] == 0 and st["mass_drift"] <= 1e-8, (prec, k, st)
+    b.close()
