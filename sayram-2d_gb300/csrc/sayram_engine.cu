@@ -356,7 +356,8 @@ int sayram_batch_s::alloc_storage(long long cells, int slots, int chunks_cap, in
     SG_ALLOC(*g, cells);
     cell_arrays.push_back({*g, 8});
   }
-  double** fs[9] = {&fl.f, &fl.fh[0], &fl.fh[1], &fl.fh[2], &fl.invD, &fl.R, &fl.colsum, &fl.y64[0], &fl.y64[1]};
+  double** fs[10] = {&fl.f, &fl.fh[0], &fl.fh[1], &fl.fh[2], &fl.fh[3], &fl.invD, &fl.R, &fl.colsum, &fl.y64[0],
+                      &fl.y64[1]};
   for (auto f : fs) {
     SG_ALLOC(*f, cells);
     cell_arrays.push_back({*f, 8});
@@ -399,7 +400,7 @@ int sayram_batch_s::alloc_storage(long long cells, int slots, int chunks_cap, in
   cm.dirv = d_dirv;
   cm.part = d_part;
   cm.dyn = d_dyn;
-  cm.hist_cap = 3;
+  cm.hist_cap = sg::kHist;
   return SAYRAM_OK;
 }
 
@@ -814,19 +815,19 @@ int sayram_batch_s::set_dtable(int idx, const sayram_dtable* t) {
 int sayram_batch_s::autotune(int steps, int* best_chunk, int* best_grid) {
   if (steps < 1) steps = 1;
   SG_CUDA(cudaSetDevice(dev));
-  double* snap = nullptr;  // f, fh[0], fh[1], fh[2]
-  if (cudaMalloc(&snap, sizeof(double) * 4 * ncell) != cudaSuccess) {
+  double* snap = nullptr;  // f and the history states
+  if (cudaMalloc(&snap, sizeof(double) * (1 + sg::kHist) * ncell) != cudaSuccess) {
     cudaGetLastError();
     return fail(SAYRAM_ERR_OOM, "autotune: no room for the state snapshot");
   }
-  double* const saved[4] = {fl.f, fl.fh[0], fl.fh[1], fl.fh[2]};
+  double* const saved[1 + sg::kHist] = {fl.f, fl.fh[0], fl.fh[1], fl.fh[2], fl.fh[3]};
   std::vector<InstState> hs(cap_slots);
-  for (int k = 0; k < 4; ++k)
+  for (int k = 0; k < 1 + sg::kHist; ++k)
     SG_CUDA(cudaMemcpyAsync(snap + k * ncell, saved[k], sizeof(double) * ncell, cudaMemcpyDeviceToDevice, stream));
   SG_CUDA(cudaMemcpyAsync(hs.data(), d_st, sizeof(InstState) * cap_slots, cudaMemcpyDeviceToHost, stream));
   SG_CUDA(cudaStreamSynchronize(stream));
   auto restore = [&]() -> int {
-    for (int k = 0; k < 4; ++k)
+    for (int k = 0; k < 1 + sg::kHist; ++k)
       SG_CUDA(cudaMemcpyAsync(saved[k], snap + k * ncell, sizeof(double) * ncell, cudaMemcpyDeviceToDevice, stream));
     SG_CUDA(cudaMemcpyAsync(d_st, hs.data(), sizeof(InstState) * cap_slots, cudaMemcpyHostToDevice, stream));
     SG_CUDA(cudaStreamSynchronize(stream));
@@ -1255,7 +1256,7 @@ void sayram_batch_destroy(sayram_batch b) { delete b; }
 size_t sayram_instance_bytes(int nx, int ny, int precision) {
   const long long pitch = round_up(nx, 4);
   const long long cells = round_up((long long)(ny + 2) * pitch, 32);
-  const long long per = 19 * 8 + (precision != SAYRAM_FP64 ? 8 * 4 + 8 * 4 : 4 * 8 + 8 * 8) + 8;
+  const long long per = 20 * 8 + (precision != SAYRAM_FP64 ? 8 * 4 + 8 * 4 : 4 * 8 + 8 * 8) + 8;
   return (size_t)(cells * per + 4096);
 }
 
@@ -1809,7 +1810,7 @@ extern "C" int sayram_step_noalloc(const sayram_problem* pd, const sayram_option
     *a = lay.take<double>(kNoAllocCells);
     if (!*a) return fail(SAYRAM_ERR_ARG, "cell arrays exceed the scratch");
   }
-  fl.fh[1] = fl.fh[2] = fl.fh[0];  // one history buffer: linear extrapolation (Common::hist_cap = 1);
+  fl.fh[1] = fl.fh[2] = fl.fh[3] = fl.fh[0];  // one history buffer: linear extrapolation (hist_cap = 1);
                                     // geo.decay stays null (no loss compensation on this path)
   unsigned char* used_end = lay.cur;
 

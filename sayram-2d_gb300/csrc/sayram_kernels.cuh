@@ -60,8 +60,8 @@ struct InstState {
   int ycur, pcur, outer_active, inner_active;
   int restart, fresh, has_x, iters;
   int iters_total, refines, status;
-  int nhist;               // earlier states held in the history buffers (0..3; extrapolated start)
-  int hslot;               // history buffer holding f^(n-1); f^(n-2), f^(n-3) are in the two before it
+  int nhist;               // earlier states held in the history buffers (extrapolated start)
+  int hslot;               // history buffer holding f^(n-1); f^(n-2), ... are in the ones before it
   unsigned int rmax_bits;  // bits of max |R| over the instance (non-negative float; atomicMax order)
   unsigned int cnt[PH_COUNT];
 };

@@ -49,7 +49,7 @@ struct Common {
   unsigned long long h_outer, h_inner;  // cudaGraphConditionalHandle of the two WHILE nodes
   int use_cond;
   int guard_refine, guard_iters;  // hard caps on loop trips, whatever the bookkeeping says
-  int hist_cap;  // history depth used for the starting point (3; 1 when the three buffers alias)
+  int hist_cap;  // history depth used for the starting point (kHist; 1 when the buffers alias)
 };
 
 __device__ __forceinline__ int n_chunks(const Common& cm) { return cm.dyn ? cm.dyn[0] : cm.nchunks; }
@@ -90,9 +90,11 @@ struct Coef {  // row-oriented scaled off-diagonal magnitudes (hi parts when spl
   float *lw, *le, *ls, *ln;  // low parts for the FP32-split storage (null for FP64)
 };
 
+constexpr int kHist = 4;  // earlier states kept for the extrapolated start of each solve
+
 struct Fields {
   double* f;       // state, padded system order
-  double* fh[3];   // earlier states f^(n-1), f^(n-2), f^(n-3), rotated per instance (InstState::hslot)
+  double* fh[kHist];  // earlier states f^(n-1) .. f^(n-4), rotated per instance (InstState::hslot)
   double* invD;    // 1 / diag(M)
   double* R;       // right-hand side
   double* colsum;  // 1^T M per column (conservation check)
@@ -125,18 +127,25 @@ struct F64A {
   __device__ static V div(V a, V b) { return a / b; }
   __device__ static V abs(V a) { return fabs(a); }
   __device__ static V neg(V a) { return -a; }
-  // D g with g the polynomial extrapolation in time through f and n earlier states (n = 1..3) of
+  // D g with g the polynomial extrapolation in time through f and n earlier states (n = 1..4) of
   // the loss-compensated sequence c_k = h_k r^k (r = 1/(1 + dt/tau), one step of pure loss), times
-  // r: g = r (c0 + d1), r (c0 + 2 d1 - d2), r (c0 + 3 (d1 - d2) + d3) with d1 = c0 - c1,
-  // d2 = c1 - c2, d3 = c2 - c3, c0 = f. Exact for pure loss; r = 1 gives the plain polynomial.
-  __device__ static V start(V D, V f, V h1, V h2, V h3, int n, V r) {
+  // r: g = r (c0 + d1), r (c0 + 2 d1 - d2), r (c0 + 3 (d1 - d2) + d3),
+  // r (c0 + 4 (d1 + d3) - 6 d2 - d4) with d_m = c_(m-1) - c_m, c0 = f. Exact for pure loss;
+  // r = 1 gives the plain polynomial.
+  __device__ static V start(V D, V f, V h1, V h2, V h3, V h4, int n, V r) {
     const double c1 = h1 * r;
     const double d1 = f - c1;
     double c = d1;
     if (n >= 2) {
       const double r2 = r * r, c2 = h2 * r2;
       const double d2 = c1 - c2;
-      c = n == 2 ? 2.0 * d1 - d2 : 3.0 * (d1 - d2) + (c2 - h3 * (r2 * r));
+      if (n == 2) {
+        c = 2.0 * d1 - d2;
+      } else {
+        const double r3 = r2 * r, c3 = h3 * r3;
+        const double d3 = c2 - c3;
+        c = n == 3 ? 3.0 * (d1 - d2) + d3 : 4.0 * (d1 + d3) - 6.0 * d2 - (c3 - h4 * (r3 * r));
+      }
     }
     return D * (r * (f + c));
   }
@@ -204,15 +213,21 @@ struct DWA {
   // as F64A::start, in double-word: with loss rates up to 10 per day an increment is ~10 % of f,
   // so FP32 increments would leave ~1e-8 of f in the start, above what the cubic achieves; the
   // starting point only steers the iteration, the converged answer does not depend on it
-  __device__ static V start(V D, V f, V h1, V h2, V h3, int n, V r) {
+  __device__ static V start(V D, V f, V h1, V h2, V h3, V h4, int n, V r) {
     const dw c1 = dw_mul(h1, r);
     const dw d1 = sub(f, c1);
     dw c = d1;
     if (n >= 2) {
       const dw r2 = dw_mul(r, r), c2 = dw_mul(h2, r2);
       const dw d2 = sub(c1, c2);
-      c = n == 2 ? sub(dw{2.0f * d1.hi, 2.0f * d1.lo}, d2)
-                 : add(dw_mul_f(sub(d1, d2), 3.0f), sub(c2, dw_mul(h3, dw_mul(r2, r))));
+      if (n == 2) {
+        c = sub(dw{2.0f * d1.hi, 2.0f * d1.lo}, d2);
+      } else {
+        const dw r3 = dw_mul(r2, r), c3 = dw_mul(h3, r3);
+        const dw d3 = sub(c2, c3);
+        c = n == 3 ? add(dw_mul_f(sub(d1, d2), 3.0f), d3)
+                   : sub(sub(dw_mul_f(add(d1, d3), 4.0f), dw_mul_f(d2, 6.0f)), sub(c3, dw_mul(h4, dw_mul(r3, r))));
+      }
     }
     return dw_mul(D, dw_mul(r, add(f, c)));
   }
@@ -575,8 +590,9 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
     const long long base = I.base;
     const int nh = min(cm.st[b].nhist, cm.hist_cap), hs = cm.st[b].hslot;
     const double* h1p = fl.fh[hs];
-    const double* h2p = fl.fh[hs == 0 ? 2 : hs - 1];
-    const double* h3p = fl.fh[hs == 2 ? 0 : hs + 1];
+    const double* h2p = fl.fh[(hs + kHist - 1) % kHist];
+    const double* h3p = fl.fh[(hs + kHist - 2) % kHist];
+    const double* h4p = fl.fh[(hs + kHist - 3) % kHist];
     // the per-cell data of step 4 is only needed after three barriers: start its trip to L2 now
 #pragma unroll
     for (int q = threadIdx.x; q < kTX * kTY; q += kAsmThreads) {
@@ -588,6 +604,7 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
         if (nh > 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(h1p + K));
         if (nh > 1) asm volatile("prefetch.global.L2 [%0];" ::"l"(h2p + K));
         if (nh > 2) asm volatile("prefetch.global.L2 [%0];" ::"l"(h3p + K));
+        if (nh > 3) asm volatile("prefetch.global.L2 [%0];" ::"l"(h4p + K));
         if (nh > 0 && geo.decay) asm volatile("prefetch.global.L2 [%0];" ::"l"(geo.decay + K));
       }
     }
@@ -729,7 +746,8 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
         y0 = A::mul(D, fK);
       } else {
         const V h1 = A::ld(h1p, K), h2 = nh >= 2 ? A::ld(h2p, K) : h1, h3 = nh >= 3 ? A::ld(h3p, K) : h2;
-        y0 = A::start(D, fK, h1, h2, h3, nh, geo.decay ? A::ld(geo.decay, K) : A::k(1.0));
+        const V h4 = nh >= 4 ? A::ld(h4p, K) : h3;
+        y0 = A::start(D, fK, h1, h2, h3, h4, nh, geo.decay ? A::ld(geo.decay, K) : A::k(1.0));
       }
       A::st(fl.y64[cm.st[b].ycur], K, y0);
       if (wIn) AsmOut<C, A>::put(co, 1, K - 1, A::mul(Aw, inv));  // row K-1, east entry
@@ -1225,7 +1243,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_polish(Common cm, Fields fl, Co
             mn = fminf(mn, A::f32(fv));
           }
         }
-        A::st4(fl.fh[st.hslot == 2 ? 0 : st.hslot + 1] + K, A::ld4(fl.f + K));  // f^n into the oldest slot
+        A::st4(fl.fh[(st.hslot + 1) % kHist] + K, A::ld4(fl.f + K));  // f^n into the oldest slot
         A::st4(fl.f + K, fo);
       }
     }
@@ -1253,8 +1271,8 @@ __global__ void __launch_bounds__(kThreads, 3) k_polish(Common cm, Fields fl, Co
       st.clamped = (long long)tot[2];
       st.mass_drift = tot[1] != 0.0 ? fabs(tot[0] - tot[1]) / fabs(tot[1]) : 0.0;
       st.steps += 1;
-      st.hslot = st.hslot == 2 ? 0 : st.hslot + 1;
-      st.nhist = min(st.nhist + 1, 3);
+      st.hslot = (st.hslot + 1) % kHist;
+      st.nhist = min(st.nhist + 1, kHist);
       if (!(gmin >= 0.0)) st.status = ST_NEGATIVE;
     }
     __syncthreads();
