@@ -214,7 +214,7 @@ def run_reference(a):
 # Algorithmic bytes per real cell per launch (FP32+refine path): reads + writes of the arrays
 # each kernel must touch once (neighbour re-reads served by cache are not counted).
 BYTES32 = {
-    "assemble": 4 * 8 + 8 * 8 + 4 * (4 + 4) + 4 * 8,  # f + 3 earlier states, 8 factors -> 4 hi+lo coefs, invD/R/colsum/y
+    "assemble": 6 * 8 + 8 * 8 + 4 * (4 + 4) + 4 * 8,  # f, 4 earlier states, loss factor, 8 factors -> 4 hi+lo coefs, invD/R/colsum/y
     "resid": 8 + 4 + 8 + 4 * (4 + 4) + 8 + 4,     # y, x, R, hi+lo coefs -> y', r
     "bicg1": 4 * 4 + 4 * 4 + 2 * 4,               # r, p, v, r^, 4 coefs -> p', v'
     "bicg2": 2 * 4 + 4 * 4 + 4,                   # r, v, 4 coefs -> t

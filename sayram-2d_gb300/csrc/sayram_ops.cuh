@@ -211,7 +211,7 @@ struct DWA {
   __device__ static V abs(V a) { return dw_abs(a); }
   __device__ static V neg(V a) { return dw_neg(a); }
   // as F64A::start, in double-word: with loss rates up to 10 per day an increment is ~10 % of f,
-  // so FP32 increments would leave ~1e-8 of f in the start, above what the cubic achieves; the
+  // so FP32 increments would leave ~1e-8 of f in the start, above what the extrapolation achieves; the
   // starting point only steers the iteration, the converged answer does not depend on it
   __device__ static V start(V D, V f, V h1, V h2, V h3, V h4, int n, V r) {
     const dw c1 = dw_mul(h1, r);
@@ -739,7 +739,7 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
       A::st(fl.R, K, Rv);
       A::st(fl.colsum, K, A::addp(sd, dir));
       // start the solve from the loss-compensated polynomial extrapolation in time through f^n and
-      // up to three earlier states (only the starting point of the iteration; the converged
+      // up to four earlier states (only the starting point of the iteration; the converged
       // answer does not depend on it)
       V y0;
       if (nh == 0) {
