@@ -181,7 +181,7 @@ struct F64A {
 
 struct DWA {
   using V = dw;
-  static constexpr int kAsmBlocks = 5;  // k_assemble: latency bound, 5 resident blocks (48 registers)
+  static constexpr int kAsmBlocks = 4;  // k_assemble: 4 resident blocks (64 registers, no spill)
   __device__ static V ld(const double* p, long long i) {
     const float2 q = reinterpret_cast<const float2*>(p)[i];
     return dw{q.x, q.y};
