@@ -226,7 +226,7 @@ BYTES32 = {
 # DRAM bytes per processed cell measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the
 # 256-instance case of the same kernels (profiles/*_dw_256instances.md); traffic grows with the
 # cells processed, so a launch's traffic is this figure times the cells it processed.
-TRAFFIC32 = {"assemble": 168.2, "bicg1": 40.3, "bicg2": 27.9, "resid": 60.9, "polish": 92.9}
+TRAFFIC32 = {"assemble": 175.2, "bicg1": 40.3, "bicg2": 27.9, "resid": 60.9, "polish": 92.9}
 
 
 def kernel_roofline(b, probs, peak, steps=2):
