@@ -100,15 +100,16 @@ struct sayram_batch_s {
   // per-step CUDA graph with device-side loops (built on the first graph step)
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
+  // the same step without its prefix (counter reset, k_begin, k_assemble), for the host-buffer
+  // step that assembles piece by piece while the rest of the state is still being copied in
+  cudaGraph_t graph_solve = nullptr;
+  cudaGraphExec_t gexec_solve = nullptr;
 
   ~sayram_batch_s() { release(); }
 
   void release() {
     if (dev >= 0) cudaSetDevice(dev);
-    if (gexec) cudaGraphExecDestroy(gexec);
-    if (graph) cudaGraphDestroy(graph);
-    gexec = nullptr;
-    graph = nullptr;
+    drop_graph();
     for (void* p : allocs) cudaFree(p);
     allocs.clear();
     if (d_tab) cudaFree(d_tab);
@@ -212,23 +213,55 @@ struct sayram_batch_s {
   }
   // dispatch of the per-step sequence on precision and chunk size (graph: build it; else: run it)
   template <typename T, typename C, typename A>
-  int run_chunked(const sg::Coef<C>& cf, const sg::Coef<T>& ck, const sg::Kry<T>& kr, bool as_graph) {
+  int run_chunked(const sg::Coef<C>& cf, const sg::Coef<T>& ck, const sg::Kry<T>& kr, bool as_graph, bool prefix) {
     switch (chunk) {
-      case 1024: return as_graph ? build_graph<T, C, A, 1024>(cf, ck, kr) : step_once<T, C, A, 1024>(cf, ck, kr);
-      case 2048: return as_graph ? build_graph<T, C, A, 2048>(cf, ck, kr) : step_once<T, C, A, 2048>(cf, ck, kr);
-      default: return as_graph ? build_graph<T, C, A, 4096>(cf, ck, kr) : step_once<T, C, A, 4096>(cf, ck, kr);
+      case 1024: return as_graph ? build_graph<T, C, A, 1024>(cf, ck, kr, prefix) : step_once<T, C, A, 1024>(cf, ck, kr);
+      case 2048: return as_graph ? build_graph<T, C, A, 2048>(cf, ck, kr, prefix) : step_once<T, C, A, 2048>(cf, ck, kr);
+      default: return as_graph ? build_graph<T, C, A, 4096>(cf, ck, kr, prefix) : step_once<T, C, A, 4096>(cf, ck, kr);
     }
   }
-  int run_mode(bool as_graph) {
-    return dwm ? run_chunked<float, float, sg::DWA>(c32, c32, k32, as_graph)
-           : mixed ? run_chunked<float, float, sg::F64A>(c32, c32, k32, as_graph)
-                   : run_chunked<double, double, sg::F64A>(c64, c64, k64, as_graph);
+  int run_mode(bool as_graph, bool prefix = true) {
+    return dwm ? run_chunked<float, float, sg::DWA>(c32, c32, k32, as_graph, prefix)
+           : mixed ? run_chunked<float, float, sg::F64A>(c32, c32, k32, as_graph, prefix)
+                   : run_chunked<double, double, sg::F64A>(c64, c64, k64, as_graph, prefix);
+  }
+  // the step prefix outside a graph: counter reset, k_begin, then k_assemble over tiles [t0, t1)
+  int launch_begin() {
+    SG_CUDA(cudaMemsetAsync(d_ctl, 0, 2 * sizeof(int), stream));
+    sg::k_begin<<<(n + 255) / 256, 256, 0, stream>>>(cm);
+    SG_CUDA(cudaGetLastError());
+    return SAYRAM_OK;
+  }
+  int launch_assemble(int t0, int t1) {
+    if (dwm)
+      sg::k_assemble<float, sg::DWA><<<grid_tiles(), sg::kAsmThreads, 0, stream>>>(cm, geo, fl, c32, t0, t1);
+    else if (mixed)
+      sg::k_assemble<float, sg::F64A><<<grid_tiles(), sg::kAsmThreads, 0, stream>>>(cm, geo, fl, c32, t0, t1);
+    else
+      sg::k_assemble<double, sg::F64A><<<grid_tiles(), sg::kAsmThreads, 0, stream>>>(cm, geo, fl, c64, t0, t1);
+    SG_CUDA(cudaGetLastError());
+    return SAYRAM_OK;
+  }
+  // the rest of one step (refinement loop and polish) as a graph
+  int ensure_solve_graph() {
+    if (gexec_solve) return SAYRAM_OK;
+    int rc = run_mode(true, false);
+    if (rc) drop_graph();
+    return rc;
+  }
+  int launch_solve() {
+    int rc = ensure_solve_graph();
+    if (rc) return rc;
+    SG_CUDA(cudaGraphLaunch(gexec_solve, stream));
+    return SAYRAM_OK;
   }
   void drop_graph() {
     if (gexec) cudaGraphExecDestroy(gexec);
     if (graph) cudaGraphDestroy(graph);
-    gexec = nullptr;
-    graph = nullptr;
+    if (gexec_solve) cudaGraphExecDestroy(gexec_solve);
+    if (graph_solve) cudaGraphDestroy(graph_solve);
+    gexec = gexec_solve = nullptr;
+    graph = graph_solve = nullptr;
   }
   int autotune(int steps, int* best_chunk, int* best_grid);
   int set_dtable(int idx, const sayram_dtable* t);
@@ -256,7 +289,7 @@ struct sayram_batch_s {
   template <typename T, typename C, typename A, int CH>
   int step_once(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, const sg::Kry<T>& kr);
   template <typename T, typename C, typename A, int CH>
-  int build_graph(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, const sg::Kry<T>& kr);
+  int build_graph(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, const sg::Kry<T>& kr, bool prefix);
   int last_captured(cudaGraphNode_t* node);
   // wide (8-byte) table entries: a double, or a (hi, lo) float pair in double-word mode
   double wide(double v) const {
@@ -581,7 +614,7 @@ int sayram_batch_s::step_once(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, c
   if (prc) return prc;
   SG_CUDA(cudaMemsetAsync(d_ctl, 0, 2 * sizeof(int), stream));
   launch("begin", [&] { k_begin<<<(n + 255) / 256, 256, 0, stream>>>(cm); });
-  launch("assemble", [&] { k_assemble<C, A><<<gt, kAsmThreads, 0, stream>>>(cm, geo, fl, cfull); });
+  launch("assemble", [&] { k_assemble<C, A><<<gt, kAsmThreads, 0, stream>>>(cm, geo, fl, cfull, 0, -1); });
   for (int o = 0; o < opt.max_refine; ++o) {
     launch("resid", [&] {
       k_resid<T, C, A, CH><<<gs, kThreads, smem_wide(), stream>>>(cm, fl, cfull, kr, opt.tol, opt.inner_tol, opt.max_refine);
@@ -621,7 +654,7 @@ int sayram_batch_s::last_captured(cudaGraphNode_t* node) {
 // One step as a graph: memset + begin + assemble, WHILE(outer){ resid, WHILE(inner){ k1 k2 k3 } },
 // polish. The WHILE conditions are set on the device by the residual and Krylov kernels.
 template <typename T, typename C, typename A, int CH>
-int sayram_batch_s::build_graph(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, const sg::Kry<T>& kr) {
+int sayram_batch_s::build_graph(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, const sg::Kry<T>& kr, bool prefix) {
   using namespace sg;
   const int gs = grid_stream(), gt = grid_tiles();
   int prc = prep_kernels<T, C, A, CH>();
@@ -629,7 +662,7 @@ int sayram_batch_s::build_graph(const sg::Coef<C>& cfull, const sg::Coef<T>& ck,
   const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
   cudaGraph_t g = nullptr;
   SG_CUDA(cudaGraphCreate(&g, 0));
-  graph = g;
+  (prefix ? graph : graph_solve) = g;
   cudaGraphConditionalHandle hout, hin;
   SG_CUDA(cudaGraphConditionalHandleCreate(&hout, g, 1, cudaGraphCondAssignDefault));
   Common c2 = cm;
@@ -639,13 +672,15 @@ int sayram_batch_s::build_graph(const sg::Coef<C>& cfull, const sg::Coef<T>& ck,
   c2.guard_iters = opt.max_iters + 1;
   int rc;
   // prefix
-  cudaGraphNode_t pre;
-  SG_CUDA(cudaStreamBeginCaptureToGraph(stream, g, nullptr, nullptr, 0, mode));
-  cudaMemsetAsync(d_ctl, 0, 2 * sizeof(int), stream);
-  k_begin<<<(n + 255) / 256, 256, 0, stream>>>(c2);
-  k_assemble<C, A><<<gt, kAsmThreads, 0, stream>>>(c2, geo, fl, cfull);
-  if ((rc = last_captured(&pre))) { cudaStreamEndCapture(stream, &g); return rc; }
-  SG_CUDA(cudaStreamEndCapture(stream, &g));
+  cudaGraphNode_t pre = nullptr;
+  if (prefix) {
+    SG_CUDA(cudaStreamBeginCaptureToGraph(stream, g, nullptr, nullptr, 0, mode));
+    cudaMemsetAsync(d_ctl, 0, 2 * sizeof(int), stream);
+    k_begin<<<(n + 255) / 256, 256, 0, stream>>>(c2);
+    k_assemble<C, A><<<gt, kAsmThreads, 0, stream>>>(c2, geo, fl, cfull, 0, -1);
+    if ((rc = last_captured(&pre))) { cudaStreamEndCapture(stream, &g); return rc; }
+    SG_CUDA(cudaStreamEndCapture(stream, &g));
+  }
   // outer WHILE
   cudaGraphNodeParams op = {};
   op.type = cudaGraphNodeTypeConditional;
@@ -653,7 +688,7 @@ int sayram_batch_s::build_graph(const sg::Coef<C>& cfull, const sg::Coef<T>& ck,
   op.conditional.type = cudaGraphCondTypeWhile;
   op.conditional.size = 1;
   cudaGraphNode_t outer;
-  SG_CUDA(cudaGraphAddNode(&outer, g, &pre, nullptr, 1, &op));
+  SG_CUDA(cudaGraphAddNode(&outer, g, prefix ? &pre : nullptr, nullptr, prefix ? 1 : 0, &op));
   cudaGraph_t obody = op.conditional.phGraph_out[0];
   SG_CUDA(cudaGraphConditionalHandleCreate(&hin, obody, 0, cudaGraphCondAssignDefault));
   c2.h_inner = hin;
@@ -680,7 +715,7 @@ int sayram_batch_s::build_graph(const sg::Coef<C>& cfull, const sg::Coef<T>& ck,
   SG_CUDA(cudaStreamBeginCaptureToGraph(stream, g, &outer, nullptr, 1, mode));
   k_polish<C, A, CH><<<gs, kThreads, smem_wide(), stream>>>(c2, fl, cfull);
   SG_CUDA(cudaStreamEndCapture(stream, &g));
-  SG_CUDA(cudaGraphInstantiate(&gexec, g, 0));
+  SG_CUDA(cudaGraphInstantiate(prefix ? &gexec : &gexec_solve, g, 0));
   return SAYRAM_OK;
 }
 
@@ -988,14 +1023,21 @@ int sayram_batch_step_host(sayram_batch b, int nsteps, const double* f_in, doubl
     b->piece_ev.push_back(e);
   }
   const int gt = b->grid_tiles();
-  if (f_in) {
-    // an instance whose state changed restarts its extrapolation history; one given back its
-    // own current state (a host round trip) keeps it
+  // Graph stepping with a host field: the first step's assembly runs piece by piece behind the
+  // copies (each piece's tiles as soon as its cells have landed), then a graph of the solve.
+  const bool overlap = f_in && nsteps >= 1 && pieces.size() >= 2 && b->opt.use_graph && !b->timing;
+  int rc = SAYRAM_OK;
+  if (overlap) {
+    if ((rc = b->ensure_solve_graph())) return rc;
+    if ((rc = b->launch_begin())) return rc;
     for (size_t k = 0; k < pieces.size(); ++k) {
       const Piece& pc = pieces[k];
       SG_CUDA(cudaMemcpyAsync(b->d_stage + pc.off, f_in + pc.off, sizeof(double) * pc.len, cudaMemcpyHostToDevice,
                               b->cstream));
       SG_CUDA(cudaEventRecord(b->piece_ev[k], b->cstream));
+    }
+    for (size_t k = 0; k < pieces.size(); ++k) {
+      const Piece& pc = pieces[k];
       SG_CUDA(cudaStreamWaitEvent(b->stream, b->piece_ev[k], 0));
       b->launch("field_in", [&] {
         if (b->dwm)
@@ -1003,9 +1045,32 @@ int sayram_batch_step_host(sayram_batch b, int nsteps, const double* f_in, doubl
         else
           sg::k_field_in<sg::F64A><<<gt, 256, 0, b->stream>>>(b->cm, b->fl.f, b->d_stage, 1, pc.t0, pc.t1);
       });
+      if ((rc = b->launch_assemble(pc.t0, pc.t1))) return rc;
     }
+    if ((rc = b->launch_solve())) return rc;
+    if ((rc = b->launch_steps(nsteps - 1))) return rc;
+    SG_CUDA(cudaStreamSynchronize(b->stream));
+    rc = b->finish_status();
+  } else {
+    if (f_in) {
+      // an instance whose state changed restarts its extrapolation history; one given back its
+      // own current state (a host round trip) keeps it
+      for (size_t k = 0; k < pieces.size(); ++k) {
+        const Piece& pc = pieces[k];
+        SG_CUDA(cudaMemcpyAsync(b->d_stage + pc.off, f_in + pc.off, sizeof(double) * pc.len, cudaMemcpyHostToDevice,
+                                b->cstream));
+        SG_CUDA(cudaEventRecord(b->piece_ev[k], b->cstream));
+        SG_CUDA(cudaStreamWaitEvent(b->stream, b->piece_ev[k], 0));
+        b->launch("field_in", [&] {
+          if (b->dwm)
+            sg::k_field_in<sg::DWA><<<gt, 256, 0, b->stream>>>(b->cm, b->fl.f, b->d_stage, 1, pc.t0, pc.t1);
+          else
+            sg::k_field_in<sg::F64A><<<gt, 256, 0, b->stream>>>(b->cm, b->fl.f, b->d_stage, 1, pc.t0, pc.t1);
+        });
+      }
+    }
+    rc = b->run_steps(nsteps);
   }
-  int rc = b->run_steps(nsteps);
   if (rc != SAYRAM_OK && rc != SAYRAM_ERR_NOT_CONVERGED && rc != SAYRAM_ERR_NEGATIVE) return rc;
   if (f_out) {
     for (size_t k = 0; k < pieces.size(); ++k) {
@@ -1118,11 +1183,11 @@ int sayram_batch_export_system(sayram_batch b, int idx, double* M5, double* R) {
   SG_CUDA(cudaSetDevice(b->dev));
   const InstDev& I = b->hinst[idx];
   if (b->dwm)
-    sg::k_assemble<float, sg::DWA><<<b->grid_tiles(), sg::kAsmThreads, 0, b->stream>>>(b->cm, b->geo, b->fl, b->c32);
+    sg::k_assemble<float, sg::DWA><<<b->grid_tiles(), sg::kAsmThreads, 0, b->stream>>>(b->cm, b->geo, b->fl, b->c32, 0, -1);
   else if (b->mixed)
-    sg::k_assemble<float, sg::F64A><<<b->grid_tiles(), sg::kAsmThreads, 0, b->stream>>>(b->cm, b->geo, b->fl, b->c32);
+    sg::k_assemble<float, sg::F64A><<<b->grid_tiles(), sg::kAsmThreads, 0, b->stream>>>(b->cm, b->geo, b->fl, b->c32, 0, -1);
   else
-    sg::k_assemble<double, sg::F64A><<<b->grid_tiles(), sg::kAsmThreads, 0, b->stream>>>(b->cm, b->geo, b->fl, b->c64);
+    sg::k_assemble<double, sg::F64A><<<b->grid_tiles(), sg::kAsmThreads, 0, b->stream>>>(b->cm, b->geo, b->fl, b->c64, 0, -1);
   SG_CUDA(cudaGetLastError());
   const size_t rows = (size_t)I.ny * I.pitch;
   std::vector<double> invD(rows), Rr(rows), c[4];
@@ -1879,7 +1944,7 @@ extern "C" int sayram_step_noalloc(const sayram_problem* pd, const sayram_option
   for (int s = 0; s < nsteps; ++s) {
     SG_CUDA(cudaMemsetAsync(d_ctl, 0, 2 * sizeof(int), stream));
     k_begin<<<1, 32, 0, stream>>>(cm);
-    k_assemble<double, F64A><<<gt, kAsmThreads, 0, stream>>>(cm, geo, fl, co);
+    k_assemble<double, F64A><<<gt, kAsmThreads, 0, stream>>>(cm, geo, fl, co, 0, -1);
     for (int r = 0; r < o.max_refine; ++r) {
       k_resid<double, double, F64A, kNoAllocChunk><<<gs, kThreads, smem_na, stream>>>(cm, fl, co, kr, o.tol, o.inner_tol, o.max_refine);
       SG_CUDA(cudaGetLastError());

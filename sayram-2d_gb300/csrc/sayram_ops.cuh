@@ -567,8 +567,10 @@ __device__ __forceinline__ void dirichlet_face(typename A::V aK, typename A::V S
 
 // One tile of kTX x kTY cells per iteration; vertices and faces are computed once per tile
 // (plus a one-cell halo), in shared memory.
+// Tiles [t0, t1) of the tile list (t1 < 0: all of them).
 template <typename C, typename A>
-__global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common cm, Geo geo, Fields fl, Coef<C> co) {
+__global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common cm, Geo geo, Fields fl, Coef<C> co,
+                                                                       int t0, int t1) {
   using V = typename A::V;
   count_launch(cm.ctl);
   constexpr int HX = kTX + 2, HY = kTY + 2, VX = kTX + 1, VY = kTY + 1;
@@ -580,7 +582,8 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
   __shared__ V xL[kTY][VX], xR[kTY][VX];
   __shared__ V yB[VY][kTX], yT[VY][kTX];
   const V zero = A::k(0.0);
-  for (int t = blockIdx.x, nt_ = n_tiles(cm); t < nt_; t += gridDim.x) {
+  const int nt_ = t1 < 0 ? n_tiles(cm) : t1;
+  for (int t = t0 + blockIdx.x; t < nt_; t += gridDim.x) {
     const int b = cm.tile_inst[t];
     const InstDev I = cm.inst[b];
     if (!I.enabled) continue;  // uniform in the block
