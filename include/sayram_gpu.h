@@ -49,6 +49,7 @@ extern "C" {
 #define SAYRAM_ERR_CUDA 6          /* CUDA runtime error (no device, launch failure, ...) */
 #define SAYRAM_ERR_BUDGET 7        /* request does not fit the serving HBM budget */
 #define SAYRAM_ERR_STATE 8         /* call not valid in the object's current state */
+#define SAYRAM_ERR_IO 9            /* file could not be created or written */
 
 /* ---- boundary ids and types (source/BCTypes.h:13-16) ------------------------------------ */
 #define SAYRAM_XMIN 0

@@ -10,8 +10,8 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT_DIR, "libsayram_gpu.so")
-SOURCES = ["sayram_engine.cu"]
-DEPS = ["sayram_kernels.cuh", "sayram_ops.cuh", "dword.cuh"]
+SOURCES = ["sayram_engine.cu", "h5_writer.cc"]
+DEPS = ["sayram_kernels.cuh", "sayram_ops.cuh", "dword.cuh", "host_errors.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -26,7 +26,8 @@ def _stale() -> bool:
     if not os.path.exists(LIB):
         return True
     t = os.path.getmtime(LIB)
-    files = [os.path.join(CSRC, f) for f in SOURCES + DEPS] + [os.path.join(ROOT, "include", "sayram_gpu.h")]
+    files = [os.path.join(CSRC, f) for f in SOURCES + DEPS] + [
+        os.path.join(ROOT, "include", h) for h in ("sayram_gpu.h", "sayram_h5.h")]
     return any(os.path.getmtime(f) > t for f in files)
 
 

@@ -21,7 +21,7 @@ from . import build as _build
 
 _dp = ctypes.POINTER(ctypes.c_double)
 
-OK, ERR_ARG, ERR_OOM, ERR_NOT_CONVERGED, ERR_NEGATIVE, ERR_TIMEOUT, ERR_CUDA, ERR_BUDGET, ERR_STATE = range(9)
+OK, ERR_ARG, ERR_OOM, ERR_NOT_CONVERGED, ERR_NEGATIVE, ERR_TIMEOUT, ERR_CUDA, ERR_BUDGET, ERR_STATE, ERR_IO = range(10)
 FP64, FP32_REFINE, FP32_REFINE_DW = 0, 1, 2
 
 
@@ -131,6 +131,9 @@ SIGNATURES = {
     "sayram_server_info_get": (ctypes.c_int, [_P, ctypes.POINTER(sayram_server_info)]),
     "sayram_server_completed_ids": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
     "sayram_server_destroy": (None, [_P]),
+    "sayram_h5_create": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_P)]),
+    "sayram_h5_write": (ctypes.c_int, [_P, ctypes.c_char_p, _dp, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)]),
+    "sayram_h5_close": (ctypes.c_int, [_P]),
     "sayram_step_noalloc": (ctypes.c_int, [ctypes.POINTER(sayram_problem), ctypes.POINTER(sayram_options),
                                            ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                            ctypes.POINTER(sayram_stats)]),
@@ -436,3 +439,33 @@ class Server:
 
 def instance_bytes(nx: int, ny: int, precision: int = FP32_REFINE) -> int:
     return int(load().sayram_instance_bytes(nx, ny, precision))
+
+
+class H5File:
+    """The run's HDF5 output file (sayram_h5.h): ``write(path, array)`` is the reference's
+    ``xt::dump(file, path, array, xt::dump_mode::overwrite)`` (main.cc:65-89); the file is
+    complete after ``close()`` (or the end of a ``with`` block)."""
+
+    def __init__(self, path: str):
+        self._L = load()
+        self.h = _P()
+        check(self._L.sayram_h5_create(os.fsencode(path), ctypes.byref(self.h)), "sayram_h5_create")
+
+    def write(self, path: str, array) -> None:
+        if not self.h:
+            raise RuntimeError("H5File is closed")
+        a = np.require(array, dtype=np.float64, requirements="C")  # keeps 0-d arrays scalars
+        dims = (ctypes.c_longlong * max(1, a.ndim))(*a.shape)
+        check(self._L.sayram_h5_write(self.h, path.encode(), _ptr(a), a.ndim, dims), "sayram_h5_write")
+
+    def close(self) -> None:
+        if self.h:
+            h, self.h = self.h, _P()
+            check(self._L.sayram_h5_close(h), "sayram_h5_close")
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+        return False

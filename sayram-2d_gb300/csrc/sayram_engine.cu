@@ -16,6 +16,7 @@
 #include <string>
 #include <vector>
 
+#include "host_errors.h"
 #include "sayram_gpu.h"
 #include "sayram_ops.cuh"
 
@@ -929,6 +930,10 @@ int sayram_batch_s::finish_status() {
   if (worst == SAYRAM_ERR_NOT_CONVERGED) return fail(worst, "a step ended above the residual target");
   return SAYRAM_OK;
 }
+
+namespace sg {
+int host_fail(int code, const std::string& msg) { return fail(code, msg); }
+}  // namespace sg
 
 // ================================================================================== C-ABI
 extern "C" {

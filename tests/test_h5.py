@@ -1,0 +1,255 @@
+"""The HDF5 output writer (include/sayram_h5.h) and the driver loop that uses it (run.py).
+
+The writer is host code: everything here but the last test runs without a GPU. Its files are
+read back with tests/h5read.py, a strict reader of the classic HDF5 format that is itself pinned
+against a file written by libhdf5 (scipy's MATLAB 7.3 test file, when scipy ships it) and
+against scipy's reading of the same variable from a MATLAB 5 file.
+"""
+import os
+import struct
+
+import numpy as np
+import pytest
+
+import h5read
+from conftest import ROOT
+
+SCIPY_MAT = None
+try:
+    import scipy.io
+
+    SCIPY_MAT = os.path.join(os.path.dirname(scipy.io.__file__), "matlab", "tests", "data")
+except ImportError:  # pragma: no cover
+    pass
+
+LIBHDF5_FILE = os.path.join(SCIPY_MAT, "testhdf5_7.4_GLNX86.mat") if SCIPY_MAT else ""
+MAT5_FILE = os.path.join(SCIPY_MAT, "testdouble_7.4_GLNX86.mat") if SCIPY_MAT else ""
+needs_libhdf5_file = pytest.mark.skipif(not os.path.exists(LIBHDF5_FILE),
+                                        reason="scipy's libhdf5-written test file is not installed")
+
+
+# ----------------------------------------------------------------------------- the reader
+@needs_libhdf5_file
+def test_reader_reads_a_libhdf5_file():
+    f = h5read.File(LIBHDF5_FILE)
+    assert f.base == 512  # MATLAB's user block
+    ds = f["/testdouble"]
+    assert ds.dtype == np.float64 and ds.layout == "contiguous" and ds.shape == (9, 1)
+    assert ds.attributes == ["MATLAB_class"]
+    if os.path.exists(MAT5_FILE):
+        ref = scipy.io.loadmat(MAT5_FILE)["testdouble"]  # the same variable, MATLAB 5 format
+        np.testing.assert_array_equal(ds.data.ravel(), ref.ravel())
+
+
+@needs_libhdf5_file
+def test_reader_rejects_a_damaged_file(tmp_path):
+    buf = bytearray(open(LIBHDF5_FILE, "rb").read())
+    i = buf.find(b"SNOD")
+    buf[i:i + 4] = b"SNOX"
+    p = tmp_path / "bad.h5"
+    p.write_bytes(bytes(buf))
+    with pytest.raises(h5read.H5FormatError):
+        h5read.File(str(p))
+
+
+# ----------------------------------------------------------------------------- the writer
+def _write(capi, path, items):
+    with capi.H5File(str(path)) as h5:
+        for name, arr in items:
+            h5.write(name, arr)
+
+
+def test_round_trip_of_the_reference_layout(capi, tmp_path):
+    rng = np.random.default_rng(3)
+    nx, ny, nplots = 9, 7, 12
+    alpha0 = np.linspace(5, 90, nx)
+    logEN = rng.standard_normal(ny)
+    fs = [rng.standard_normal((nx, ny)) for _ in range(nplots + 1)]
+    items = [("/alpha0", alpha0), ("/logEN", logEN)] + [(f"/f/{k}", fs[k]) for k in range(nplots + 1)]
+    items.append(("/t", np.linspace(0, 1, nplots + 1)))
+    p = tmp_path / "out.h5"
+    _write(capi, p, items)
+    f = h5read.File(str(p))
+    assert f.eof == os.path.getsize(p)
+    assert sorted(f.root.members) == ["alpha0", "f", "logEN", "t"]
+    # names in the group's byte order, as the B-tree's comparison wants
+    assert list(f["/f"].members) == sorted(str(k) for k in range(nplots + 1))
+    for name, arr in items:
+        ds = f[name]
+        assert ds.shape == arr.shape and ds.dtype == np.dtype("<f8")
+        np.testing.assert_array_equal(ds.data, arr)
+
+
+def test_overwrite_scalars_empty_and_nesting(capi, tmp_path):
+    p = tmp_path / "misc.h5"
+    _write(capi, p, [("/a/b/c", np.arange(6.0).reshape(2, 3)), ("/a/b/c", np.ones(4)), ("/s", np.array(2.5)),
+                     ("/e", np.zeros((0, 3))), ("x", np.array([np.inf, -0.0, np.nan, 5e-324]))])
+    f = h5read.File(str(p))
+    np.testing.assert_array_equal(f["/a/b/c"].data, np.ones(4))  # dump_mode::overwrite
+    assert f["/s"].shape == () and float(f["/s"].data) == 2.5
+    assert f["/e"].shape == (0, 3) and f["/e"].address == h5read.UNDEF
+    x = f["/x"].data
+    assert np.isinf(x[0]) and np.signbit(x[1]) and np.isnan(x[2]) and x[3] == 5e-324
+
+
+def test_many_entries_in_one_group(capi, tmp_path):
+    p = tmp_path / "many.h5"
+    n = 1001
+    _write(capi, p, [(f"/f/{k}", np.full(3, float(k))) for k in range(n)])
+    f = h5read.File(str(p))
+    assert f.leaf_k >= (n + 1) // 2
+    assert len(f["/f"].members) == n
+    for k in (0, 7, 500, 1000):
+        np.testing.assert_array_equal(f[f"/f/{k}"].data, np.full(3, float(k)))
+
+
+@needs_libhdf5_file
+def test_message_encodings_match_libhdf5(capi, tmp_path):
+    """The datatype and fill-value messages of a float64 dataset are byte for byte the ones
+    libhdf5 wrote for the float64 dataset of its own file."""
+    ref = h5read.File(LIBHDF5_FILE)
+    p = tmp_path / "one.h5"
+    _write(capi, p, [("/testdouble", np.zeros((9, 1)))])
+    ours = h5read.File(str(p))
+
+    def msgs(f):
+        stab = f._messages(f.root_ohdr)[0]
+        bt, hp = struct.unpack_from("<QQ", stab.body)
+        heap, _ = f._heap(hp)
+        snod = f._abs(f._btree_leaves(bt, heap)[0])
+        _n, oaddr, _c, _r = struct.unpack_from("<QQII", f.buf, snod + 8)
+        return {m.type: m for m in f._messages(oaddr)}
+
+    a, b = msgs(ref), msgs(ours)
+    for t in (0x3, 0x5):
+        assert a[t].body == b[t].body and a[t].flags == b[t].flags
+    assert a[0x1].body == b[0x1].body  # dataspace version 1, (9, 1)
+    # superblock fields other than addresses
+    assert ours.leaf_k == ref.leaf_k and ours.internal_k == ref.internal_k
+
+
+@pytest.mark.parametrize("name,arr,needle", [
+    ("/a", np.ones(2), "is a dataset"),  # then /a/b below
+    ("/", np.ones(2), "empty dataset name"),
+    ("/x/../y", np.ones(2), "'.' or '..'"),
+])
+def test_bad_paths_rejected(capi, tmp_path, name, arr, needle):
+    h5 = capi.H5File(str(tmp_path / "bad.h5"))
+    try:
+        if needle == "is a dataset":
+            h5.write(name, arr)
+            name = "/a/b"
+        with pytest.raises(RuntimeError, match=needle):
+            h5.write(name, arr)
+    finally:
+        h5.close()
+
+
+def test_group_path_cannot_become_a_dataset(capi, tmp_path):
+    with capi.H5File(str(tmp_path / "g.h5")) as h5:
+        h5.write("/f/0", np.ones(2))
+        with pytest.raises(RuntimeError, match="is a group"):
+            h5.write("/f", np.ones(2))
+
+
+def test_null_and_io_errors(capi, tmp_path):
+    import ctypes
+
+    L = capi.load()
+    assert L.sayram_h5_close(None) == capi.ERR_ARG
+    assert L.sayram_h5_write(None, b"/a", None, 0, None) == capi.ERR_ARG
+    h = ctypes.c_void_p()
+    assert L.sayram_h5_create(str(tmp_path / "no" / "such" / "dir.h5").encode(), ctypes.byref(h)) == capi.ERR_IO
+    assert "cannot create" in capi.last_error()
+
+
+CPP_PROGRAM = r'''
+#include <array>
+#include <cstdio>
+#include "H5File.h"
+struct Grid2 {  // an xtensor-like (nx, ny) array: data() and shape()
+  std::array<std::size_t, 2> s{3, 2};
+  double d[6] = {1, 2, 3, 4, 5, 6};
+  const std::array<std::size_t, 2>& shape() const { return s; }
+  const double* data() const { return d; }
+};
+int main(int, char** argv) {
+  sayram::H5File file(argv[1]);
+  Grid2 f;
+  file.dump("/f/0", f);
+  const double a[3] = {5.0, 47.5, 90.0};
+  file.dump("/alpha0", a, {3});
+  try {
+    file.dump("/f", a, {3});
+  } catch (const std::runtime_error& e) {
+    std::printf("%s\n", e.what());
+  }
+  file.close();
+  return 0;
+}
+'''
+
+
+def test_cpp_wrapper_writes_the_file(capi, tmp_path):
+    """host/H5File.h, the replacement of main.cc's HighFive/xt::dump lines, from C++."""
+    import subprocess
+
+    src = tmp_path / "h5main.cc"
+    src.write_text(CPP_PROGRAM)
+    exe = tmp_path / "h5main"
+    libdir = os.path.dirname(capi.lib_path())
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I", os.path.join(ROOT, "sayram-2d_gb300", "host"),
+                    "-I", os.path.join(ROOT, "include"), str(src), "-L", libdir, "-lsayram_gpu",
+                    f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe), str(tmp_path / "cc.h5")], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert "sayram_h5_write" in out.stdout and "is a group" in out.stdout
+    f = h5read.File(str(tmp_path / "cc.h5"))
+    np.testing.assert_array_equal(f["/f/0"].data, np.arange(1.0, 7.0).reshape(3, 2))
+    np.testing.assert_array_equal(f["/alpha0"].data, [5.0, 47.5, 90.0])
+
+
+# ----------------------------------------------------------------------------- the driver
+def test_run_rejects_a_mismatched_problem(capi, tmp_path):
+    from sayram2d_gb300 import cases, run
+
+    ini = os.path.join(ROOT, "sayram-2d_gb300", "configs", "c0.ini")
+    with pytest.raises(ValueError, match="differs"):
+        run.run(ini, root=str(tmp_path), problem=cases.synthetic_problem(8, 8, 1e-3, 0))
+    with pytest.raises(ValueError, match="precision"):
+        run.run(ini, root=str(tmp_path), precision="fp16")
+
+
+@pytest.mark.gpu
+def test_run_writes_what_the_solver_computes(capi, tmp_path):
+    """main.cc's loop end to end on a short c0 run: the file holds the axes, f after every
+    save_every_step steps (bit-identical to stepping a Solver directly) and t."""
+    import math
+
+    from sayram2d_gb300 import cases, run
+
+    ini = tmp_path / "short.ini"
+    src = open(os.path.join(ROOT, "sayram-2d_gb300", "configs", "c0.ini")).read()
+    ini.write_text(src.replace("nsteps = 1000", "nsteps = 25").replace("nplots = 10", "nplots = 4"))
+    rp = cases.read_ini(str(ini))
+    assert (rp.nsteps, rp.save_every_step) == (24, 6)  # Parameters.cc:58-60 rounding
+    path = run.run(str(ini), root=str(tmp_path))
+    assert path == str(tmp_path / "output" / rp.run_id / (rp.run_id + "_data.h5"))
+    assert (tmp_path / "output" / rp.run_id / (rp.run_id + ".ini")).read_text() == ini.read_text()
+    f = h5read.File(path)
+    prob = cases.problem_from_params(rp)
+    x = 0.5 * (prob.x_edges[:-1] + prob.x_edges[1:])
+    y = 0.5 * (prob.y_edges[:-1] + prob.y_edges[1:])
+    np.testing.assert_array_equal(f["/alpha0"].data, x / cases.PI * 180.0)
+    np.testing.assert_array_equal(f["/logEN"].data, y - math.log(cases.E0))
+    np.testing.assert_array_equal(f["/t"].data, np.linspace(0.0, rp.T, rp.nplots + 1))
+    s = capi.Solver(prob, precision=capi.FP64, tol=rp.tol)
+    try:
+        np.testing.assert_array_equal(f["/f/0"].data, prob.f0)
+        for k in range(1, rp.nplots + 1):
+            for _ in range(rp.save_every_step):
+                s.update()
+            np.testing.assert_array_equal(f[f"/f/{k}"].data, s.f())
+    finally:
+        s.close()
+    assert sorted(f["/f"].members, key=int) == [str(k) for k in range(rp.nplots + 1)]
