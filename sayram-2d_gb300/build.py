@@ -10,7 +10,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT_DIR, "libsayram_gpu.so")
-SOURCES = ["sayram_engine.cu", "h5_writer.cc"]
+SOURCES = ["sayram_engine.cu", "h5_writer.cc", "h5_reader.cc"]
 DEPS = ["sayram_kernels.cuh", "sayram_ops.cuh", "dword.cuh", "host_errors.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -134,6 +134,11 @@ SIGNATURES = {
     "sayram_h5_create": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_P)]),
     "sayram_h5_write": (ctypes.c_int, [_P, ctypes.c_char_p, _dp, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)]),
     "sayram_h5_close": (ctypes.c_int, [_P]),
+    "sayram_h5_read": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                      ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(_dp)]),
+    "sayram_h5_free": (None, [ctypes.c_void_p]),
+    "sayram_dtable_load_h5": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(sayram_dtable)]),
+    "sayram_dtable_free": (None, [ctypes.POINTER(sayram_dtable)]),
     "sayram_step_noalloc": (ctypes.c_int, [ctypes.POINTER(sayram_problem), ctypes.POINTER(sayram_options),
                                            ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                            ctypes.POINTER(sayram_stats)]),
@@ -469,3 +474,34 @@ class H5File:
     def __exit__(self, *exc):
         self.close()
         return False
+
+
+def h5_read(file: str, path: str) -> np.ndarray:
+    """``xt::load_hdf5(file, path)``: one dataset of a classic-format HDF5 file as float64."""
+    L = load()
+    rank, dims, data = ctypes.c_int(), (ctypes.c_longlong * 32)(), _dp()
+    check(L.sayram_h5_read(os.fsencode(file), path.encode(), 32, ctypes.byref(rank), dims, ctypes.byref(data)),
+          "sayram_h5_read")
+    try:
+        shape = tuple(dims[k] for k in range(rank.value))
+        n = int(np.prod(shape)) if shape else 1
+        return np.ctypeslib.as_array(data, shape=(max(n, 1),))[:n].copy().reshape(shape)
+    finally:
+        L.sayram_h5_free(ctypes.cast(data, ctypes.c_void_p))
+
+
+def load_dtable(file: str):
+    """``Albert_Young_IO::read_D`` (Albert_Young_IO.cc:17-36): the D table of a D/<dID>.h5 file as
+    a cases.DTable (/alpha0 in degrees, /E, /Daa, /Dap, /Dpp)."""
+    from .cases import DTable
+
+    L = load()
+    t = sayram_dtable()
+    check(L.sayram_dtable_load_h5(os.fsencode(file), ctypes.byref(t)), "sayram_dtable_load_h5")
+    try:
+        na, ne = t.n_alpha, t.n_energy
+        vec = lambda p, n: np.ctypeslib.as_array(p, shape=(n,)).copy()
+        return DTable(vec(t.alpha0_deg, na), vec(t.energy, ne), vec(t.Daa, na * ne).reshape(na, ne),
+                      vec(t.Dap, na * ne).reshape(na, ne), vec(t.Dpp, na * ne).reshape(na, ne))
+    finally:
+        L.sayram_dtable_free(ctypes.byref(t))

@@ -209,6 +209,80 @@ def test_cpp_wrapper_writes_the_file(capi, tmp_path):
     np.testing.assert_array_equal(f["/alpha0"].data, [5.0, 47.5, 90.0])
 
 
+# ----------------------------------------------------------------------------- the reader in the library
+@needs_libhdf5_file
+def test_library_reader_reads_a_libhdf5_file(capi):
+    """sayram_h5_read on a file libhdf5 wrote (with a 512-byte user block), against scipy's
+    reading of the same variable from its MATLAB 5 copy."""
+    d = capi.h5_read(LIBHDF5_FILE, "/testdouble")
+    assert d.shape == (9, 1)
+    if os.path.exists(MAT5_FILE):
+        np.testing.assert_array_equal(d.ravel(), scipy.io.loadmat(MAT5_FILE)["testdouble"].ravel())
+    with pytest.raises(RuntimeError, match="no object named"):
+        capi.h5_read(LIBHDF5_FILE, "/nothing")
+
+
+def test_library_reader_round_trip(capi, tmp_path):
+    rng = np.random.default_rng(11)
+    items = {"/a": rng.standard_normal((4, 5)), "/g/h/b": rng.standard_normal(7), "/s": np.array(1.25),
+             "/e": np.zeros((0, 2))}
+    items.update({f"/f/{k}": rng.standard_normal((3, 2)) for k in range(40)})
+    p = tmp_path / "rt.h5"
+    _write(capi, p, list(items.items()))
+    for name, arr in items.items():
+        got = capi.h5_read(str(p), name)
+        assert got.shape == arr.shape
+        np.testing.assert_array_equal(got, arr)
+    with pytest.raises(RuntimeError, match="is a group"):
+        capi.h5_read(str(p), "/g/h")
+    with pytest.raises(RuntimeError, match="cannot open"):
+        capi.h5_read(str(tmp_path / "missing.h5"), "/a")
+
+
+def _patched(src, dst, old: bytes, new: bytes):
+    buf = open(src, "rb").read()
+    assert buf.count(old) == 1
+    open(dst, "wb").write(buf.replace(old, new))
+
+
+def test_library_reader_refuses_what_it_does_not_read(capi, tmp_path):
+    p = tmp_path / "x.h5"
+    _write(capi, p, [("/a", np.arange(4.0))])
+    ds = h5read.File(str(p))["/a"]
+    lay = b"\x03\x01" + struct.pack("<QQ", ds.address, ds.size)
+    _patched(p, tmp_path / "chunked.h5", lay, b"\x03\x02" + lay[2:])  # layout class 2: chunked
+    with pytest.raises(RuntimeError, match="chunked storage"):
+        capi.h5_read(str(tmp_path / "chunked.h5"), "/a")
+    sig = b"\x89HDF\r\n\x1a\n\x00"
+    _patched(p, tmp_path / "v2.h5", sig, sig[:-1] + b"\x02")  # superblock version 2
+    with pytest.raises(RuntimeError, match="superblock version 2"):
+        capi.h5_read(str(tmp_path / "v2.h5"), "/a")
+    (tmp_path / "not.h5").write_bytes(b"plain text, not HDF5" * 40)
+    with pytest.raises(RuntimeError, match="not an HDF5 file"):
+        capi.h5_read(str(tmp_path / "not.h5"), "/a")
+
+
+def test_load_dtable(capi, tmp_path):
+    """Albert_Young_IO::read_D: a D file written in the reference's layout loads bit for bit;
+    mismatched shapes and missing datasets are refused."""
+    from sayram2d_gb300 import cases
+
+    t = cases.synthetic_dtable(5)
+    p = tmp_path / "D.h5"
+    _write(capi, p, [("/alpha0", t.alpha0_deg), ("/E", t.E), ("/Daa", t.Daa), ("/Dap", t.Dap), ("/Dpp", t.Dpp)])
+    u = capi.load_dtable(str(p))
+    for k in ("alpha0_deg", "E", "Daa", "Dap", "Dpp"):
+        np.testing.assert_array_equal(getattr(u, k), getattr(t, k))
+    bad = tmp_path / "Dbad.h5"
+    _write(capi, bad, [("/alpha0", t.alpha0_deg), ("/E", t.E), ("/Daa", t.Daa.T), ("/Dap", t.Dap), ("/Dpp", t.Dpp)])
+    with pytest.raises(RuntimeError, match="must be \\(n_alpha0, n_E\\)"):
+        capi.load_dtable(str(bad))
+    missing = tmp_path / "Dmiss.h5"
+    _write(capi, missing, [("/alpha0", t.alpha0_deg), ("/E", t.E)])
+    with pytest.raises(RuntimeError, match="no object named 'Daa'"):
+        capi.load_dtable(str(missing))
+
+
 # ----------------------------------------------------------------------------- the driver
 def test_run_rejects_a_mismatched_problem(capi, tmp_path):
     from sayram2d_gb300 import cases, run
