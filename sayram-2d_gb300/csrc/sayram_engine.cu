@@ -565,8 +565,19 @@ int sayram_batch_s::build(const sayram_problem* probs, int count, const sayram_o
     maxcells = std::max(maxcells, (long long)p.nx * p.ny);
   }
   nreal = h;
-  // default launch shape: the largest chunk that still gives every SM several blocks
-  chunk = nreal >= 8LL * 4096 * nsm ? 4096 : nreal >= 8LL * 2048 * nsm ? 2048 : 1024;
+  // default launch shape: the largest chunk that still leaves two chunks per SM (measured over
+  // single 128^2..2048^2 instances and mixed batches of 19..200: larger chunks pay below that,
+  // when too few blocks share the stream, and above it, from fewer, longer block latencies)
+  chunk = 1024;
+  for (int c : {4096, 2048}) {
+    long long nch = 0;
+    for (int b = 0; b < count; ++b)
+      nch += (round_up((long long)probs[b].ny * round_up(probs[b].nx, 4), 4) + c - 1) / c;
+    if (nch >= 2LL * nsm) {
+      chunk = c;
+      break;
+    }
+  }
   if ((rc = alloc_storage(cursor + 64, count, chunks, tiles, xoff, yoff, doff, std::max(6 * maxcells, nreal))))
     return rc;
   n = count;

@@ -287,6 +287,16 @@ def test_launch_shape_setter(capi):
     ref.close()
 
 
+@pytest.mark.parametrize("n,chunk", [(256, 1024), (512, 1024), (1024, 2048), (2048, 4096)])
+def test_default_launch_shape(capi, n, chunk):
+    """Without tuning, a batch takes the largest chunk that leaves at least two chunks per SM
+    (GB300: 152 SMs, so 304 chunks): 512^2 cells make 128 chunks of 2048, 1024^2 make 256 of 4096
+    but 512 of 2048, 2048^2 make 1024 of 4096."""
+    s = capi.Solver(cases.synthetic_problem(n, n, 1e-2, seed=1), precision=capi.FP32_REFINE_DW)
+    assert s.launch_shape()[0] == chunk
+    s.close()
+
+
 @pytest.mark.parametrize("pinned", [False, True])
 @pytest.mark.parametrize("prec", [0, 2])
 def test_step_host_round_trips_keep_history(capi, prec, pinned):
