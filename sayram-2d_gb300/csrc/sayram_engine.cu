@@ -101,8 +101,9 @@ struct sayram_batch_s {
   // per-step CUDA graph with device-side loops (built on the first graph step)
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
-  // the same step without its prefix (counter reset, k_begin, k_assemble), for the host-buffer
-  // step that assembles piece by piece while the rest of the state is still being copied in
+  // the same step without its prefix (counter reset, k_begin, k_assemble) and its polish, for the
+  // host-buffer step that assembles piece by piece while the state is still being copied in and
+  // polishes piece by piece while the finished pieces are copied out
   cudaGraph_t graph_solve = nullptr;
   cudaGraphExec_t gexec_solve = nullptr;
 
@@ -243,7 +244,26 @@ struct sayram_batch_s {
     SG_CUDA(cudaGetLastError());
     return SAYRAM_OK;
   }
-  // the rest of one step (refinement loop and polish) as a graph
+  // the polish over chunks [c0, c1) (whole instances; c1 < 0: all)
+  template <typename C, typename A>
+  int launch_polish_t(const sg::Coef<C>& cf, int c0, int c1) {
+    const int gs = grid_stream();
+    const size_t sm = smem_wide();
+    if (chunk == 1024)
+      sg::k_polish<C, A, 1024><<<gs, sg::kThreads, sm, stream>>>(cm, fl, cf, c0, c1);
+    else if (chunk == 2048)
+      sg::k_polish<C, A, 2048><<<gs, sg::kThreads, sm, stream>>>(cm, fl, cf, c0, c1);
+    else
+      sg::k_polish<C, A, 4096><<<gs, sg::kThreads, sm, stream>>>(cm, fl, cf, c0, c1);
+    SG_CUDA(cudaGetLastError());
+    return SAYRAM_OK;
+  }
+  int launch_polish(int c0, int c1) {
+    return dwm ? launch_polish_t<float, sg::DWA>(c32, c0, c1)
+           : mixed ? launch_polish_t<float, sg::F64A>(c32, c0, c1)
+                   : launch_polish_t<double, sg::F64A>(c64, c0, c1);
+  }
+  // the refinement loop of one step as a graph (no prefix, no polish)
   int ensure_solve_graph() {
     if (gexec_solve) return SAYRAM_OK;
     int rc = run_mode(true, false);
@@ -648,7 +668,7 @@ int sayram_batch_s::step_once(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, c
       }
     }
   }
-  launch("polish", [&] { k_polish<C, A, CH><<<gs, kThreads, smem_wide(), stream>>>(cm, fl, cfull); });
+  launch("polish", [&] { k_polish<C, A, CH><<<gs, kThreads, smem_wide(), stream>>>(cm, fl, cfull, 0, -1); });
   SG_CUDA(cudaGetLastError());
   return SAYRAM_OK;
 }
@@ -723,10 +743,12 @@ int sayram_batch_s::build_graph(const sg::Coef<C>& cfull, const sg::Coef<T>& ck,
   k_bicg2<T, CH><<<gs, kThreads, smem_spmv<T>(), stream>>>(c2, ck, kr);
   k_bicg3<T, CH><<<gs, kThreads, 0, stream>>>(c2, kr, opt.max_iters);
   SG_CUDA(cudaStreamEndCapture(stream, &ibody));
-  // suffix
-  SG_CUDA(cudaStreamBeginCaptureToGraph(stream, g, &outer, nullptr, 1, mode));
-  k_polish<C, A, CH><<<gs, kThreads, smem_wide(), stream>>>(c2, fl, cfull);
-  SG_CUDA(cudaStreamEndCapture(stream, &g));
+  // suffix (the solve-only graph leaves the polish to its caller)
+  if (prefix) {
+    SG_CUDA(cudaStreamBeginCaptureToGraph(stream, g, &outer, nullptr, 1, mode));
+    k_polish<C, A, CH><<<gs, kThreads, smem_wide(), stream>>>(c2, fl, cfull, 0, -1);
+    SG_CUDA(cudaStreamEndCapture(stream, &g));
+  }
   SG_CUDA(cudaGraphInstantiate(prefix ? &gexec : &gexec_solve, g, 0));
   return SAYRAM_OK;
 }
@@ -1010,11 +1032,13 @@ int sayram_batch_step(sayram_batch b, int nsteps) {
 // faster than kernels reading host memory over the CPU-GPU link (208 against 153 GB/s on GB300).
 int sayram_batch_step_host(sayram_batch b, int nsteps, const double* f_in, double* f_out) {
   if (!b) return fail(SAYRAM_ERR_ARG, "null handle");
+  if (nsteps < 0) return fail(SAYRAM_ERR_ARG, "nsteps must be >= 0");
   SG_CUDA(cudaSetDevice(b->dev));
   constexpr int kPieces = 8;
   struct Piece {
     long long off, len;  // doubles of the packed host array
     int t0, t1;          // tiles
+    int c0, c1;          // chunks
   };
   std::vector<Piece> pieces;
   {
@@ -1029,78 +1053,106 @@ int sayram_batch_step_host(sayram_batch b, int nsteps, const double* f_in, doubl
       }
       const sg::InstDev& A = b->hinst[a];
       const sg::InstDev& E = b->hinst[e - 1];
-      pieces.push_back({A.hoff, len, A.tile0, E.tile0 + E.ntx * E.nty});
+      pieces.push_back({A.hoff, len, A.tile0, E.tile0 + E.ntx * E.nty, A.chunk0, E.chunk0 + E.nchunks});
       a = e;
     }
   }
-  while (b->piece_ev.size() < 2 * pieces.size()) {
+  const size_t np = pieces.size();
+  while (b->piece_ev.size() < 2 * np) {
     cudaEvent_t e;
     SG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     b->piece_ev.push_back(e);
   }
   const int gt = b->grid_tiles();
-  // Graph stepping with a host field: the first step's assembly runs piece by piece behind the
-  // copies (each piece's tiles as soon as its cells have landed), then a graph of the solve.
-  const bool overlap = f_in && nsteps >= 1 && pieces.size() >= 2 && b->opt.use_graph && !b->timing;
+  auto field_in = [&](const Piece& pc) {
+    b->launch("field_in", [&] {
+      if (b->dwm)
+        sg::k_field_in<sg::DWA><<<gt, 256, 0, b->stream>>>(b->cm, b->fl.f, b->d_stage, 1, pc.t0, pc.t1);
+      else
+        sg::k_field_in<sg::F64A><<<gt, 256, 0, b->stream>>>(b->cm, b->fl.f, b->d_stage, 1, pc.t0, pc.t1);
+    });
+  };
+  auto field_out = [&](const Piece& pc) {
+    b->launch("field_out", [&] {
+      if (b->dwm)
+        sg::k_field_out<sg::DWA><<<gt, 256, 0, b->stream>>>(b->cm, b->d_stage, b->fl.f, pc.t0, pc.t1);
+      else
+        sg::k_field_out<sg::F64A><<<gt, 256, 0, b->stream>>>(b->cm, b->d_stage, b->fl.f, pc.t0, pc.t1);
+    });
+  };
+  auto copy_in = [&](size_t k) -> int {  // H2D of piece k on the copy stream, then an event
+    const Piece& pc = pieces[k];
+    SG_CUDA(cudaMemcpyAsync(b->d_stage + pc.off, f_in + pc.off, sizeof(double) * pc.len, cudaMemcpyHostToDevice,
+                            b->cstream));
+    SG_CUDA(cudaEventRecord(b->piece_ev[k], b->cstream));
+    return SAYRAM_OK;
+  };
+  auto copy_out = [&](size_t k) -> int {  // after piece k's transform: D2H on the copy stream
+    const Piece& pc = pieces[k];
+    SG_CUDA(cudaEventRecord(b->piece_ev[np + k], b->stream));
+    SG_CUDA(cudaStreamWaitEvent(b->cstream, b->piece_ev[np + k], 0));
+    SG_CUDA(cudaMemcpyAsync(f_out + pc.off, b->d_stage + pc.off, sizeof(double) * pc.len, cudaMemcpyDeviceToHost,
+                            b->cstream));
+    return SAYRAM_OK;
+  };
+  // An instance whose state changed restarts its extrapolation history; one given back its own
+  // current state (a host round trip) keeps it (k_field_in compares bit for bit).
   int rc = SAYRAM_OK;
-  if (overlap) {
+  const bool split = b->opt.use_graph && !b->timing && nsteps >= 1 && np >= 2 && (f_in || f_out);
+  if (split) {
+    // Graph stepping with host buffers: the first step's assembly runs piece by piece behind the
+    // copies in (each piece's tiles as soon as its cells have landed), and the last step's
+    // polish runs piece by piece ahead of the copies out; in between, graphs. Every piece holds
+    // whole instances, so the per-instance reductions stay inside one launch.
     if ((rc = b->ensure_solve_graph())) return rc;
-    if ((rc = b->launch_begin())) return rc;
-    for (size_t k = 0; k < pieces.size(); ++k) {
-      const Piece& pc = pieces[k];
-      SG_CUDA(cudaMemcpyAsync(b->d_stage + pc.off, f_in + pc.off, sizeof(double) * pc.len, cudaMemcpyHostToDevice,
-                              b->cstream));
-      SG_CUDA(cudaEventRecord(b->piece_ev[k], b->cstream));
-    }
-    for (size_t k = 0; k < pieces.size(); ++k) {
-      const Piece& pc = pieces[k];
-      SG_CUDA(cudaStreamWaitEvent(b->stream, b->piece_ev[k], 0));
-      b->launch("field_in", [&] {
-        if (b->dwm)
-          sg::k_field_in<sg::DWA><<<gt, 256, 0, b->stream>>>(b->cm, b->fl.f, b->d_stage, 1, pc.t0, pc.t1);
-        else
-          sg::k_field_in<sg::F64A><<<gt, 256, 0, b->stream>>>(b->cm, b->fl.f, b->d_stage, 1, pc.t0, pc.t1);
-      });
-      if ((rc = b->launch_assemble(pc.t0, pc.t1))) return rc;
-    }
-    if ((rc = b->launch_solve())) return rc;
-    if ((rc = b->launch_steps(nsteps - 1))) return rc;
-    SG_CUDA(cudaStreamSynchronize(b->stream));
-    rc = b->finish_status();
-  } else {
-    if (f_in) {
-      // an instance whose state changed restarts its extrapolation history; one given back its
-      // own current state (a host round trip) keeps it
-      for (size_t k = 0; k < pieces.size(); ++k) {
-        const Piece& pc = pieces[k];
-        SG_CUDA(cudaMemcpyAsync(b->d_stage + pc.off, f_in + pc.off, sizeof(double) * pc.len, cudaMemcpyHostToDevice,
-                                b->cstream));
-        SG_CUDA(cudaEventRecord(b->piece_ev[k], b->cstream));
-        SG_CUDA(cudaStreamWaitEvent(b->stream, b->piece_ev[k], 0));
-        b->launch("field_in", [&] {
-          if (b->dwm)
-            sg::k_field_in<sg::DWA><<<gt, 256, 0, b->stream>>>(b->cm, b->fl.f, b->d_stage, 1, pc.t0, pc.t1);
-          else
-            sg::k_field_in<sg::F64A><<<gt, 256, 0, b->stream>>>(b->cm, b->fl.f, b->d_stage, 1, pc.t0, pc.t1);
-        });
+    if (nsteps > 2 && (rc = b->launch_steps(0))) return rc;  // builds the full step's graph up front
+    for (int s = 0; s < nsteps; ++s) {
+      const bool head = s == 0 && f_in, tail = s == nsteps - 1 && f_out;
+      if (!head && !tail) {
+        if ((rc = b->launch_steps(1))) return rc;
+        continue;
+      }
+      if ((rc = b->launch_begin())) return rc;
+      if (head) {
+        for (size_t k = 0; k < np; ++k)
+          if ((rc = copy_in(k))) return rc;
+        for (size_t k = 0; k < np; ++k) {
+          SG_CUDA(cudaStreamWaitEvent(b->stream, b->piece_ev[k], 0));
+          field_in(pieces[k]);
+          if ((rc = b->launch_assemble(pieces[k].t0, pieces[k].t1))) return rc;
+        }
+      } else if ((rc = b->launch_assemble(0, -1))) {
+        return rc;
+      }
+      if ((rc = b->launch_solve())) return rc;
+      if (tail) {
+        for (size_t k = 0; k < np; ++k) {
+          if ((rc = b->launch_polish(pieces[k].c0, pieces[k].c1))) return rc;
+          field_out(pieces[k]);
+          if ((rc = copy_out(k))) return rc;
+        }
+      } else if ((rc = b->launch_polish(0, -1))) {
+        return rc;
       }
     }
-    rc = b->run_steps(nsteps);
+    SG_CUDA(cudaStreamSynchronize(b->cstream));
+    SG_CUDA(cudaStreamSynchronize(b->stream));
+    return b->finish_status();
   }
+  if (f_in) {
+    for (size_t k = 0; k < np; ++k) {
+      if ((rc = copy_in(k))) return rc;
+      SG_CUDA(cudaStreamWaitEvent(b->stream, b->piece_ev[k], 0));
+      field_in(pieces[k]);
+    }
+  }
+  rc = b->run_steps(nsteps);
   if (rc != SAYRAM_OK && rc != SAYRAM_ERR_NOT_CONVERGED && rc != SAYRAM_ERR_NEGATIVE) return rc;
   if (f_out) {
-    for (size_t k = 0; k < pieces.size(); ++k) {
-      const Piece& pc = pieces[k];
-      b->launch("field_out", [&] {
-        if (b->dwm)
-          sg::k_field_out<sg::DWA><<<gt, 256, 0, b->stream>>>(b->cm, b->d_stage, b->fl.f, pc.t0, pc.t1);
-        else
-          sg::k_field_out<sg::F64A><<<gt, 256, 0, b->stream>>>(b->cm, b->d_stage, b->fl.f, pc.t0, pc.t1);
-      });
-      SG_CUDA(cudaEventRecord(b->piece_ev[pieces.size() + k], b->stream));
-      SG_CUDA(cudaStreamWaitEvent(b->cstream, b->piece_ev[pieces.size() + k], 0));
-      SG_CUDA(cudaMemcpyAsync(f_out + pc.off, b->d_stage + pc.off, sizeof(double) * pc.len, cudaMemcpyDeviceToHost,
-                              b->cstream));
+    for (size_t k = 0; k < np; ++k) {
+      field_out(pieces[k]);
+      int rc2 = copy_out(k);
+      if (rc2) return rc2;
     }
     SG_CUDA(cudaStreamSynchronize(b->cstream));
     SG_CUDA(cudaStreamSynchronize(b->stream));
@@ -1980,7 +2032,7 @@ extern "C" int sayram_step_noalloc(const sayram_problem* pd, const sayram_option
         }
       }
     }
-    k_polish<double, F64A, kNoAllocChunk><<<gs, kThreads, smem_na, stream>>>(cm, fl, co);
+    k_polish<double, F64A, kNoAllocChunk><<<gs, kThreads, smem_na, stream>>>(cm, fl, co, 0, -1);
     SG_CUDA(cudaGetLastError());
   }
   k_field_out<F64A><<<gt, 256, 0, stream>>>(cm, f_out, fl.f, 0, -1);

@@ -796,18 +796,19 @@ __device__ __forceinline__ Slot slot_of(int c, const InstDev& I, int g) {
 // passing chunks are compacted in shared memory: a launch in which most instances have finished
 // costs one round of checks per block instead of two dependent loads per chunk. Chunks are
 // independent, so the order in which a block takes them does not change any result.
+// Chunks [c0, c1) of the list only (c1 < 0: to the end).
 template <typename W, typename Body>
-__device__ __forceinline__ void for_active_chunks(const Common& cm, W&& want, Body&& body) {
+__device__ __forceinline__ void for_active_chunks(const Common& cm, W&& want, Body&& body, int c0 = 0, int c1 = -1) {
   __shared__ int s_list[kThreads];
   __shared__ int s_cnt;
-  const int nc = n_chunks(cm);
+  const int nc = (c1 < 0 ? n_chunks(cm) : c1) - c0;
   const int per = (int)blockIdx.x < nc ? (nc - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
   for (int r0 = 0; r0 < per; r0 += kThreads) {
     if (threadIdx.x == 0) s_cnt = 0;
     __syncthreads();
     const int k = r0 + (int)threadIdx.x;
     if (k < per) {
-      const int c = (int)blockIdx.x + k * (int)gridDim.x;
+      const int c = c0 + (int)blockIdx.x + k * (int)gridDim.x;
       if (want(cm.chunk_inst[c])) s_list[atomicAdd(&s_cnt, 1)] = c;
     }
     __syncthreads();
@@ -1195,9 +1196,10 @@ __global__ void __launch_bounds__(kThreads, krylov_blocks<T>()) k_bicg3(Common c
 
 // ------------------------------------------------------------------------------ polish + checks
 // y' = R + (I - A~) max(y, 0) >= 0 (R >= 0, fractions >= 0), f = y' / D; partials: sum colsum*f,
-// sum R, clamped count; the chunk minimum of f travels in part slot 3.
+// sum R, clamped count; the chunk minimum of f travels in part slot 3. Chunks [c0, c1) of the
+// list (c1 < 0: all); a range must hold whole instances.
 template <typename C, typename A, int CH>
-__global__ void __launch_bounds__(kThreads, 3) k_polish(Common cm, Fields fl, Coef<C> co) {
+__global__ void __launch_bounds__(kThreads, 3) k_polish(Common cm, Fields fl, Coef<C> co, int c0, int c1) {
   using V = typename A::V;
   count_launch(cm.ctl);
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -1267,19 +1269,29 @@ __global__ void __launch_bounds__(kThreads, 3) k_polish(Common cm, Fields fl, Co
     double tot[3], mine[3];
     block_sum_lane0<3>(w, mine);
     if (threadIdx.x == 0) cm.part[(size_t)c * 4 + 3] = (double)smin[0];
-    if (chunk_finish<3>(st, PH_POLISH, I.chunk0, I.nchunks, c, cm.part, mine, tot) && threadIdx.x == 0) {
-      double gmin = 1.0e300;
-      for (int k = 0; k < I.nchunks; ++k) gmin = fmin(gmin, __ldcg(&cm.part[(size_t)(I.chunk0 + k) * 4 + 3]));
-      st.min_f = gmin;
-      st.clamped = (long long)tot[2];
-      st.mass_drift = tot[1] != 0.0 ? fabs(tot[0] - tot[1]) / fabs(tot[1]) : 0.0;
-      st.steps += 1;
-      st.hslot = (st.hslot + 1) % kHist;
-      st.nhist = min(st.nhist + 1, kHist);
-      if (!(gmin >= 0.0)) st.status = ST_NEGATIVE;
+    if (chunk_finish<3>(st, PH_POLISH, I.chunk0, I.nchunks, c, cm.part, mine, tot)) {
+      // the last block of the instance: minimum over its chunks, by the whole block
+      __shared__ double s_min[kThreads / 32];
+      double m = 1.0e300;
+      for (int k = threadIdx.x; k < I.nchunks; k += blockDim.x) m = fmin(m, __ldcg(&cm.part[(size_t)(I.chunk0 + k) * 4 + 3]));
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));
+      if ((threadIdx.x & 31) == 0) s_min[threadIdx.x >> 5] = m;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double gmin = s_min[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) gmin = fmin(gmin, s_min[w]);
+        st.min_f = gmin;
+        st.clamped = (long long)tot[2];
+        st.mass_drift = tot[1] != 0.0 ? fabs(tot[0] - tot[1]) / fabs(tot[1]) : 0.0;
+        st.steps += 1;
+        st.hslot = (st.hslot + 1) % kHist;
+        st.nhist = min(st.nhist + 1, kHist);
+        if (!(gmin >= 0.0)) st.status = ST_NEGATIVE;
+      }
     }
     __syncthreads();
-  });
+  }, c0, c1);
 }
 
 }  // namespace sg

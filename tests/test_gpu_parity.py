@@ -138,6 +138,35 @@ def test_step_host_roundtrip(capi, prec):
     c.close()
 
 
+@pytest.mark.parametrize("prec", [0, 2])
+def test_step_host_forms_equal_device_stepping(capi, prec):
+    """Every form of the host-buffer step (state in and out, in only, out only; one to five steps,
+    so the first and last steps run split around the copies and the middle ones as whole-step
+    graphs) leaves bit for bit the state of the same steps taken on the device."""
+    probs = cases.batch_problems(5, seed=31, dt=1e-2, lo=30, hi=90)
+    a = capi.Batch(probs, precision=prec)
+    b = capi.Batch(probs, precision=prec)
+    a.step(1)
+    b.step(1)
+    n = sum(p.nx * p.ny for p in probs)
+    for nsteps, with_in, with_out in ((1, True, True), (2, True, False), (3, False, True), (5, True, True),
+                                      (1, False, True), (4, True, True)):
+        fin = np.concatenate([a.f(k).ravel() for k in range(len(probs))]) if with_in else None
+        fout = np.full(n, np.nan) if with_out else None
+        a.step_host(nsteps, fin.ctypes.data if with_in else None, fout.ctypes.data if with_out else None)
+        b.step(nsteps)
+        want = np.concatenate([b.f(k).ravel() for k in range(len(probs))])
+        got = np.concatenate([a.f(k).ravel() for k in range(len(probs))])
+        assert np.array_equal(got, want), (nsteps, with_in, with_out)
+        if with_out:
+            assert np.array_equal(fout, want), (nsteps, with_in, with_out)
+        for k in range(len(probs)):
+            sa, sb = a.stats(k), b.stats(k)
+            assert sa["steps"] == sb["steps"] and sa["min_f"] == sb["min_f"] and sa["mass_drift"] == sb["mass_drift"]
+    a.close()
+    b.close()
+
+
 def test_set_f_get_f_and_dirichlet(capi, oracle):
     p = cases.synthetic_problem(20, 15, 1e-2, seed=3)
     s = capi.Solver(p)
