@@ -202,7 +202,7 @@ int sayram_batch_enable_timing(sayram_batch b, int enable);
 int sayram_batch_kernel_times(sayram_batch b, const char** names, double* total_ms,
                               long long* launches, int cap);
 /* Autotuner: times `steps` steps of each launch shape -- cells per block iteration (1024, 2048,
- * 4096) x resident blocks per SM (8, 16, 32) -- on this batch's own instances and keeps the
+ * 4096) x blocks per SM in the grid (8, 16, 32, 64) -- on this batch's own instances and keeps the
  * fastest. The instances' state is restored afterwards, so tuning does not advance the
  * simulation. Writes the choice if the pointers are not NULL. */
 int sayram_batch_autotune(sayram_batch b, int steps, int* chunk_out, int* blocks_per_sm_out);

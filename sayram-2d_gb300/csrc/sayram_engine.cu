@@ -905,14 +905,16 @@ int sayram_batch_s::autotune(int steps, int* best_chunk, int* best_grid) {
   cudaEvent_t e0, e1;
   SG_CUDA(cudaEventCreate(&e0));
   SG_CUDA(cudaEventCreate(&e1));
-  const int chunks[3] = {1024, 2048, 4096}, grids[3] = {8, 16, 32};
+  // blocks per SM: more blocks than fit at once balance the uneven chunks better (on the 4096-
+  // instance batch: 23.2, 21.8, 21.0, 20.8 ms per step for 8, 12, 32, 48)
+  const int chunks[3] = {1024, 2048, 4096}, grids[4] = {8, 16, 32, 64};
   const bool timing_was = timing;
   timing = false;  // per-kernel events would split the graph into a host loop
   double best = 1e300;
   int bc = chunk, bg = gmult, rc = SAYRAM_OK;
   tune_log.clear();
   for (int ci = 0; ci < 3 && rc == SAYRAM_OK; ++ci)
-    for (int gi = 0; gi < 3 && rc == SAYRAM_OK; ++gi) {
+    for (int gi = 0; gi < 4 && rc == SAYRAM_OK; ++gi) {
       chunk = chunks[ci];
       gmult = grids[gi];
       drop_graph();
