@@ -47,6 +47,61 @@ UNIT = "instance-steps/s"
 DT = 1e-2
 
 
+class Ranks:
+    """One process per GPU under torchrun (RANK / LOCAL_RANK / WORLD_SIZE from the environment).
+    Instances are independent, so each rank steps its own shard of the batch and nothing crosses
+    between GPUs on the data path; the process group only lines the ranks up around the timed
+    region and takes the maximum of their times (NCCL on GPUs, gloo without). A single process
+    (no torchrun) needs no process group."""
+
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", str(self.rank)))
+        self.dist = None
+        self.device = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+
+            if torch.cuda.is_available():
+                torch.cuda.set_device(self.local)
+                self.device = torch.device("cuda", self.local)
+                dist.init_process_group("nccl")
+            else:
+                self.device = torch.device("cpu")
+                dist.init_process_group("gloo")
+            self.dist = dist
+            self._torch = torch
+
+    def barrier(self) -> None:
+        if self.dist is not None:
+            self.dist.barrier()
+
+    def _reduce(self, x: float, op) -> float:
+        if self.dist is None:
+            return float(x)
+        t = self._torch.tensor([float(x)], dtype=self._torch.float64, device=self.device)
+        self.dist.all_reduce(t, op=op)
+        return float(t.item())
+
+    def max(self, x: float) -> float:
+        return self._reduce(x, None if self.dist is None else self.dist.ReduceOp.MAX)
+
+    def sum(self, x: float) -> float:
+        return self._reduce(x, None if self.dist is None else self.dist.ReduceOp.SUM)
+
+    def emit(self, line: dict) -> None:
+        """Rank 0 prints the JSON line; the other ranks print nothing."""
+        if self.rank == 0:
+            print(json.dumps(line), flush=True)
+
+    def close(self) -> None:
+        if self.dist is not None:
+            self.dist.destroy_process_group()
+            self.dist = None
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -89,13 +144,15 @@ class Clocks:
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
-    def __init__(self):
+    def __init__(self, local: int = 0):
+        vis = [v for v in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if v.strip()]
+        self.gpu = vis[local] if local < len(vis) else str(local)
         self.proc = None
         self.lines = []
 
     def start(self):
         try:
-            self.proc = subprocess.Popen(["nvidia-smi", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", self.gpu,
                                           f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
@@ -345,18 +402,19 @@ def run_1024(capi):
     return out
 
 
-def run_ours(a):
+def run_ours(a, R: Ranks):
     from sayram2d_gb300 import build, capi
 
     build.build()
     capi.load()
     t0 = time.perf_counter()
-    probs = cases.batch_problems(a.instances, a.seed, DT)
+    # weak scaling: every rank steps a.instances instances of a batch of world * a.instances
+    probs = cases.batch_shard(a.instances, a.seed, DT, R.rank, R.world)
     gen_s = time.perf_counter() - t0
     ncells = int(sum(p.nx * p.ny for p in probs))
     prec = capi.FP32_REFINE_DW if a.precision == "dw" else capi.FP32_REFINE
     other = capi.FP32_REFINE if a.precision == "dw" else capi.FP32_REFINE_DW
-    b = capi.Batch(probs, precision=prec, use_graph=0 if a.no_graph else 1)
+    b = capi.Batch(probs, precision=prec, use_graph=0 if a.no_graph else 1, device=R.local)
     t0 = time.perf_counter()
     if a.launch_shape:
         b.set_launch_shape(*[int(v) for v in a.launch_shape.split(",")])
@@ -367,23 +425,28 @@ def run_ours(a):
     for _ in range(a.warmup):
         b.step(1, allow_not_converged=True)
     l0 = b.launches()
-    clk = Clocks()
+    clk = Clocks(R.local)
     clk.start()
+    R.barrier()  # every rank's warm-up has finished (b.step synchronises its stream)
     b.record_event(0)
     rc = b.step(a.steps, allow_not_converged=True)
     b.record_event(1)
-    ms = b.elapsed_ms(0, 1)
+    ms = R.max(b.elapsed_ms(0, 1))  # elapsed_ms synchronises on the end event
+    R.barrier()
     clocks = clk.stop()
-    launches = b.launches() - l0
-    value = a.instances * a.steps / (ms * 1e-3)
+    launches = int(R.sum(b.launches() - l0))
+    value = R.world * a.instances * a.steps / (ms * 1e-3)
     peak = peak_hbm()
     roof, kern = kernel_roofline(b, probs, peak)
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": a.steps,
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": R.world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded)",
             "config": {"workload": f"batched FP32 Krylov + refinement: {a.instances} instances, nalpha,nE~U[64,256], "
                                    f"rho~U[-0.9,0.9], tau~logU[0.1,10] d, dt={DT} day, refined to rel residual 1e-11",
-                       "instances": a.instances, "cells": ncells, "seed": a.seed,
+                       "instances": R.world * a.instances, "instances_per_gpu": a.instances,
+                       "parallelism": (f"{R.world} ranks, one GPU each, instance-sharded (no data-path collective)"
+                                       if R.world > 1 else "one GPU"),
+                       "cells": int(R.sum(ncells)), "seed": a.seed,
                        "precision": ("fp32_refine_dw: FP32 Krylov, double-word (FP32-pair, ~48-bit) residual/"
                                      "refinement/assembly/checks" if a.precision == "dw" else
                                      "fp32_refine: FP32 Krylov, IEEE FP64 residual/refinement/assembly/checks"),
@@ -399,9 +462,12 @@ def run_ours(a):
     line["max_mass_drift"] = max(s["mass_drift"] for s in st)
     line["max_rel_residual"] = max(s["rel_residual"] for s in st)
     line["not_converged"] = int(sum(1 for s in st if s["status"] != 0))
+    for key, red in (("min_f", min), ("max_mass_drift", max), ("max_rel_residual", max)):
+        line[key] = -R.max(-line[key]) if red is min else R.max(line[key])
+    line["not_converged"] = int(R.sum(line["not_converged"]))
     if not a.quick:
         f32 = [b.f(k) for k in range(len(probs))]
-        # e2e through the public C-ABI with pinned host buffers
+        # e2e through the public C-ABI with pinned host buffers (every rank its own shard)
         L = capi.load()
         nbytes = 8 * ncells
         hin = L.sayram_host_alloc(nbytes)
@@ -410,17 +476,19 @@ def run_ours(a):
         arr_in[:] = np.concatenate([f.ravel() for f in f32])
         b.step_host(1, hin, hout, allow_not_converged=True)  # warm
         e2e_steps = max(3, a.steps // 2)
+        R.barrier()
         t0 = time.perf_counter()
         for s in range(e2e_steps):
             src, dst = (hout, hin) if s % 2 == 0 else (hin, hout)
             b.step_host(1, src, dst, allow_not_converged=True)
-        wall = time.perf_counter() - t0
+        wall = R.max(time.perf_counter() - t0)
         L.sayram_host_free(hin)
         L.sayram_host_free(hout)
-        line["e2e"] = {"value": a.instances * e2e_steps / wall, "unit": UNIT, "h2d_bytes_per_step": nbytes,
-                       "d2h_bytes_per_step": nbytes, "steps": e2e_steps,
-                       "api": "sayram_batch_step_host (pinned host f in/out every step)"}
+        line["e2e"] = {"value": R.world * a.instances * e2e_steps / wall, "unit": UNIT,
+                       "h2d_bytes_per_step": int(R.sum(nbytes)), "d2h_bytes_per_step": int(R.sum(nbytes)),
+                       "steps": e2e_steps, "api": "sayram_batch_step_host (pinned host f in/out every step)"}
         b.close()
+    if not a.quick and R.world == 1:
         # the other refinement arithmetic on the same batch (device-timed, a few steps)
         bo = capi.Batch(probs, precision=other)
         bo.autotune(2)
@@ -466,9 +534,8 @@ def run_ours(a):
         line["speedup_vs_plain_fp64"] = value / plain
         line["cpu_baseline"] = cpu_baseline_single(a.seed, a.instances, a.cpu_seconds)
         line["config_1024"] = run_1024(capi)
-    else:
-        b.close()
-    if a.serve_requests > 0:
+    b.close()
+    if a.serve_requests > 0 and R.world == 1:
         arr, sprobs, ssteps = serving_requests(a.serve_requests, a.serve_rate, a.seed)
         cfg = (f"{a.serve_requests} Poisson requests at {a.serve_rate}/s, n~logU[32,512] (n x n), "
                f"steps~logU[10,2000], dt={DT} day, HBM budget {a.serve_budget_gb} GB")
@@ -477,7 +544,7 @@ def run_ours(a):
         if not a.quick:
             line["serving_plain_fp64"] = {"config": cfg, "precision": "fp64",
                                           **run_serving(capi, arr, sprobs, ssteps, capi.FP64, a.serve_budget_gb)}
-    print(json.dumps(line))
+    R.emit(line)
 
 
 def run_serve_only(a):
@@ -503,17 +570,26 @@ def run_serve_only(a):
 
 def main():
     a = parse()
-    if a.gpus != 1 or int(os.environ.get("WORLD_SIZE", "1")) != 1:
-        raise SystemExit("bench.py runs on one GPU (instances are independent; multi-GPU is replicas only "
-                         "and not part of this build)")
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if a.gpus != world:
+        raise SystemExit(f"--gpus {a.gpus} with WORLD_SIZE={world}: launch N > 1 GPUs with torchrun "
+                         "(one process per GPU)")
     if a.warmup < 3 and a.impl == "ours":
         a.warmup = 3
     if a.impl == "reference":
-        run_reference(a)
-    elif a.serve_only:
-        run_serve_only(a)
-    else:
-        run_ours(a)
+        # the reference's CPU path runs once, on rank 0's host cores; other ranks do no work
+        if int(os.environ.get("RANK", "0")) == 0:
+            run_reference(a)
+        return
+    if a.serve_only:
+        if int(os.environ.get("RANK", "0")) == 0:
+            run_serve_only(a)
+        return
+    R = Ranks()
+    try:
+        run_ours(a, R)
+    finally:
+        R.close()
 
 
 if __name__ == "__main__":

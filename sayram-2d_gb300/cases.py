@@ -369,6 +369,17 @@ def batch_instance(k: int, seed: int, dt: float, size) -> Problem:
     return synthetic_problem(int(a), int(e), dt, seed=seed * 7919 + k, tau=tau, rho=rho)
 
 
+def batch_shard(n_per_rank: int, seed: int, dt: float, rank: int, world: int) -> List[Problem]:
+    """Rank `rank`'s share of a batch of world * n_per_rank instances (weak scaling over GPUs):
+    global instances [rank * n_per_rank, (rank + 1) * n_per_rank), each generated exactly as
+    batch_problems would generate it in the whole batch. Instances are independent, so the
+    shards need no exchange."""
+    if not (0 <= rank < world):
+        raise ValueError(f"rank {rank} outside [0, {world})")
+    sizes = batch_sizes(world * n_per_rank, seed)
+    return [batch_instance(k, seed, dt, sizes[k]) for k in range(rank * n_per_rank, (rank + 1) * n_per_rank)]
+
+
 def batch_problems(n_instances: int, seed: int, dt: float, lo: int = 64, hi: int = 256,
                    sizes: Optional[Sequence] = None) -> List[Problem]:
     """Independent seeded instances: sizes uniform in [lo, hi]^2 (see batch_instance)."""
