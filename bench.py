@@ -116,6 +116,7 @@ def parse():
     ap.add_argument("--serve-requests", type=int, default=600, help="requests in the serving run (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=30.0, help="Poisson arrival rate (requests/s)")
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
+    ap.add_argument("--serve-lanes", type=int, default=2, help="server lanes (2: grids <= 128 in their own lane)")
     ap.add_argument("--serve-only", action="store_true")
     ap.add_argument("--launch-shape", default="",
                     help="CHUNK,BLOCKS_PER_SM instead of the autotuner (e.g. 4096,32; for profiling)")
@@ -342,10 +343,12 @@ def serving_requests(nreq, rate, seed):
     return arrivals, probs, steps
 
 
-def run_serving(capi, arrivals, probs, steps, precision, budget_gb):
+def run_serving(capi, arrivals, probs, steps, precision, budget_gb, lanes=2):
     """Drives a server in real time: submits each request at its arrival time, ticks, polls.
-    Latency = result ready - arrival time (both on the monotonic clock)."""
-    srv = capi.Server(budget_gb * 1e9, max_slots=4096, max_side=512, precision=precision)
+    Latency = result ready - arrival time (both on the monotonic clock). Two lanes by default:
+    grids up to 128 x 128 in their own lane with a quarter of the budget."""
+    srv = capi.Server(budget_gb * 1e9, max_slots=4096, max_side=512, precision=precision, lanes=lanes,
+                      split_side=128, small_fraction=0.25)
     nreq = len(probs)
     t0 = time.monotonic()
     nxt, live, lat, min_f, not_conv = 0, {}, [], float("inf"), 0
@@ -371,7 +374,8 @@ def run_serving(capi, arrivals, probs, steps, precision, budget_gb):
     info = srv.info()
     srv.close()
     lat = np.array(lat) * 1e3
-    return {"requests": nreq, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+    return {"requests": nreq, "lanes": lanes, "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)),
             "mean_ms": float(lat.mean()), "wall_s": wall,
             "instance_steps_per_s": info["instance_steps"] / wall,
             "cell_steps_per_s": float(sum(p.nx * p.ny * int(s) for p, s in zip(probs, steps))) / wall,
@@ -540,10 +544,10 @@ def run_ours(a, R: Ranks):
         cfg = (f"{a.serve_requests} Poisson requests at {a.serve_rate}/s, n~logU[32,512] (n x n), "
                f"steps~logU[10,2000], dt={DT} day, HBM budget {a.serve_budget_gb} GB")
         line["serving"] = {"config": cfg, "precision": "fp32_refine_dw",
-                           **run_serving(capi, arr, sprobs, ssteps, capi.FP32_REFINE_DW, a.serve_budget_gb)}
+                           **run_serving(capi, arr, sprobs, ssteps, capi.FP32_REFINE_DW, a.serve_budget_gb, a.serve_lanes)}
         if not a.quick:
             line["serving_plain_fp64"] = {"config": cfg, "precision": "fp64",
-                                          **run_serving(capi, arr, sprobs, ssteps, capi.FP64, a.serve_budget_gb)}
+                                          **run_serving(capi, arr, sprobs, ssteps, capi.FP64, a.serve_budget_gb, a.serve_lanes)}
     R.emit(line)
 
 
@@ -561,10 +565,10 @@ def run_serve_only(a):
     line = {"metric": "serving latency p50/p99 (ms) and throughput", "unit": "ms", "n_gpus": 1,
             "data": "synthetic (seeded)", "config": {"workload": cfg}}
     line["serving"] = {"precision": "fp32_refine_dw",
-                       **run_serving(capi, arr, sprobs, ssteps, capi.FP32_REFINE_DW, a.serve_budget_gb)}
+                       **run_serving(capi, arr, sprobs, ssteps, capi.FP32_REFINE_DW, a.serve_budget_gb, a.serve_lanes)}
     if not a.quick:
         line["serving_plain_fp64"] = {"precision": "fp64",
-                                      **run_serving(capi, arr, sprobs, ssteps, capi.FP64, a.serve_budget_gb)}
+                                      **run_serving(capi, arr, sprobs, ssteps, capi.FP64, a.serve_budget_gb, a.serve_lanes)}
     print(json.dumps(line))
 
 

@@ -232,13 +232,20 @@ typedef struct sayram_server_s* sayram_server;
 
 typedef struct sayram_server_config {
   double hbm_budget_bytes; /* device bytes the server may use (arena + tables + solver state) */
-  int max_slots;           /* instances resident at once (default 4096) */
+  int max_slots;           /* instances resident at once, per lane (default 4096) */
   int max_side;            /* largest nx or ny accepted (default 1024) */
+  /* Lanes (0 or 1: one). With 2, requests with max(nx, ny) <= lane_split_side (default 128) run
+   * in a lane of their own -- its own stream, arena (lane_small_fraction of the budget, default
+   * 0.25) and work lists -- so that their steps do not wait for the Krylov iterations of large
+   * grids; each tick collects whichever lanes have finished a step and relaunches the idle ones. */
+  int lanes;
+  int lane_split_side;
+  double lane_small_fraction;
 } sayram_server_config;
 
 typedef struct sayram_server_info {
   long long submitted, admitted, completed, waiting, resident;
-  long long ticks;              /* ticks that ran a step */
+  long long ticks;              /* steps run, summed over the lanes */
   long long instance_steps;     /* steps executed, summed over instances */
   double device_bytes;          /* bytes held by the server */
   double arena_cells, arena_cells_used;
@@ -253,7 +260,10 @@ int sayram_server_create(const sayram_server_config* cfg, const sayram_options* 
 /* Copies the problem (arrays are not retained) and queues it for nsteps steps. SAYRAM_ERR_BUDGET
  * if the request could never fit the server (grid larger than max_side or than the arena). */
 int sayram_server_submit(sayram_server s, const sayram_problem* p, int nsteps, long long* id_out);
-/* One scheduling round (admission, one step of every resident instance, completions). */
+/* One scheduling round: every idle lane admits waiting requests and launches one step of its
+ * resident instances; the call returns when at least one lane's step has finished, after copying
+ * out the instances of the finished lanes that reached their step count. With one lane: admission,
+ * one step of every resident instance, completions. */
 int sayram_server_tick(sayram_server s, int* n_completed);
 /* SAYRAM_OK and the result (f alpha-major, stats, submit/done times in seconds of the steady
  * clock) when request id has completed -- the result is then released; SAYRAM_ERR_STATE if not

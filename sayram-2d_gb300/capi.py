@@ -63,7 +63,8 @@ class sayram_dtable(ctypes.Structure):
 
 
 class sayram_server_config(ctypes.Structure):
-    _fields_ = [("hbm_budget_bytes", ctypes.c_double), ("max_slots", ctypes.c_int), ("max_side", ctypes.c_int)]
+    _fields_ = [("hbm_budget_bytes", ctypes.c_double), ("max_slots", ctypes.c_int), ("max_side", ctypes.c_int),
+                ("lanes", ctypes.c_int), ("lane_split_side", ctypes.c_int), ("lane_small_fraction", ctypes.c_double)]
 
 
 class sayram_server_info(ctypes.Structure):
@@ -385,10 +386,12 @@ class Server:
     """Continuous-batching service of solve requests (sayram_server_*)."""
 
     def __init__(self, hbm_budget_bytes: float, max_slots: int = 4096, max_side: int = 1024,
-                 opts: Optional[sayram_options] = None, **kw):
+                 opts: Optional[sayram_options] = None, lanes: int = 1, split_side: int = 0,
+                 small_fraction: float = 0.0, **kw):
         L = load()
         self._L = L
-        cfg = sayram_server_config(float(hbm_budget_bytes), int(max_slots), int(max_side))
+        cfg = sayram_server_config(float(hbm_budget_bytes), int(max_slots), int(max_side), int(lanes),
+                                   int(split_side), float(small_fraction))
         opts = opts if opts is not None else options(**kw)
         h = ctypes.c_void_p()
         check(L.sayram_server_create(ctypes.byref(cfg), ctypes.byref(opts), ctypes.byref(h)), "sayram_server_create")

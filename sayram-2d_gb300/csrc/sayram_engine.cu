@@ -14,6 +14,7 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "host_errors.h"
@@ -1475,7 +1476,10 @@ long long region_cells(int nx, int ny) { return round_up((long long)(ny + 2) * r
 
 }  // namespace
 
-struct sayram_server_s {
+// One lane of the server: an engine with its own stream, arena, slots and queue. A lane runs one
+// step at a time; the server launches every idle lane that has work and collects each lane when
+// its step has finished, so lanes of small and of large instances advance at their own pace.
+struct ServerLane {
   sayram_batch_s eng;
   sayram_server_config cfg{};
   long long arena = 0;
@@ -1488,13 +1492,15 @@ struct sayram_server_s {
   };
   std::vector<Slot> slots;
   std::deque<Request*> waiting;
-  std::map<long long, Result> results;
-  long long next_id = 1;
   sayram_server_info info{};
   bool dirty = false;
+  bool inflight = false;         // a step has been launched and not yet collected
+  cudaEvent_t done_ev = nullptr;  // recorded after the step's launches
+  double t_launch = 0.0, t_begin = 0.0;
 
-  ~sayram_server_s() {
+  ~ServerLane() {
     for (Request* r : waiting) delete r;
+    if (done_ev) cudaEventDestroy(done_ev);
   }
 
   bool take(long long len, long long* off) {  // first fit
@@ -1577,8 +1583,8 @@ struct sayram_server_s {
     return SAYRAM_OK;
   }
 
-  int tick(int* ncomp) {
-    if (ncomp) *ncomp = 0;
+  // admission, work lists, then the step's launches (not waited for)
+  int launch() {
     SG_CUDA(cudaSetDevice(eng.dev));
     const double t0 = now_seconds();
     int rc = admit();
@@ -1593,12 +1599,31 @@ struct sayram_server_s {
     info.lists_seconds += tl - ta;
     if (info.resident == 0) return SAYRAM_OK;
     if ((rc = eng.launch_steps(1))) return rc;
-    SG_CUDA(cudaStreamSynchronize(eng.stream));
+    SG_CUDA(cudaEventRecord(done_ev, eng.stream));
+    inflight = true;
+    t_begin = t0;
+    t_launch = tl;
+    return SAYRAM_OK;
+  }
+
+  // 1 if the launched step has finished, 0 if not yet, < 0 on a CUDA error
+  int ready() {
+    const cudaError_t e = cudaEventQuery(done_ev);
+    if (e == cudaSuccess) return 1;
+    if (e == cudaErrorNotReady) return 0;
+    fail(SAYRAM_ERR_CUDA, std::string("server step: ") + cudaGetErrorString(e));
+    return -1;
+  }
+
+  // after the step: completions (state rows back to the host), then free their slots
+  int finish(std::map<long long, Result>& results, int* ncomp) {
+    if (ncomp) *ncomp = 0;
+    SG_CUDA(cudaSetDevice(eng.dev));
+    inflight = false;
     const double ts = now_seconds();
-    info.step_seconds += ts - tl;
+    info.step_seconds += ts - t_launch;
     info.ticks++;
     info.instance_steps += info.resident;
-    // completions: state rows back to the host, then free the slot
     std::vector<int> fin;
     for (int k = 0; k < cfg.max_slots; ++k)
       if (slots[k].used && ++slots[k].done >= slots[k].nsteps) fin.push_back(k);
@@ -1613,7 +1638,7 @@ struct sayram_server_s {
     }
     SG_CUDA(cudaStreamSynchronize(eng.stream));
     const double t1 = now_seconds();
-    info.busy_seconds += t1 - t0;
+    info.busy_seconds += t1 - t_begin;
     info.collect_seconds += t1 - ts;
     for (size_t q = 0; q < fin.size(); ++q) {
       Slot& S = slots[fin[q]];
@@ -1648,6 +1673,91 @@ struct sayram_server_s {
     if (ncomp) *ncomp = (int)fin.size();
     return SAYRAM_OK;
   }
+
+  // sizes the lane's arrays from its share of the budget (tables, staging, lists, cell arena)
+  int create(const sayram_server_config& c, const sayram_options* opt) {
+    cfg = c;
+    sayram_batch_s& e = eng;
+    int rc = e.set_options(opt);
+    if (!rc) rc = e.init_device();
+    if (rc) return rc;
+    SG_CUDA(cudaEventCreateWithFlags(&done_ev, cudaEventDisableTiming));
+    const long long ms = c.max_side + 1;
+    const double table_bytes = (double)c.max_slots * ms * (1 + 1 + 2 + 2 + 4) * 8.0;
+    const double stage_bytes = 6.0 * (double)c.max_side * c.max_side * 8.0;
+    const double per_cell = (double)sayram_instance_bytes(64, 64, e.opt.precision) /
+                            (double)region_cells(64, 64);  // bytes per arena cell (all arrays)
+    const double avail = c.hbm_budget_bytes - table_bytes - stage_bytes - 64.0 * 1048576.0;
+    const long long cells = (long long)(avail / (per_cell + 4.0 / 1024 * 2 + 8.0 * 4 / 1024));
+    if (cells < region_cells(1, 1) + 64) return fail(SAYRAM_ERR_BUDGET, "HBM budget too small for any instance");
+    const long long side_tiles = (long long)c.max_slots * (c.max_side / sg::kTX + c.max_side / sg::kTY + 2);
+    const int chunks_cap = (int)std::min<long long>(cells / 1024 + c.max_slots + 1, 1LL << 30);
+    const int tiles_cap = (int)std::min<long long>(cells / (sg::kTX * sg::kTY) + side_tiles, 1LL << 30);
+    rc = e.alloc_storage(cells + 64, c.max_slots, chunks_cap, tiles_cap, (long long)c.max_slots * ms,
+                         (long long)c.max_slots * ms, 4LL * c.max_slots * ms,
+                         std::max<long long>(6LL * c.max_side * c.max_side, 1));
+    if (rc) return rc;
+    e.n = c.max_slots;
+    e.pmax = (int)round_up(c.max_side, 4);
+    if ((rc = e.rebuild_lists())) return rc;
+    arena = cells;
+    free_[0] = cells;
+    slots.resize(c.max_slots);
+    info.arena_cells = (double)cells;
+    info.device_bytes = (double)e.bytes;
+    return SAYRAM_OK;
+  }
+
+  // SAYRAM_OK if a request of this grid can ever run in the lane
+  int accepts(int nx, int ny) const {
+    if (nx > cfg.max_side || ny > cfg.max_side) return fail(SAYRAM_ERR_BUDGET, "grid side exceeds the server's max_side");
+    if (region_cells(nx, ny) > arena) return fail(SAYRAM_ERR_BUDGET, "request larger than the HBM budget");
+    return SAYRAM_OK;
+  }
+};
+
+// The server: one lane, or two -- instances with max(nx, ny) <= split in the first (its own
+// share of the budget and of the tables), the rest in the second.
+struct sayram_server_s {
+  std::vector<std::unique_ptr<ServerLane>> lanes;
+  int split = 0;
+  std::map<long long, Result> results;
+  long long next_id = 1;
+
+  ServerLane* lane_for(int nx, int ny) {
+    if (lanes.size() > 1 && std::max(nx, ny) <= split && lanes[0]->accepts(nx, ny) == SAYRAM_OK)
+      return lanes[0].get();
+    return lanes.back().get();
+  }
+
+  int tick(int* ncomp) {
+    if (ncomp) *ncomp = 0;
+    int rc;
+    for (auto& L : lanes)
+      if (!L->inflight && (rc = L->launch())) return rc;
+    bool any = false;
+    for (auto& L : lanes) any = any || L->inflight;
+    if (!any) return SAYRAM_OK;
+    // wait for the first lane whose step finishes, then collect every finished lane
+    int total = 0;
+    for (;;) {
+      bool done = false;
+      for (auto& L : lanes) {
+        if (!L->inflight) continue;
+        const int r = L->ready();
+        if (r < 0) return SAYRAM_ERR_CUDA;
+        if (r == 0) continue;
+        int n = 0;
+        if ((rc = L->finish(results, &n))) return rc;
+        total += n;
+        done = true;
+      }
+      if (done) break;
+      std::this_thread::yield();
+    }
+    if (ncomp) *ncomp = total;
+    return SAYRAM_OK;
+  }
 };
 
 extern "C" {
@@ -1659,53 +1769,31 @@ int sayram_server_create(const sayram_server_config* cfg, const sayram_options* 
   if (c.max_slots <= 0) c.max_slots = 4096;
   if (c.max_side <= 0) c.max_side = 1024;
   if (!(c.hbm_budget_bytes > 0)) return fail(SAYRAM_ERR_ARG, "HBM budget must be positive");
-  sayram_server_s* s = new (std::nothrow) sayram_server_s();
+  const int nl = c.lanes >= 2 ? 2 : 1;
+  const int split = c.lane_split_side > 0 ? c.lane_split_side : 128;
+  const double frac = c.lane_small_fraction > 0 && c.lane_small_fraction < 1 ? c.lane_small_fraction : 0.25;
+  if (nl == 2 && split >= c.max_side) return fail(SAYRAM_ERR_ARG, "lane_split_side must be below max_side");
+  std::unique_ptr<sayram_server_s> s(new (std::nothrow) sayram_server_s());
   if (!s) return fail(SAYRAM_ERR_OOM, "host allocation failed");
-  s->cfg = c;
-  sayram_batch_s& e = s->eng;
-  int rc = e.set_options(opt);
-  if (!rc) rc = e.init_device();
-  if (rc) {
-    std::string m = g_err;
-    delete s;
-    return fail(rc, m);
+  s->split = split;
+  for (int k = 0; k < nl; ++k) {
+    sayram_server_config lc = c;
+    if (nl == 2) {
+      lc.hbm_budget_bytes = c.hbm_budget_bytes * (k == 0 ? frac : 1.0 - frac);
+      if (k == 0) lc.max_side = split;
+    }
+    std::unique_ptr<ServerLane> L(new (std::nothrow) ServerLane());
+    if (!L) return fail(SAYRAM_ERR_OOM, "host allocation failed");
+    int rc = L->create(lc, opt);
+    if (rc) {
+      std::string m = g_err;
+      L.reset();
+      s.reset();
+      return fail(rc, m);
+    }
+    s->lanes.push_back(std::move(L));
   }
-  // budget split: per-slot tables, staging, work lists, then the cell arena
-  const long long ms = c.max_side + 1;
-  const double table_bytes = (double)c.max_slots * ms * (1 + 1 + 2 + 2 + 4) * 8.0;
-  const double stage_bytes = 6.0 * (double)c.max_side * c.max_side * 8.0;
-  const double per_cell = (double)sayram_instance_bytes(64, 64, e.opt.precision) /
-                          (double)region_cells(64, 64);  // bytes per arena cell (all arrays)
-  const double avail = c.hbm_budget_bytes - table_bytes - stage_bytes - 64.0 * 1048576.0;
-  const long long cells = (long long)(avail / (per_cell + 4.0 / 1024 * 2 + 8.0 * 4 / 1024));
-  if (cells < region_cells(1, 1) + 64) {
-    delete s;
-    return fail(SAYRAM_ERR_BUDGET, "HBM budget too small for any instance");
-  }
-  const long long side_tiles = (long long)c.max_slots * (c.max_side / sg::kTX + c.max_side / sg::kTY + 2);
-  const int chunks_cap = (int)std::min<long long>(cells / 1024 + c.max_slots + 1, 1LL << 30);
-  const int tiles_cap = (int)std::min<long long>(cells / (sg::kTX * sg::kTY) + side_tiles, 1LL << 30);
-  rc = e.alloc_storage(cells + 64, c.max_slots, chunks_cap, tiles_cap, (long long)c.max_slots * ms,
-                       (long long)c.max_slots * ms, 4LL * c.max_slots * ms,
-                       std::max<long long>(6LL * c.max_side * c.max_side, 1));
-  if (rc) {
-    std::string m = g_err;
-    delete s;
-    return fail(rc, m);
-  }
-  e.n = c.max_slots;
-  e.pmax = (int)round_up(c.max_side, 4);
-  if ((rc = e.rebuild_lists())) {
-    std::string m = g_err;
-    delete s;
-    return fail(rc, m);
-  }
-  s->arena = cells;
-  s->free_[0] = cells;
-  s->slots.resize(c.max_slots);
-  s->info.arena_cells = (double)cells;
-  s->info.device_bytes = (double)e.bytes;
-  *out = s;
+  *out = s.release();
   g_err.clear();
   return SAYRAM_OK;
 }
@@ -1714,18 +1802,17 @@ int sayram_server_submit(sayram_server s, const sayram_problem* p, int nsteps, l
   if (!s || !p || nsteps < 1) return fail(SAYRAM_ERR_ARG, "bad server, problem or step count");
   int rc = validate_problem(*p);
   if (rc) return rc;
-  if (p->nx > s->cfg.max_side || p->ny > s->cfg.max_side)
-    return fail(SAYRAM_ERR_BUDGET, "grid side exceeds the server's max_side");
-  if (region_cells(p->nx, p->ny) > s->arena) return fail(SAYRAM_ERR_BUDGET, "request larger than the HBM budget");
+  ServerLane* L = s->lane_for(p->nx, p->ny);
+  if ((rc = L->accepts(p->nx, p->ny))) return rc;
   Request* r = new (std::nothrow) Request();
   if (!r) return fail(SAYRAM_ERR_OOM, "host allocation failed");
   r->own(*p);
   r->nsteps = nsteps;
   r->id = s->next_id++;
   r->t_submit = now_seconds();
-  s->waiting.push_back(r);
-  s->info.submitted++;
-  s->info.waiting++;
+  L->waiting.push_back(r);
+  L->info.submitted++;
+  L->info.waiting++;
   if (id_out) *id_out = r->id;
   return SAYRAM_OK;
 }
@@ -1750,8 +1837,26 @@ int sayram_server_poll(sayram_server s, long long id, double* f_out, sayram_stat
 
 int sayram_server_info_get(sayram_server s, sayram_server_info* out) {
   if (!s || !out) return fail(SAYRAM_ERR_ARG, "null server or output");
-  *out = s->info;
-  out->device_bytes = (double)s->eng.bytes;
+  sayram_server_info t{};
+  for (auto& L : s->lanes) {  // sums over the lanes (their step times overlap)
+    const sayram_server_info& i = L->info;
+    t.submitted += i.submitted;
+    t.admitted += i.admitted;
+    t.completed += i.completed;
+    t.waiting += i.waiting;
+    t.resident += i.resident;
+    t.ticks += i.ticks;
+    t.instance_steps += i.instance_steps;
+    t.device_bytes += (double)L->eng.bytes;
+    t.arena_cells += i.arena_cells;
+    t.arena_cells_used += i.arena_cells_used;
+    t.busy_seconds += i.busy_seconds;
+    t.admit_seconds += i.admit_seconds;
+    t.lists_seconds += i.lists_seconds;
+    t.step_seconds += i.step_seconds;
+    t.collect_seconds += i.collect_seconds;
+  }
+  *out = t;
   return SAYRAM_OK;
 }
 

@@ -27,10 +27,13 @@ def _requests():
             for k, (a, e, n) in enumerate(shapes)]
 
 
+@pytest.mark.parametrize("lanes", [1, 2])
 @pytest.mark.parametrize("prec,tol", [(0, 1e-12), (2, 1e-8), (1, 1e-8)])
-def test_same_alone_and_in_the_mix(capi, prec, tol):
+def test_same_alone_and_in_the_mix(capi, prec, tol, lanes):
+    """With two lanes (max side <= 64 in the first), the four small requests and the two large
+    ones step in separate lanes at their own pace; every result is still the request alone."""
     reqs = _requests()
-    srv = capi.Server(2e9, max_slots=16, max_side=256, precision=prec)
+    srv = capi.Server(2e9, max_slots=16, max_side=256, precision=prec, lanes=lanes, split_side=64)
     ids = {}
     # staggered arrivals: two at once, then one per tick while the others run
     ids[srv.submit(*reqs[0])] = 0
@@ -50,7 +53,8 @@ def test_same_alone_and_in_the_mix(capi, prec, tol):
             break
     info = srv.info()
     srv.close()
-    assert len(got) == len(reqs) and info["completed"] == len(reqs)
+    assert len(got) == len(reqs) and info["completed"] == len(reqs) and info["submitted"] == len(reqs)
+    assert info["resident"] == 0 and info["waiting"] == 0
     for k, (p, n) in enumerate(reqs):
         f, st, t0, t1 = got[k]
         assert st["steps"] == n and t1 >= t0
@@ -93,6 +97,15 @@ def test_admission_waits_for_memory(capi):
     assert len(got) == 3
     for k, (p, m) in enumerate(reqs):
         assert rel(got[k][0], _alone(capi, p, m, capi.FP32_REFINE_DW)) <= 1e-8
+
+
+def test_lane_configuration_checked(capi):
+    with pytest.raises(RuntimeError, match="lane_split_side"):
+        capi.Server(1e9, max_slots=4, max_side=128, precision=capi.FP32_REFINE_DW, lanes=2, split_side=128)
+    srv = capi.Server(1e9, max_slots=4, max_side=128, precision=capi.FP32_REFINE_DW, lanes=2, split_side=32)
+    with pytest.raises(RuntimeError, match="max_side"):
+        srv.submit(cases.synthetic_problem(130, 20, 1e-2, seed=1), 2)
+    srv.close()
 
 
 def test_oversized_request_refused(capi):
