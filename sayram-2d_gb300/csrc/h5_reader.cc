@@ -88,6 +88,7 @@ class File {
     uint64_t n = 1;
     for (int k = 0; k < rank; ++k) {
       const uint64_t v = le64(&sb[doff + 8 * k]);
+      need(v < (1ull << 48) && (v == 0 || n <= (1ull << 60) / v), name + ": dataspace dimensions out of range");
       d.dims.push_back((long long)v);
       n *= v;
     }
@@ -106,6 +107,8 @@ class File {
     const int lver = lb[0];
     std::vector<uint8_t> raw;
     const uint64_t bytes = n * esz;
+    // storage that was never written reads as zeros, but only up to the size of the file itself
+    need(bytes <= std::max<uint64_t>(size_, 1ull << 20) * 8, name + ": dataset larger than its file allows");
     if (lver == 3) {
       const int lcls = lb[1];
       if (lcls == 1) {

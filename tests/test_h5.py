@@ -262,6 +262,41 @@ def test_library_reader_refuses_what_it_does_not_read(capi, tmp_path):
         capi.h5_read(str(tmp_path / "not.h5"), "/a")
 
 
+F64_TYPE = bytes.fromhex("11203f00" "08000000" "00004000340b0034ff030000")  # IEEE binary64 LE
+F32_TYPE = bytes.fromhex("11201f00" "04000000" "0000200017080017" "7f000000")  # IEEE binary32 LE
+
+
+def test_library_reader_binary32_and_big_endian(capi, tmp_path):
+    """Files whose datasets are binary32 or big-endian (as other writers produce): the same raw
+    bytes under a patched datatype message read back as what those bytes mean."""
+    a = np.random.default_rng(5).standard_normal(6)
+    p = tmp_path / "a.h5"
+    _write(capi, p, [("/a", a)])
+    # binary32: the 48 bytes of six doubles are twelve floats
+    space6 = b"\x01\x01\x00\x00\x00\x00\x00\x00" + struct.pack("<Q", 6)
+    buf = open(p, "rb").read()
+    assert buf.count(F64_TYPE) == 1 and buf.count(space6) == 1
+    f32 = buf.replace(F64_TYPE, F32_TYPE).replace(space6, space6[:8] + struct.pack("<Q", 12))
+    (tmp_path / "f32.h5").write_bytes(f32)
+    got = capi.h5_read(str(tmp_path / "f32.h5"), "/a")
+    np.testing.assert_array_equal(got, np.frombuffer(a.tobytes(), dtype="<f4").astype(np.float64))
+    # big-endian binary64: byte-swapped data under the byte-order bit
+    q = tmp_path / "b.h5"
+    _write(capi, q, [("/a", a.byteswap())])
+    be = F64_TYPE[:1] + bytes([F64_TYPE[1] | 1]) + F64_TYPE[2:]
+    (tmp_path / "be.h5").write_bytes(open(q, "rb").read().replace(F64_TYPE, be))
+    np.testing.assert_array_equal(capi.h5_read(str(tmp_path / "be.h5"), "/a"), a)
+
+
+def test_library_reader_refuses_absurd_dimensions(capi, tmp_path):
+    p = tmp_path / "a.h5"
+    _write(capi, p, [("/a", np.arange(4.0))])
+    space4 = b"\x01\x01\x00\x00\x00\x00\x00\x00" + struct.pack("<Q", 4)
+    _patched(p, tmp_path / "huge.h5", space4, space4[:8] + struct.pack("<Q", 1 << 50))
+    with pytest.raises(RuntimeError, match="out of range|differs|larger than its file"):
+        capi.h5_read(str(tmp_path / "huge.h5"), "/a")
+
+
 def test_load_dtable(capi, tmp_path):
     """Albert_Young_IO::read_D: a D file written in the reference's layout loads bit for bit;
     mismatched shapes and missing datasets are refused."""
