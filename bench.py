@@ -19,7 +19,7 @@ Prints ONE JSON line:
 and accuracy against FP64 (rel L2 per instance vs the batched FP64 path), min cell, mass drift.
 
 --impl reference times the oracle port on all host cores instead (the reference's own build needs
-Eigen/xtensor/HDF5, which are not available).
+Eigen/xtensor/HDF5, which are not available here).
 """
 from __future__ import annotations
 
@@ -282,7 +282,7 @@ BYTES32 = {
 
 
 # DRAM bytes per processed cell measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the
-# 256-instance case of the same kernels (profiles/*_dw_256instances.md); traffic grows with the
+# 256-instance case of the same kernels (one ncu capture per kernel); traffic grows with the
 # cells processed, so a launch's traffic is this figure times the cells it processed.
 TRAFFIC32 = {"assemble": 175.2, "bicg1": 40.3, "bicg2": 27.9, "resid": 60.9, "polish": 92.9}
 

@@ -2,13 +2,14 @@
  * banded_lu.h -- TEST INFRASTRUCTURE (oracle). Direct banded LU without pivoting.
  *
  * The reference solves M f = R each step with Eigen::SparseLU<SpMat, COLAMDOrdering<int>>
- * (Sayram-2D source/Solver.h:35, source/Solver.cc:361-362). Eigen is a third-party
- * dependency that is not vendored in the reference (no pinned version; README.md lists it by
- * home page only), so the oracle restates "a direct LU solve of M" instead:
+ * (Sayram-2D source/Solver.h:35; analyzePattern at source/Solver.cc:54, factorize and solve at
+ * Solver.cc:277-278). Eigen is a third-party dependency that is not vendored in the reference
+ * (no pinned version; the reference's README.md:69-77 lists it by home page only), so the
+ * oracle restates "a direct LU solve of M" instead:
  *   Gaussian elimination without pivoting on the band of M (lower/upper bandwidth p/q).
  * M is a column-diagonally-dominant M-matrix (its columns sum to G*dx*dy/dt*(1+dt/tau) plus
  * Dirichlet face terms, because every inner face adds +A to a diagonal and -A to the same
- * column, Solver.cc:220-223), and elimination without pivoting is backward stable for
+ * column, Solver.cc:135-138), and elimination without pivoting is backward stable for
  * column-diagonally-dominant matrices.  The solution therefore equals Eigen's up to
  * rounding (~1e-14 relative for these systems).
  *

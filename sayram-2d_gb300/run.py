@@ -1,4 +1,4 @@
-"""The reference's driver (Sayram-2D ``source/main.cc:39-95``) on the GPU path: an ini file in,
+"""The reference's main program (Sayram-2D ``source/main.cc:39-95``) on the GPU path: an ini file in,
 the HDF5 output file out.
 
 ``run(ini)`` does what ``main`` does with a parameter file:

@@ -1,4 +1,4 @@
-"""The HDF5 output writer (include/sayram_h5.h) and the driver loop that uses it (run.py).
+"""The HDF5 output writer (include/sayram_h5.h) and the main.cc loop that uses it (run.py).
 
 The writer is host code: everything here but the last test runs without a GPU. Its files are
 read back with tests/h5read.py, a strict reader of the classic HDF5 format that is itself pinned
@@ -318,7 +318,7 @@ def test_load_dtable(capi, tmp_path):
         capi.load_dtable(str(missing))
 
 
-# ----------------------------------------------------------------------------- the driver
+# ----------------------------------------------------------------------------- the main.cc loop
 def test_run_rejects_a_mismatched_problem(capi, tmp_path):
     from sayram2d_gb300 import cases, run
 
