@@ -478,6 +478,12 @@ class H5File:
         self.close()
         return False
 
+    def __del__(self):  # an unclosed file is finished (and its handle freed) when collected
+        try:
+            self.close()
+        except Exception:
+            pass
+
 
 def h5_read(file: str, path: str) -> np.ndarray:
     """``xt::load_hdf5(file, path)``: one dataset of a classic-format HDF5 file as float64."""
