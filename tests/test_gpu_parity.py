@@ -185,6 +185,38 @@ def test_set_f_get_f_and_dirichlet(capi, oracle):
     s.close()
 
 
+@pytest.mark.parametrize("prec", [0, 2])
+def test_time_dependent_coefficients(capi, oracle, prec):
+    """Equation::update with new G, D and 1/tau between steps (sayram_set_coeffs, the path of
+    Solver.h's time_dependent_coeffs): the steps after the change match the oracle stepping the
+    changed problem from the same state, in a single instance and inside a batch."""
+    import dataclasses
+
+    p = cases.synthetic_problem(40, 30, 1e-2, seed=8)
+    rng = np.random.default_rng(3)
+    scale = rng.uniform(0.5, 2.0, size=(40, 30))
+    q = dataclasses.replace(p, G=p.G * 1.1, Dxx=p.Dxx * scale, Dxy=p.Dxy * 0.5 * scale, Dyy=p.Dyy * scale[::-1, ::-1],
+                            inv_tau=p.inv_tau + 0.3)
+    tol = TOL64 if prec == capi.FP64 else TOL32
+    s = capi.Solver(p, precision=prec)
+    s.step(2)
+    mid = s.f()
+    s.set_coeffs(q.G, q.Dxx, q.Dxy, q.Dyy, q.inv_tau)
+    s.step(3)
+    ref = oracle.step(q, mid, 3)
+    assert rel(s.f(), ref) <= tol and s.f().min() >= 0.0
+    s.close()
+    others = cases.batch_problems(3, seed=9, dt=1e-2, lo=20, hi=50)
+    b = capi.Batch([others[0], p, others[1]], precision=prec)
+    b.step(2)
+    mid_b = b.f(1)
+    b.set_coeffs(1, q.G, q.Dxx, q.Dxy, q.Dyy, q.inv_tau)
+    b.step(3)
+    assert rel(b.f(1), oracle.step(q, mid_b, 3)) <= tol
+    assert rel(b.f(0), oracle.step(others[0], None, 5)) <= tol  # the neighbours are untouched
+    b.close()
+
+
 def test_not_converged_is_reported_not_hidden(capi):
     """A forced non-convergence (one Krylov iteration, two residual checks) returns
     NOT_CONVERGED but the state still advances and stays non-negative."""
