@@ -75,6 +75,23 @@ def test_null_handles_rejected(capi):
     assert L.sayram_batch_get_launch_shape(None, None, None) == capi.ERR_ARG
 
 
+def test_empty_and_bad_requests_rejected_on_host(capi):
+    """An empty batch, a negative step count, a null server and a malformed server config are
+    refused before any CUDA call."""
+    L = capi.load()
+    h = ctypes.c_void_p()
+    pack = _problem_struct(capi)
+    assert L.sayram_batch_create(pack.arr, 0, ctypes.byref(capi.options()), ctypes.byref(h)) == capi.ERR_ARG
+    assert "empty batch" in capi.last_error() and not h.value
+    assert L.sayram_batch_step_host(None, -1, None, None) == capi.ERR_ARG
+    assert L.sayram_server_tick(None, None) == capi.ERR_ARG
+    assert L.sayram_server_submit(None, pack.arr, 1, None) == capi.ERR_ARG
+    cfg = capi.sayram_server_config(0.0, 4, 64, 1, 0, 0.0)
+    assert L.sayram_server_create(ctypes.byref(cfg), ctypes.byref(capi.options()), ctypes.byref(h)) == capi.ERR_ARG
+    assert "budget" in capi.last_error()
+    assert L.sayram_server_create(None, None, ctypes.byref(h)) == capi.ERR_ARG
+
+
 def test_instance_bytes_monotone(capi):
     a = capi.instance_bytes(64, 64, capi.FP32_REFINE)
     b = capi.instance_bytes(128, 128, capi.FP32_REFINE)
