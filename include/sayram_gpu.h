@@ -172,7 +172,10 @@ int sayram_batch_step(sayram_batch b, int nsteps);
  * NULL, writes every instance's f back the same way. Pinned buffers (sayram_host_alloc) copy
  * fastest. The first guess of each step's solve is extrapolated from the last few states; an
  * instance whose f_in differs from the state it holds restarts that history, one given back its
- * own f_out unchanged keeps it (results never depend on the guess, only the iteration count). */
+ * own f_out unchanged keeps it (results never depend on the guess, only the iteration count).
+ * The copies overlap the computation: runs of instances are copied in while the first step
+ * assembles the runs already on the device, and copied out while the last step's positivity
+ * polish finishes the later runs; the result is bit for bit that of sayram_batch_step. */
 int sayram_batch_step_host(sayram_batch b, int nsteps, const double* f_in, double* f_out);
 int sayram_batch_get_f(sayram_batch b, int idx, double* f_out);
 int sayram_batch_set_f(sayram_batch b, int idx, const double* f);
