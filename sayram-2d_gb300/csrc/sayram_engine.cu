@@ -1738,7 +1738,11 @@ struct sayram_server_s {
     bool any = false;
     for (auto& L : lanes) any = any || L->inflight;
     if (!any) return SAYRAM_OK;
-    // wait for the first lane whose step finishes, then collect every finished lane
+    // wait for the first lane whose step finishes, then collect every finished lane (a step
+    // takes milliseconds; one that has not finished after kWaitSeconds is reported, and a later
+    // tick waits for it again)
+    constexpr double kWaitSeconds = 600.0;
+    const double t_wait = now_seconds();
     int total = 0;
     for (;;) {
       bool done = false;
@@ -1753,6 +1757,8 @@ struct sayram_server_s {
         done = true;
       }
       if (done) break;
+      if (now_seconds() - t_wait > kWaitSeconds)
+        return fail(SAYRAM_ERR_TIMEOUT, "server step still running after 600 s");
       std::this_thread::yield();
     }
     if (ncomp) *ncomp = total;
