@@ -318,6 +318,50 @@ def test_load_dtable(capi, tmp_path):
         capi.load_dtable(str(missing))
 
 
+C_PROGRAM = r'''
+#include <stdio.h>
+#include "sayram_h5.h"
+int main(int argc, char** argv) {
+  (void)argc;
+  double a[3] = {5.0, 47.5, 90.0}, f[6] = {1, 2, 3, 4, 5, 6};
+  long long d1[1] = {3}, d2[2] = {3, 2};
+  sayram_h5 h;
+  if (sayram_h5_create(argv[1], &h) != SAYRAM_OK) return 1;
+  if (sayram_h5_write(h, "/alpha0", a, 1, d1) != SAYRAM_OK) return 2;
+  if (sayram_h5_write(h, "/f/0", f, 2, d2) != SAYRAM_OK) return 3;
+  if (sayram_h5_close(h) != SAYRAM_OK) return 4;
+  double* back = NULL;
+  int rank = 0;
+  long long dims[4];
+  if (sayram_h5_read(argv[1], "/f/0", 4, &rank, dims, &back) != SAYRAM_OK) return 5;
+  printf("%d %lld %lld %g\n", rank, dims[0], dims[1], back[5]);
+  sayram_h5_free(back);
+  sayram_dtable t;
+  if (sayram_dtable_load_h5(argv[1], &t) == SAYRAM_OK) return 6;  /* no /E: refused */
+  printf("%s\n", sayram_last_error());
+  return 0;
+}
+'''
+
+
+def test_c_callers(capi, tmp_path):
+    """include/sayram_h5.h from C (C99): write, read back, and a refused D-table load."""
+    import subprocess
+
+    src = tmp_path / "h5.c"
+    src.write_text(C_PROGRAM)
+    exe = tmp_path / "h5c"
+    libdir = os.path.dirname(capi.lib_path())
+    subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-L", libdir, "-lsayram_gpu",
+                    f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe), str(tmp_path / "c.h5")], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, (out.returncode, out.stdout, out.stderr)
+    first, second = out.stdout.strip().splitlines()
+    assert first == "2 3 2 6"
+    assert "no object named 'E'" in second
+    assert h5read.File(str(tmp_path / "c.h5"))["/alpha0"].data.tolist() == [5.0, 47.5, 90.0]
+
+
 # ----------------------------------------------------------------------------- the main.cc loop
 def test_run_rejects_a_mismatched_problem(capi, tmp_path):
     from sayram2d_gb300 import cases, run
