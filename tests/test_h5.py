@@ -363,6 +363,13 @@ def test_c_callers(capi, tmp_path):
 
 
 # ----------------------------------------------------------------------------- the main.cc loop
+def test_run_main_takes_at_most_one_argument(capsys):
+    from sayram2d_gb300 import run
+
+    assert run.main(["a.ini", "b.ini"]) == 1
+    assert "at most one argument" in capsys.readouterr().err
+
+
 def test_run_rejects_a_mismatched_problem(capi, tmp_path):
     from sayram2d_gb300 import cases, run
 
