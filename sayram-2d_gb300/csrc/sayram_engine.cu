@@ -1499,6 +1499,7 @@ struct ServerLane {
   double t_launch = 0.0, t_begin = 0.0;
 
   ~ServerLane() {
+    if (inflight && done_ev) cudaEventSynchronize(done_ev);  // the engine's arrays outlive its step
     for (Request* r : waiting) delete r;
     if (done_ev) cudaEventDestroy(done_ev);
   }
