@@ -157,6 +157,7 @@ class File {
   };
   FILE* fp_;
   uint64_t size_ = 0, base_ = 0, root_ = kUndef;
+  long visits_ = 0;  // B-tree nodes read by this file's lookups
 
   static uint64_t le64(const uint8_t* p) {
     uint64_t v = 0;
@@ -265,6 +266,7 @@ class File {
 
   void search(uint64_t node, const std::vector<uint8_t>& heap, const std::string& name, uint64_t* found, int depth) {
     need(depth < 64, "B-tree too deep");
+    need(++visits_ < (1 << 20), "B-tree has too many nodes (a cycle?)");
     std::vector<uint8_t> h = read(base_ + node, 24);
     need(!std::memcmp(h.data(), "TREE", 4) && h[4] == 0, "group B-tree node");
     const int level = h[5];
