@@ -13,8 +13,15 @@ oracle/ref_case_harness.cc): for each grid and seeded D table, the fields a Solv
 case -- G, Dxx, Dxy, Dyy (interpolated from the table), inv_tau, init_f, the BC types and the
 Dirichlet vertex values.
 
-Run here (where the reference sources exist):  python tests/golden/make_golden.py [cases]
-("cases" regenerates only ref_cases.npz)
+The config-1 prefix (ref_c1_1024_prefix.npz: one 1024 x 1024 instance, dt = 1e-2, f after 1 and
+10 steps) is too large for the reference's build here, whose LU shim is a banded elimination
+(bandwidth 1024). It comes from the C restatement of the reference's assembly (bit-exact with the
+reference build on every small fixture) and SciPy's SuperLU with COLAMD, the algorithm family
+of the reference's Eigen SparseLU; it stores a strided sample of f (every 8th cell in each
+direction), the row and column sums of f and its sum of squares, plus an input digest.
+
+Run here (where the reference sources exist):  python tests/golden/make_golden.py [cases|config1]
+("cases" regenerates only ref_cases.npz, "config1" only the config-1 prefix, ~6 min)
 """
 import hashlib
 import os
@@ -110,8 +117,31 @@ def write_case_fixtures():
     np.savez_compressed(os.path.join(HERE, "ref_cases.npz"), **data)
 
 
+def config1_problem():
+    return cases.synthetic_problem(1024, 1024, 1e-2, seed=11)
+
+
+def write_config1_prefix(nsteps=10):
+    p = config1_problem()
+    out = {"digest": np.frombuffer(bytes.fromhex(input_digest(p)), dtype=np.uint8),
+           "nsteps": np.array([nsteps])}
+    f = oracle.step(p, None, 1, solver="splu")
+    out["f1_sub"] = f[::8, ::8].copy()
+    out["f1_rows"], out["f1_cols"] = f.sum(axis=1), f.sum(axis=0)
+    f = oracle.step(p, f, nsteps - 1, solver="splu")
+    out["fN_sub"] = f[::8, ::8].copy()
+    out["fN_rows"], out["fN_cols"] = f.sum(axis=1), f.sum(axis=0)
+    out["fN_ssq"] = np.array([float((f * f).sum())])
+    out["fN_min"] = np.array([float(f.min())])
+    np.savez_compressed(os.path.join(HERE, "ref_c1_1024_prefix.npz"), **out)
+
+
 def main():
     oracle.build()
+    if sys.argv[1:] == ["config1"]:
+        write_config1_prefix()
+        print("wrote ref_c1_1024_prefix.npz")
+        return
     if oracle.build_ref() is None:
         raise SystemExit("the reference sources are needed to generate fixtures")
     write_case_fixtures()

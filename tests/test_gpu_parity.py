@@ -243,6 +243,32 @@ def test_large_grid_properties(capi, oracle):
     assert f.min() >= 0.0 and st["mass_drift"] <= 1e-9
 
 
+def _c1_close(z, pre, f, tol):
+    sub = f[::8, ::8]
+    assert rel(sub, z[pre + "_sub"]) <= tol, (pre, rel(sub, z[pre + "_sub"]))
+    assert rel(f.sum(axis=1), z[pre + "_rows"]) <= tol, (pre, "rows")
+    assert rel(f.sum(axis=0), z[pre + "_cols"]) <= tol, (pre, "cols")
+
+
+def test_config1_prefix_against_superlu_fixture(capi):
+    """Config 1 at full size (1024 x 1024, dt = 1e-2): 1 and 10 steps of the FP64 drop-in and of
+    the double-word path against the fixture made with the restated assembly and SuperLU
+    (strided sample of f, row and column sums, sum of squares)."""
+    z = np.load(os.path.join(GOLDEN, "ref_c1_1024_prefix.npz"))
+    n = int(z["nsteps"][0])
+    p = cases.synthetic_problem(1024, 1024, 1e-2, seed=11)
+    for prec, tol in ((capi.FP64, TOL64), (capi.FP32_REFINE_DW, TOL32)):
+        s = capi.Solver(p, precision=prec)
+        s.step(1)
+        _c1_close(z, "f1", s.f(), tol)
+        s.step(n - 1)
+        f = s.f()
+        s.close()
+        _c1_close(z, "fN", f, tol)
+        assert abs(float((f * f).sum()) - z["fN_ssq"][0]) <= 2 * tol * z["fN_ssq"][0]
+        assert f.min() >= 0.0
+
+
 def test_config1_size_1024(capi, oracle):
     """The single-instance configuration at full size (1024 x 1024, dt = 1e-2): one step of the
     FP64 path against SuperLU, then size-independent properties over further steps -- the

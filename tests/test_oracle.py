@@ -39,6 +39,22 @@ def test_config0_prefix_vs_reference(oracle):
     assert err <= 1e-13
 
 
+def test_config1_fixture_inputs():
+    """The config-1 prefix fixture was made from exactly the inputs the seeded generator gives
+    (its digest), and its sample and sums agree with each other."""
+    import hashlib
+
+    z = np.load(os.path.join(GOLDEN, "ref_c1_1024_prefix.npz"))
+    p = cases.synthetic_problem(1024, 1024, 1e-2, seed=11)
+    h = hashlib.sha256()
+    for k in ("x_edges", "y_edges", "G", "Dxx", "Dxy", "Dyy", "inv_tau", "f0"):
+        h.update(np.ascontiguousarray(getattr(p, k)).tobytes())
+    assert bytes(z["digest"]) == bytes.fromhex(h.hexdigest())
+    assert z["fN_sub"].shape == (128, 128) and z["fN_rows"].shape == (1024,)
+    assert abs(z["fN_rows"].sum() - z["fN_cols"].sum()) <= 1e-12 * abs(z["fN_rows"].sum())
+    assert z["fN_min"][0] >= 0.0 and (z["fN_sub"] >= 0).all()
+
+
 def test_ini_semantics(tmp_path):
     """nsteps rounds down to a multiple of nplots and dt = T/nsteps (Parameters.cc:58-60)."""
     ini = tmp_path / "p.ini"
