@@ -89,6 +89,22 @@ def load_table_cases():
     return out
 
 
+def ay80_problem():
+    """The reference's own run configuration (p.ini: Albert_Young, 80 x 80, dt = 2e-3) with the
+    fields the reference's Albert_Young built from a seeded D table, and its Solver's f after 50,
+    250 and 500 steps: (problem, {steps: f})."""
+    import numpy as np
+    from sayram2d_gb300 import cases
+
+    z = np.load(os.path.join(GOLDEN, "ref_ay_80x80.npz"))
+    dt = float(z["meta"][0])
+    bc = [int(v) for v in z["bc"]]
+    dirs = [z[f"dir{s}"] if bc[s] == cases.DIRICHLET else None for s in range(4)]
+    p = cases.Problem(80, 80, z["x_edges"], z["y_edges"], dt, bc, z["G"], z["Dxx"], z["Dxy"], z["Dyy"],
+                      z["inv_tau"], z["f0"], dirs, name="ay_80x80")
+    return p, {int(k[1:]): z[k] for k in z.files if k.startswith("f") and k[1:].isdigit()}
+
+
 def case_problem(c):
     """A cases.Problem for a table fixture, built by the host case generators with the
     reference's interpolated D (the generators' G, f0 and inv_tau are compared separately)."""

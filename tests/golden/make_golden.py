@@ -20,8 +20,14 @@ reference build on every small fixture) and SciPy's SuperLU with COLAMD, the alg
 of the reference's Eigen SparseLU; it stores a strided sample of f (every 8th cell in each
 direction), the row and column sums of f and its sum of squares, plus an input digest.
 
-Run here (where the reference sources exist):  python tests/golden/make_golden.py [cases|config1]
-("cases" regenerates only ref_cases.npz, "config1" only the config-1 prefix, ~6 min)
+ref_ay_80x80.npz is the reference's own run configuration (p.ini: Albert_Young, 80 x 80, 500 steps
+of dt = 2e-3) with a seeded D table standing in for its D file: the case fields from the
+reference's Albert_Young and f after 50, 250 and 500 steps of the reference's own Solver.
+
+Run here (where the reference sources exist):
+  python tests/golden/make_golden.py [cases|ay80|config1]
+("cases" regenerates only ref_cases.npz, "ay80" the case fixtures and ref_ay_80x80.npz,
+"config1" only the config-1 prefix, ~6 min)
 """
 import hashlib
 import os
@@ -117,6 +123,36 @@ def write_case_fixtures():
     np.savez_compressed(os.path.join(HERE, "ref_cases.npz"), **data)
 
 
+def ay80_case():
+    """The reference's own run configuration, p.ini:1-27: Albert_Young, 80 x 80 cells, alpha0 from
+    5 to 90 degrees, E from 0.2 to 5 MeV, T = 1 day in 500 steps (dt = 2e-3), saved every 50
+    steps. Its D file (D/AlbertYoung_chorus.h5) is not in the repository: a seeded table stands
+    in for it."""
+    d2r = PI / 180
+    xe = cases.uniform_edges(80, 5 * d2r, 90 * d2r)
+    ye = cases.uniform_edges(80, np.log(0.2), np.log(5.0))
+    return xe, ye, 1.0 / 500, 0.2, 5.0, cases.synthetic_dtable(80)
+
+
+def write_ay80(saves=(50, 250, 500)):
+    xe, ye, dt, Emin, Emax, t = ay80_case()
+    r = oracle.ref_case(0, xe, ye, dt, Emin, Emax, t)
+    data = {"meta": np.array([dt, Emin, Emax], dtype=np.float64), "x_edges": xe, "y_edges": ye}
+    for k in ("alpha0_deg", "E", "Daa", "Dap", "Dpp"):
+        data["table_" + k] = getattr(t, k)
+    for k in ("G", "Dxx", "Dxy", "Dyy", "inv_tau", "f0"):
+        data[k] = r[k]
+    data["bc"] = np.array(r["bc"], dtype=np.float64)
+    for s in range(4):
+        data[f"dir{s}"] = r["dirichlet"][s] if r["dirichlet"][s] is not None else np.zeros(0)
+    p = cases.Problem(80, 80, xe, ye, dt, list(r["bc"]), r["G"], r["Dxx"], r["Dxy"], r["Dyy"], r["inv_tau"],
+                      r["f0"], list(r["dirichlet"]), name="ay_80x80")
+    for n in saves:
+        _, _, f = oracle.ref_run(p, n)
+        data[f"f{n}"] = f
+    np.savez_compressed(os.path.join(HERE, "ref_ay_80x80.npz"), **data)
+
+
 def config1_problem():
     return cases.synthetic_problem(1024, 1024, 1e-2, seed=11)
 
@@ -147,6 +183,10 @@ def main():
     write_case_fixtures()
     if sys.argv[1:] == ["cases"]:
         print("wrote ref_cases.npz")
+        return
+    write_ay80()
+    if sys.argv[1:] == ["ay80"]:
+        print("wrote ref_ay_80x80.npz")
         return
     nsteps = 10
     data = {}

@@ -243,6 +243,25 @@ def test_large_grid_properties(capi, oracle):
     assert f.min() >= 0.0 and st["mass_drift"] <= 1e-9
 
 
+@pytest.mark.parametrize("prec", [0, 2])
+def test_reference_run_configuration_ay80(capi, prec):
+    """The reference's own p.ini run (Albert_Young, 80 x 80, T = 1 day in 500 steps) against the
+    reference Solver's f after 50, 250 and 500 steps."""
+    from conftest import ay80_problem
+
+    p, saved = ay80_problem()
+    tol = TOL64 if prec == capi.FP64 else TOL32
+    s = capi.Solver(p, precision=prec)
+    done = 0
+    for n in sorted(saved):
+        s.step(n - done)
+        done = n
+        f = s.f()
+        assert rel(f, saved[n]) <= tol, (prec, n, rel(f, saved[n]))
+        assert f.min() >= 0.0
+    s.close()
+
+
 def _c1_close(z, pre, f, tol):
     sub = f[::8, ::8]
     assert rel(sub, z[pre + "_sub"]) <= tol, (pre, rel(sub, z[pre + "_sub"]))

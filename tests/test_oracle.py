@@ -39,6 +39,20 @@ def test_config0_prefix_vs_reference(oracle):
     assert err <= 1e-13
 
 
+def test_ay80_run_vs_reference(oracle):
+    """The reference's own p.ini configuration (Albert_Young 80 x 80, 500 steps): the restatement
+    follows the reference's Solver to a few ulps at every saved step."""
+    from conftest import ay80_problem
+
+    p, saved = ay80_problem()
+    f, done = p.f0, 0
+    for n in sorted(saved):
+        f = oracle.step(p, f, n - done)
+        done = n
+        assert np.allclose(f, saved[n], rtol=1e-13, atol=0), n
+        assert f.min() >= 0.0
+
+
 def test_config1_fixture_inputs():
     """The config-1 prefix fixture was made from exactly the inputs the seeded generator gives
     (its digest), and its sample and sums agree with each other."""
