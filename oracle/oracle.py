@@ -57,11 +57,32 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
-def build_ref(reference_root: str = "/root/reference") -> str | None:
-    """Compiles the reference's own solver sources when they are present; returns the path."""
-    if not os.path.isdir(os.path.join(reference_root, "source")):
+ROOT_NOTE = os.path.join(HERE, "_ref", "REFERENCE_ROOT")
+
+
+def reference_root() -> str | None:
+    """The reference's source tree (the directory holding ``source/`` and ``D/``): the
+    ``SAYRAM_REFERENCE`` environment variable, else the tree the last :func:`build_ref` compiled;
+    None when neither names an existing tree (callers skip what needs the reference)."""
+    cands = [os.environ.get("SAYRAM_REFERENCE", "")]
+    if os.path.exists(ROOT_NOTE):
+        with open(ROOT_NOTE) as fh:
+            cands.append(fh.read().strip())
+    for c in cands:
+        if c and os.path.isdir(os.path.join(c, "source")):
+            return c
+    return None
+
+
+def build_ref(reference_root_dir: str | None = None) -> str | None:
+    """Compiles the reference's own solver sources when they are present (the given tree, else
+    :func:`reference_root`) and records the tree in ``_ref/REFERENCE_ROOT``; returns the path."""
+    root = reference_root_dir or reference_root()
+    if not root or not os.path.isdir(os.path.join(root, "source")):
         return REF_PATH if os.path.exists(REF_PATH) else None
-    subprocess.run(["make", "-C", HERE, "-s", "ref", f"REF={reference_root}"], check=True)
+    subprocess.run(["make", "-C", HERE, "-s", "ref", f"REF={root}"], check=True)
+    with open(ROOT_NOTE, "w") as fh:
+        fh.write(os.path.abspath(root) + "\n")
     return REF_PATH
 
 

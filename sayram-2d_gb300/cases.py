@@ -22,6 +22,7 @@ from __future__ import annotations
 import configparser
 import dataclasses
 import math
+import os
 from typing import List, Optional, Sequence
 
 import numpy as np
@@ -197,12 +198,13 @@ def synthetic_problem(
 
 def albert_young_problem(nalpha: int, nE: int, dt: float, seed: int = 0, rho: float = 0.5,
                          alpha0_min_deg: float = 5.0, Emin: float = 0.2, Emax: float = 5.0,
-                         D=None) -> Problem:
-    """Albert_Young's G, f0 and BCs (Albert_Young.h:37-62, Albert_Young.cc:42-92). D is
-    (Dxx, Dxy, Dyy) at the cell centres if given (for example interpolated from a
-    :class:`DTable`); otherwise seeded synthetic fields stand in for the HDF5 table."""
+                         D=None, alpha0_max_deg: float = 90.0) -> Problem:
+    """Albert_Young's G, f0 and BCs (Albert_Young.h:37-62, Albert_Young.cc:42-92) on main.cc's
+    uniform grid (main.cc:20-37). D is (Dxx, Dxy, Dyy) at the cell centres if given (for example
+    interpolated from a :class:`DTable`; zeros when the device interpolates the table afterwards,
+    ``sayram_set_dtable``); otherwise seeded synthetic fields stand in for the HDF5 table."""
     rng = np.random.default_rng(seed)
-    xe = uniform_edges(nalpha, alpha0_min_deg * PI / 180, 90.0 * PI / 180)
+    xe = uniform_edges(nalpha, alpha0_min_deg * PI / 180, alpha0_max_deg * PI / 180)
     ye = uniform_edges(nE, math.log(Emin), math.log(Emax))
     A, Y = np.meshgrid(_centres(xe), _centres(ye), indexing="ij")
 
@@ -228,12 +230,13 @@ def bounce_period(a0, p, L):
 
 
 def albert_young_lc_problem(nalpha: int, nE: int, dt: float, seed: int = 0, rho: float = 0.5,
-                            Emin: float = 0.2, Emax: float = 5.0, D=None) -> Problem:
-    """The loss-cone case (Albert_Young_LC.{h,cc}): alpha0 from 0 deg, zero flux at both alpha0
-    sides, inv_tau = 4/bounce period inside the loss cone (L = 4.5), Dirichlet in E; D as in
-    :func:`albert_young_problem`."""
+                            Emin: float = 0.2, Emax: float = 5.0, D=None, alpha0_min_deg: float = 0.0,
+                            alpha0_max_deg: float = 90.0) -> Problem:
+    """The loss-cone case (Albert_Young_LC.{h,cc}): alpha0 from 0 deg (the ini's alpha0min), zero
+    flux at both alpha0 sides, inv_tau = 4/bounce period inside the loss cone (L = 4.5), Dirichlet
+    in E; D as in :func:`albert_young_problem`."""
     rng = np.random.default_rng(seed)
-    xe = uniform_edges(nalpha, 0.0, 90.0 * PI / 180)
+    xe = uniform_edges(nalpha, alpha0_min_deg * PI / 180, alpha0_max_deg * PI / 180)
     ye = uniform_edges(nE, math.log(Emin), math.log(Emax))
     A, Y = np.meshgrid(_centres(xe), _centres(ye), indexing="ij")
 
@@ -294,10 +297,18 @@ def stretched_edges(n: int, lo: float, hi: float, a: float) -> np.ndarray:
 
 
 # ----------------------------------------------------------------------------- ini front end
+SYNTHETIC, ALBERT_YOUNG, ALBERT_YOUNG_LC = "synthetic", "Albert_Young", "Albert_Young_LC"
+EQUATIONS = (SYNTHETIC, ALBERT_YOUNG, ALBERT_YOUNG_LC)
+
+
 @dataclasses.dataclass
 class RunParams:
-    """The [basic]/[diagnostics] keys of Parameters::read_inp_file (Parameters.cc:35-65) plus the
-    [synthetic] and [solver] sections this project adds."""
+    """The [basic]/[diagnostics]/[diffusion_coefficients] keys of Parameters::read_inp_file
+    (Parameters.cc:35-65) plus the [case], [synthetic] and [solver] sections this project adds.
+
+    ``equation`` is the Equation the run builds: ``Albert_Young`` (what main.cc:49 builds, with D
+    interpolated from ``D/<dID>.h5``), ``Albert_Young_LC`` (its loss-cone variant) or
+    ``synthetic`` (the seeded benchmark case)."""
 
     run_id: str
     nalpha0: int
@@ -315,6 +326,8 @@ class RunParams:
     rho: Optional[float] = None
     precision: str = "fp64"
     tol: float = 1e-12
+    equation: str = SYNTHETIC
+    dID: Optional[str] = None
 
     @property
     def dt(self) -> float:
@@ -323,7 +336,14 @@ class RunParams:
 
 def read_ini(path: str) -> RunParams:
     """Reads an ini file with the reference's semantics: nsteps is rounded down to a multiple of
-    nplots (Parameters.cc:58-60) and dt = T / nsteps."""
+    nplots (Parameters.cc:58-60) and dt = T / nsteps.
+
+    Which Equation it describes: ``[case] equation`` when given; otherwise ``synthetic`` when the
+    file has a ``[synthetic]`` section, and an Albert_Young case when it names a D table
+    (``[diffusion_coefficients] dID``, Parameters.cc:63): ``Albert_Young_LC`` when alpha0 starts
+    at 0 (the loss-cone grid of the reference's ``p_AlbertYoungLC.ini``), ``Albert_Young``
+    otherwise (the reference's ``p.ini``). A file with neither is refused: it never silently
+    becomes a synthetic case."""
     cp = configparser.ConfigParser(inline_comment_prefixes=("#", ";"))
     with open(path) as fh:
         cp.read_file(fh)
@@ -333,23 +353,56 @@ def read_ini(path: str) -> RunParams:
     save_every = nsteps // nplots
     syn = cp["synthetic"] if cp.has_section("synthetic") else {}
     sol = cp["solver"] if cp.has_section("solver") else {}
+    dc = cp["diffusion_coefficients"] if cp.has_section("diffusion_coefficients") else {}
     tau = syn.get("tau", "1.0")
     rho = syn.get("rho", None)
+    dID = dc.get("dID", None)
+    dID = dID.strip() if dID is not None and dID.strip() else None
+    alpha0_min = float(b["alpha0min"])
+    if cp.has_section("case") and cp["case"].get("equation", "").strip():
+        equation = cp["case"]["equation"].strip()
+        if equation not in EQUATIONS:
+            raise ValueError(f"{path}: [case] equation = {equation!r}: expected one of {list(EQUATIONS)}")
+    elif cp.has_section("synthetic"):
+        equation = SYNTHETIC
+    elif dID is not None:
+        equation = ALBERT_YOUNG_LC if alpha0_min == 0.0 else ALBERT_YOUNG
+    else:
+        raise ValueError(f"{path}: no case to run: the file has neither a [synthetic] section nor "
+                         "[diffusion_coefficients] dID (the D table of the Albert_Young cases)")
+    if equation != SYNTHETIC and dID is None:
+        raise ValueError(f"{path}: {equation} needs [diffusion_coefficients] dID (its D table)")
     return RunParams(
         run_id=b["run_id"], nalpha0=int(b["nalpha0"]), nE=int(b["nE"]),
-        alpha0_min_deg=float(b["alpha0min"]), alpha0_max_deg=float(b["alpha0max"]),
+        alpha0_min_deg=alpha0_min, alpha0_max_deg=float(b["alpha0max"]),
         Emin=float(b["Emin"]), Emax=float(b["Emax"]), T=float(b["T"]),
         nsteps=save_every * nplots, nplots=nplots, save_every_step=save_every,
         seed=int(syn.get("seed", 0)), tau=None if str(tau).lower() == "none" else float(tau),
         rho=None if rho is None else float(rho), precision=str(sol.get("precision", "fp64")),
-        tol=float(sol.get("tol", 1e-12)),
+        tol=float(sol.get("tol", 1e-12)), equation=equation, dID=dID,
     )
 
 
+def dtable_path(rp: RunParams, root: str = ".") -> str:
+    """Where the Albert_Young cases read their D table: ``D/<dID>.h5`` relative to the working
+    directory (Albert_Young_IO.cc:19); ``root`` stands for that directory."""
+    if rp.dID is None:
+        raise ValueError(f"run {rp.run_id!r} names no D table")
+    return os.path.join(root, "D", rp.dID + ".h5")
+
+
 def problem_from_params(rp: RunParams) -> Problem:
-    return synthetic_problem(rp.nalpha0, rp.nE, rp.dt, rp.seed, tau=rp.tau, rho=rp.rho,
-                             alpha0_min_deg=rp.alpha0_min_deg, alpha0_max_deg=rp.alpha0_max_deg,
-                             Emin=rp.Emin, Emax=rp.Emax)
+    """The Problem an ini file describes. For the Albert_Young cases the D fields are left zero:
+    they come from the D table, interpolated on the device after the solver is created
+    (``Solver.set_dtable``, as ``run.run`` does)."""
+    if rp.equation == SYNTHETIC:
+        return synthetic_problem(rp.nalpha0, rp.nE, rp.dt, rp.seed, tau=rp.tau, rho=rp.rho,
+                                 alpha0_min_deg=rp.alpha0_min_deg, alpha0_max_deg=rp.alpha0_max_deg,
+                                 Emin=rp.Emin, Emax=rp.Emax)
+    zero = np.zeros((rp.nalpha0, rp.nE))
+    mk = albert_young_problem if rp.equation == ALBERT_YOUNG else albert_young_lc_problem
+    return mk(rp.nalpha0, rp.nE, rp.dt, Emin=rp.Emin, Emax=rp.Emax, D=(zero, zero, zero),
+              alpha0_min_deg=rp.alpha0_min_deg, alpha0_max_deg=rp.alpha0_max_deg)
 
 
 # ----------------------------------------------------------------------------- batch workloads

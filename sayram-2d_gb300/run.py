@@ -6,6 +6,10 @@ the HDF5 output file out.
 * ``Parameters`` (``Parameters.cc:3-17``): reads the ini (:func:`cases.read_ini`, with the
   reference's ``nsteps`` rounding and ``dt = T / nsteps``), creates ``./output/<run_id>/`` and
   copies the ini file there as ``<run_id>.ini``;
+* ``Albert_Young eq(paras, m)`` (``main.cc:49``): :func:`case_of` -- G, f0, the BCs and the loss
+  term on the host, the D table from ``D/<dID>.h5`` (``Albert_Young_IO.cc:17-36``, read by the
+  library's HDF5 reader) interpolated on the device (``Albert_Young.cc:94-134``); the loss-cone
+  variant ``Albert_Young_LC`` and the seeded ``[synthetic]`` case are chosen by the ini;
 * ``Solver solver(m, &eq)`` (``main.cc:51``): the drop-in :class:`capi.Solver`;
 * ``HighFive::File(..._data.h5, Overwrite)`` (``main.cc:56-57``): :class:`capi.H5File`;
 * ``/alpha0 = x / pi * 180`` and ``/logEN = y - ln E0`` (``main.cc:59-66``), ``/f/0`` (``:74``);
@@ -52,14 +56,34 @@ def write_axes(h5: "capi.H5File", problem: cases.Problem) -> None:
     h5.write("/logEN", y - math.log(cases.E0))
 
 
+def case_of(rp: cases.RunParams, root: str = "."):
+    """The Equation an ini describes (``Albert_Young eq(paras, m)``, main.cc:49): its Problem and,
+    for the Albert_Young cases, the D table read from ``D/<dID>.h5`` under ``root``
+    (Albert_Young_IO::read_D, Albert_Young_IO.cc:17-36), else None. A missing or unreadable table
+    is an error, as in the reference (its HDF5 read throws)."""
+    prob = cases.problem_from_params(rp)
+    if rp.equation == cases.SYNTHETIC:
+        return prob, None
+    path = cases.dtable_path(rp, root)
+    if not os.path.isfile(path):
+        raise FileNotFoundError(f"{rp.equation} run {rp.run_id!r}: D table {path} not found")
+    return prob, capi.load_dtable(path)
+
+
 def run(ini_path: str, root: str = ".", problem: Optional[cases.Problem] = None,
         precision: Optional[str] = None) -> str:
     """Runs the case an ini file describes and returns the path of its HDF5 output.
 
-    ``problem`` replaces the case the ini's ``[synthetic]`` section generates (same grid and
-    ``dt`` expected); ``precision`` replaces its ``[solver] precision``."""
+    The case is the ini's (:func:`cases.read_ini`): an Albert_Young case takes its D table from
+    ``<root>/D/<dID>.h5`` and interpolates it on the device (``constructD``,
+    Albert_Young.cc:112-134); a ``[synthetic]`` ini generates its seeded fields. ``problem``
+    replaces the case entirely (same grid expected; no D table is read then); ``precision``
+    replaces the ini's ``[solver] precision``."""
     rp = cases.read_ini(ini_path)
-    prob = problem if problem is not None else cases.problem_from_params(rp)
+    if problem is not None:
+        prob, table = problem, None
+    else:
+        prob, table = case_of(rp, root)
     if (prob.nx, prob.ny) != (rp.nalpha0, rp.nE):
         raise ValueError(f"problem grid {prob.nx}x{prob.ny} differs from the ini's {rp.nalpha0}x{rp.nE}")
     name = precision or rp.precision
@@ -69,6 +93,12 @@ def run(ini_path: str, root: str = ".", problem: Optional[cases.Problem] = None,
     os.makedirs(out, exist_ok=True)
     shutil.copyfile(ini_path, os.path.join(out, rp.run_id + ".ini"))  # Parameters.cc:10-16
     solver = capi.Solver(prob, precision=PRECISIONS[name], tol=rp.tol)
+    if table is not None:
+        try:
+            solver.set_dtable(table)
+        except Exception:
+            solver.close()
+            raise
     path = output_file(rp, root)
     try:
         with capi.H5File(path) as h5:

@@ -89,20 +89,38 @@ def load_table_cases():
     return out
 
 
-def ay80_problem():
-    """The reference's own run configuration (p.ini: Albert_Young, 80 x 80, dt = 2e-3) with the
-    fields the reference's Albert_Young built from a seeded D table, and its Solver's f after 50,
-    250 and 500 steps: (problem, {steps: f})."""
+def ay80_table():
+    """The reference's D table (D/AlbertYoung_chorus.h5) as stored in the fixture."""
     import numpy as np
     from sayram2d_gb300 import cases
 
     z = np.load(os.path.join(GOLDEN, "ref_ay_80x80.npz"))
-    dt = float(z["meta"][0])
-    bc = [int(v) for v in z["bc"]]
-    dirs = [z[f"dir{s}"] if bc[s] == cases.DIRICHLET else None for s in range(4)]
-    p = cases.Problem(80, 80, z["x_edges"], z["y_edges"], dt, bc, z["G"], z["Dxx"], z["Dxy"], z["Dyy"],
-                      z["inv_tau"], z["f0"], dirs, name="ay_80x80")
-    return p, {int(k[1:]): z[k] for k in z.files if k.startswith("f") and k[1:].isdigit()}
+    return cases.DTable(*[z["table_" + k] for k in ("alpha0_deg", "E", "Daa", "Dap", "Dpp")])
+
+
+def ay80_problem(name="ay"):
+    """The reference's own run configurations fed its own D table: ``ay`` (p.ini: Albert_Young,
+    80 x 80, alpha0 from 5 deg, dt = 2e-3) or ``lc`` (p_AlbertYoungLC.ini: Albert_Young_LC, alpha0
+    from 0 deg). Returns (problem with the fields the reference's case built, {steps: f of the
+    reference's Solver after that many steps}); saves every 50 steps up to 500."""
+    import numpy as np
+    from sayram2d_gb300 import cases
+
+    z = np.load(os.path.join(GOLDEN, "ref_ay_80x80.npz"))
+    g = lambda k: z[f"{name}/{k}"]
+    which, dt, Emin, Emax = g("meta")
+    bc = [int(v) for v in g("bc")]
+    dirs = [g(f"dir{s}") if bc[s] == cases.DIRICHLET else None for s in range(4)]
+    p = cases.Problem(80, 80, g("x_edges"), g("y_edges"), float(dt), bc, g("G"), g("Dxx"), g("Dxy"),
+                      g("Dyy"), g("inv_tau"), g("f0"), dirs, name=f"ay80_{name}")
+    return p, {int(n): g(f"f{int(n)}") for n in z["saves"]}
+
+
+def reference_tree():
+    """The reference's source tree when this machine has it (oracle.reference_root), else None."""
+    import oracle as orc  # the checker (tests only)
+
+    return orc.reference_root()
 
 
 def case_problem(c):

@@ -20,11 +20,15 @@ reference build on every small fixture) and SciPy's SuperLU with COLAMD, the alg
 of the reference's Eigen SparseLU; it stores a strided sample of f (every 8th cell in each
 direction), the row and column sums of f and its sum of squares, plus an input digest.
 
-ref_ay_80x80.npz is the reference's own run configuration (p.ini: Albert_Young, 80 x 80, 500 steps
-of dt = 2e-3) with a seeded D table standing in for its D file: the case fields from the
-reference's Albert_Young and f after 50, 250 and 500 steps of the reference's own Solver.
+ref_ay_80x80.npz is the reference's own run configurations (p.ini: Albert_Young, 80 x 80, alpha0
+from 5 deg, 500 steps of dt = 2e-3, saved every 50 steps; p_AlbertYoungLC.ini: the same with
+alpha0 from 0 deg, run with Albert_Young_LC) fed the reference's own D table,
+D/AlbertYoung_chorus.h5, read by the library's HDF5 reader (sayram_dtable_load_h5): the table's
+values (so that tests can write the D file anywhere, the GPU host included), the case fields from
+the reference's Albert_Young / Albert_Young_LC, and f at every save (/f/1 .. /f/10) of the
+reference's own Solver.
 
-Run here (where the reference sources exist):
+The reference tree is $SAYRAM_REFERENCE (default /root/reference). Run where it exists:
   python tests/golden/make_golden.py [cases|ay80|config1]
 ("cases" regenerates only ref_cases.npz, "ay80" the case fixtures and ref_ay_80x80.npz,
 "config1" only the config-1 prefix, ~6 min)
@@ -123,33 +127,49 @@ def write_case_fixtures():
     np.savez_compressed(os.path.join(HERE, "ref_cases.npz"), **data)
 
 
-def ay80_case():
-    """The reference's own run configuration, p.ini:1-27: Albert_Young, 80 x 80 cells, alpha0 from
-    5 to 90 degrees, E from 0.2 to 5 MeV, T = 1 day in 500 steps (dt = 2e-3), saved every 50
-    steps. Its D file (D/AlbertYoung_chorus.h5) is not in the repository: a seeded table stands
-    in for it."""
+REFERENCE = os.environ.get("SAYRAM_REFERENCE") or "/root/reference"
+AY80_SAVES = tuple(range(50, 501, 50))
+
+
+def ay80_table():
+    """The reference's D table D/AlbertYoung_chorus.h5 (p.ini:25-26), read by the library's HDF5
+    reader."""
+    from sayram2d_gb300 import build, capi
+
+    build.build()
+    return capi.load_dtable(os.path.join(REFERENCE, "D", "AlbertYoung_chorus.h5"))
+
+
+def ay80_cases():
+    """p.ini:1-27 and p_AlbertYoungLC.ini: 80 x 80 cells, E from 0.2 to 5 MeV, T = 1 day in 500
+    steps (dt = 2e-3); alpha0 from 5 deg (Albert_Young, which 0) or 0 deg (Albert_Young_LC,
+    which 1) to 90 deg (main.cc:20-37)."""
     d2r = PI / 180
-    xe = cases.uniform_edges(80, 5 * d2r, 90 * d2r)
     ye = cases.uniform_edges(80, np.log(0.2), np.log(5.0))
-    return xe, ye, 1.0 / 500, 0.2, 5.0, cases.synthetic_dtable(80)
+    return {"ay": (0, cases.uniform_edges(80, 5 * d2r, 90 * d2r), ye),
+            "lc": (1, cases.uniform_edges(80, 0 * d2r, 90 * d2r), ye)}
 
 
-def write_ay80(saves=(50, 250, 500)):
-    xe, ye, dt, Emin, Emax, t = ay80_case()
-    r = oracle.ref_case(0, xe, ye, dt, Emin, Emax, t)
-    data = {"meta": np.array([dt, Emin, Emax], dtype=np.float64), "x_edges": xe, "y_edges": ye}
+def write_ay80():
+    t = ay80_table()
+    dt, Emin, Emax = 1.0 / 500, 0.2, 5.0
+    data = {"saves": np.array(AY80_SAVES)}
     for k in ("alpha0_deg", "E", "Daa", "Dap", "Dpp"):
         data["table_" + k] = getattr(t, k)
-    for k in ("G", "Dxx", "Dxy", "Dyy", "inv_tau", "f0"):
-        data[k] = r[k]
-    data["bc"] = np.array(r["bc"], dtype=np.float64)
-    for s in range(4):
-        data[f"dir{s}"] = r["dirichlet"][s] if r["dirichlet"][s] is not None else np.zeros(0)
-    p = cases.Problem(80, 80, xe, ye, dt, list(r["bc"]), r["G"], r["Dxx"], r["Dxy"], r["Dyy"], r["inv_tau"],
-                      r["f0"], list(r["dirichlet"]), name="ay_80x80")
-    for n in saves:
-        _, _, f = oracle.ref_run(p, n)
-        data[f"f{n}"] = f
+    for name, (which, xe, ye) in ay80_cases().items():
+        r = oracle.ref_case(which, xe, ye, dt, Emin, Emax, t)
+        data[name + "/meta"] = np.array([which, dt, Emin, Emax], dtype=np.float64)
+        data[name + "/x_edges"], data[name + "/y_edges"] = xe, ye
+        for k in ("G", "Dxx", "Dxy", "Dyy", "inv_tau", "f0"):
+            data[name + "/" + k] = r[k]
+        data[name + "/bc"] = np.array(r["bc"], dtype=np.float64)
+        for s in range(4):
+            data[name + f"/dir{s}"] = r["dirichlet"][s] if r["dirichlet"][s] is not None else np.zeros(0)
+        p = cases.Problem(80, 80, xe, ye, dt, list(r["bc"]), r["G"], r["Dxx"], r["Dxy"], r["Dyy"],
+                          r["inv_tau"], r["f0"], list(r["dirichlet"]), name="ay80_" + name)
+        for n in AY80_SAVES:
+            _, _, f = oracle.ref_run(p, n)
+            data[name + f"/f{n}"] = f
     np.savez_compressed(os.path.join(HERE, "ref_ay_80x80.npz"), **data)
 
 
@@ -178,8 +198,8 @@ def main():
         write_config1_prefix()
         print("wrote ref_c1_1024_prefix.npz")
         return
-    if oracle.build_ref() is None:
-        raise SystemExit("the reference sources are needed to generate fixtures")
+    if oracle.build_ref(REFERENCE) is None:
+        raise SystemExit("the reference sources are needed to generate fixtures ($SAYRAM_REFERENCE)")
     write_case_fixtures()
     if sys.argv[1:] == ["cases"]:
         print("wrote ref_cases.npz")

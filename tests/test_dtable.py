@@ -15,6 +15,24 @@ pytestmark = pytest.mark.gpu
 TABLE_CASES = load_table_cases()
 
 
+def _reference_table_cases():
+    """The reference's own D table (D/AlbertYoung_chorus.h5) on the grids of its run files, with
+    the fields the reference's Albert_Young / Albert_Young_LC built from it."""
+    from conftest import ay80_problem, ay80_table
+
+    out = {}
+    for name, which in (("ay", 0), ("lc", 1)):
+        p, _ = ay80_problem(name)
+        out["ref_table_" + name + "_80x80"] = {
+            "which": which, "dt": p.dt, "Emin": 0.2, "Emax": 5.0, "x_edges": p.x_edges, "y_edges": p.y_edges,
+            "table": ay80_table(), "G": p.G, "Dxx": p.Dxx, "Dxy": p.Dxy, "Dyy": p.Dyy, "inv_tau": p.inv_tau,
+            "f0": p.f0, "bc": p.bc, "dirichlet": p.dirichlet}
+    return out
+
+
+TABLE_CASES.update(_reference_table_cases())
+
+
 def with_D(p, D):
     q = cases.Problem(p.nx, p.ny, p.x_edges, p.y_edges, p.dt, list(p.bc), p.G, *D, p.inv_tau, p.f0,
                       p.dirichlet, name=p.name)

@@ -13,7 +13,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, c0_problem, load_small, problem_from
+from conftest import GOLDEN, ROOT, c0_problem, load_small, problem_from
 from sayram2d_gb300 import cases
 
 pytestmark = pytest.mark.gpu
@@ -243,13 +243,15 @@ def test_large_grid_properties(capi, oracle):
     assert f.min() >= 0.0 and st["mass_drift"] <= 1e-9
 
 
+@pytest.mark.parametrize("name", ["ay", "lc"])
 @pytest.mark.parametrize("prec", [0, 2])
-def test_reference_run_configuration_ay80(capi, prec):
-    """The reference's own p.ini run (Albert_Young, 80 x 80, T = 1 day in 500 steps) against the
-    reference Solver's f after 50, 250 and 500 steps."""
+def test_reference_run_configuration_ay80(capi, prec, name):
+    """The reference's own run configurations (p.ini: Albert_Young; p_AlbertYoungLC.ini:
+    Albert_Young_LC; 80 x 80, T = 1 day in 500 steps) with the fields the reference's case built
+    from its own D table, against the reference Solver's f at every save (every 50 steps)."""
     from conftest import ay80_problem
 
-    p, saved = ay80_problem()
+    p, saved = ay80_problem(name)
     tol = TOL64 if prec == capi.FP64 else TOL32
     s = capi.Solver(p, precision=prec)
     done = 0
@@ -260,6 +262,41 @@ def test_reference_run_configuration_ay80(capi, prec):
         assert rel(f, saved[n]) <= tol, (prec, n, rel(f, saved[n]))
         assert f.min() >= 0.0
     s.close()
+
+
+@pytest.mark.parametrize("name,ini", [("ay", "albert_young_80x80.ini"), ("lc", "albert_young_lc_80x80.ini")])
+@pytest.mark.parametrize("prec", ["fp64", "fp32_refine_dw"])
+def test_run_reference_ini_with_its_d_table(capi, tmp_path, prec, name, ini):
+    """main.cc end to end on the reference's run files (the same keys as its p.ini and
+    p_AlbertYoungLC.ini): run.run reads the ini, selects Albert_Young / Albert_Young_LC, reads
+    D/AlbertYoung_chorus.h5 (written here from the reference's table values with the library's
+    own writer), interpolates D on the device and writes /f/0 .. /f/10; every save is compared with
+    the reference Solver's f at that step (FP64 drop-in <= 1e-10, double-word path <= 1e-8)."""
+    import shutil
+
+    from conftest import ay80_problem, ay80_table
+    from sayram2d_gb300 import run
+
+    p, saved = ay80_problem(name)
+    t = ay80_table()
+    os.makedirs(tmp_path / "D")
+    with capi.H5File(str(tmp_path / "D" / "AlbertYoung_chorus.h5")) as h5:
+        h5.write("/alpha0", t.alpha0_deg)
+        h5.write("/E", t.E)
+        h5.write("/Daa", t.Daa)
+        h5.write("/Dap", t.Dap)
+        h5.write("/Dpp", t.Dpp)
+    src = tmp_path / ini
+    shutil.copyfile(os.path.join(ROOT, "sayram-2d_gb300", "configs", ini), src)
+    path = run.run(str(src), root=str(tmp_path), precision=prec)
+    tol = TOL64 if prec == "fp64" else TOL32
+    f0 = capi.h5_read(path, "/f/0")
+    assert np.allclose(f0, p.f0, rtol=1e-13, atol=0.0)
+    for k, n in enumerate(sorted(saved), start=1):
+        f = capi.h5_read(path, f"/f/{k}")
+        assert rel(f, saved[n]) <= tol, (prec, name, k, rel(f, saved[n]))
+        assert f.min() >= 0.0
+    np.testing.assert_array_equal(capi.h5_read(path, "/t"), np.linspace(0.0, 1.0, 11))
 
 
 def _c1_close(z, pre, f, tol):

@@ -5,7 +5,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, c0_problem, load_small, problem_from
+from conftest import GOLDEN, ROOT, c0_problem, load_small, problem_from
 from sayram2d_gb300 import cases
 
 
@@ -39,18 +39,116 @@ def test_config0_prefix_vs_reference(oracle):
     assert err <= 1e-13
 
 
-def test_ay80_run_vs_reference(oracle):
-    """The reference's own p.ini configuration (Albert_Young 80 x 80, 500 steps): the restatement
-    follows the reference's Solver to a few ulps at every saved step."""
+@pytest.mark.parametrize("name", ["ay", "lc"])
+def test_ay80_run_vs_reference(oracle, name):
+    """The reference's own run configurations (p.ini: Albert_Young; p_AlbertYoungLC.ini:
+    Albert_Young_LC; 80 x 80, 500 steps) with the reference's own D table: the restatement follows
+    the reference's Solver to a few ulps at every save."""
     from conftest import ay80_problem
 
-    p, saved = ay80_problem()
+    p, saved = ay80_problem(name)
+    assert sorted(saved) == list(range(50, 501, 50))
     f, done = p.f0, 0
     for n in sorted(saved):
         f = oracle.step(p, f, n - done)
         done = n
         assert np.allclose(f, saved[n], rtol=1e-13, atol=0), n
         assert f.min() >= 0.0
+
+
+@pytest.mark.parametrize("name", ["ay", "lc"])
+def test_ay80_fields_from_the_reference_table(oracle, name):
+    """constructD on the reference's own D table: the restatement's interpolated D fields equal the
+    ones the reference's Albert_Young / Albert_Young_LC built (Albert_Young.cc:112-134), and the
+    host case generators give its G, f0, inv_tau and Dirichlet values to a few ulps."""
+    from conftest import ay80_problem, ay80_table
+
+    p, _ = ay80_problem(name)
+    D = oracle.dtable_fields(p.x_edges, p.y_edges, ay80_table())
+    for k, d in zip(("Dxx", "Dxy", "Dyy"), D):
+        assert np.allclose(d, getattr(p, k), rtol=1e-14, atol=0.0), k
+    mk = cases.albert_young_problem if name == "ay" else cases.albert_young_lc_problem
+    q = mk(80, 80, p.dt, D=D, alpha0_min_deg=5.0 if name == "ay" else 0.0)
+    np.testing.assert_array_equal(q.x_edges, p.x_edges)
+    np.testing.assert_array_equal(q.y_edges, p.y_edges)
+    assert q.bc == p.bc
+    for k in ("G", "f0", "inv_tau"):
+        assert np.allclose(getattr(q, k), getattr(p, k), rtol=1e-13, atol=0.0), k
+    for s in range(4):
+        assert (q.dirichlet[s] is None) == (p.dirichlet[s] is None)
+        if p.dirichlet[s] is not None:
+            assert np.allclose(q.dirichlet[s], p.dirichlet[s], rtol=1e-13, atol=0.0), s
+
+
+def test_reference_d_table_read_by_the_library(capi):
+    """The reference's D file (D/AlbertYoung_chorus.h5: 91 alpha0 x 49 E) as the library's reader
+    gives it (sayram_dtable_load_h5, Albert_Young_IO::read_D): what the fixture holds, and -- where
+    the reference tree is present -- the same values an independent reader (tests/h5read.py)
+    takes from the file, bit for bit."""
+    from conftest import ay80_table, reference_tree
+
+    t = ay80_table()
+    assert t.alpha0_deg.shape == (91,) and t.E.shape == (49,)
+    assert t.Daa.shape == t.Dap.shape == t.Dpp.shape == (91, 49)
+    assert t.alpha0_deg[0] == 0.0 and t.alpha0_deg[-1] == 90.0
+    assert np.all(np.diff(t.alpha0_deg) > 0) and np.all(np.diff(t.E) > 0)
+    assert abs(t.E[0] - 0.1) < 1e-12 and abs(t.E[-1] - 5.0) < 1e-12
+    ref = reference_tree()
+    if ref is None:
+        pytest.skip("reference tree not present: fixture checked only")
+    path = os.path.join(ref, "D", "AlbertYoung_chorus.h5")
+    got = capi.load_dtable(path)
+    import h5read
+
+    indep = h5read.File(path)
+    for k, name in (("alpha0_deg", "/alpha0"), ("E", "/E"), ("Daa", "/Daa"), ("Dap", "/Dap"), ("Dpp", "/Dpp")):
+        np.testing.assert_array_equal(getattr(got, k), getattr(t, k))
+        np.testing.assert_array_equal(indep[name].data, getattr(t, k))
+
+
+def test_ini_selects_the_reference_cases(tmp_path):
+    """The reference's run files select the Equation main.cc builds: [diffusion_coefficients] dID
+    -> Albert_Young (p.ini), alpha0min = 0 -> Albert_Young_LC (p_AlbertYoungLC.ini), an explicit
+    [case] equation wins; an ini with neither a [synthetic] section nor a dID is refused."""
+    cfg = os.path.join(ROOT, "sayram-2d_gb300", "configs")
+    ay = cases.read_ini(os.path.join(cfg, "albert_young_80x80.ini"))
+    assert (ay.equation, ay.dID, ay.nsteps, ay.save_every_step, ay.dt) == \
+        (cases.ALBERT_YOUNG, "AlbertYoung_chorus", 500, 50, 1.0 / 500)
+    lc = cases.read_ini(os.path.join(cfg, "albert_young_lc_80x80.ini"))
+    assert (lc.equation, lc.alpha0_min_deg) == (cases.ALBERT_YOUNG_LC, 0.0)
+    assert cases.read_ini(os.path.join(cfg, "c0.ini")).equation == cases.SYNTHETIC
+    assert cases.dtable_path(ay, "/data") == os.path.join("/data", "D", "AlbertYoung_chorus.h5")
+    body = ("[basic]\nrun_id=x\nnalpha0=8\nnE=6\nalpha0min=5\nalpha0max=90\nEmin=0.2\nEmax=5\n"
+            "T=1.0\nnsteps=10\n[diagnostics]\nnplots=2\n")
+    bare = tmp_path / "bare.ini"
+    bare.write_text(body)
+    with pytest.raises(ValueError, match="no case to run"):
+        cases.read_ini(str(bare))
+    forced = tmp_path / "forced.ini"
+    forced.write_text(body + "[diffusion_coefficients]\ndID = T1\n[case]\nequation = Albert_Young_LC\n")
+    assert cases.read_ini(str(forced)).equation == cases.ALBERT_YOUNG_LC
+    wrong = tmp_path / "wrong.ini"
+    wrong.write_text(body + "[case]\nequation = Albert_Young\n")
+    with pytest.raises(ValueError, match="needs \\[diffusion_coefficients\\] dID"):
+        cases.read_ini(str(wrong))
+    bogus = tmp_path / "bogus.ini"
+    bogus.write_text(body + "[case]\nequation = Vlasov\n")
+    with pytest.raises(ValueError, match="expected one of"):
+        cases.read_ini(str(bogus))
+    p = cases.problem_from_params(ay)
+    assert p.bc == [cases.DIRICHLET, cases.ZEROFLUX, cases.DIRICHLET, cases.DIRICHLET]
+    assert not p.Dxx.any()  # filled from the D table on the device
+
+
+def test_run_refuses_a_missing_d_table(tmp_path):
+    """An Albert_Young run whose D file is absent fails before anything is written (the
+    reference's HDF5 read throws); it is never replaced by a synthetic case."""
+    from sayram2d_gb300 import run
+
+    ini = os.path.join(ROOT, "sayram-2d_gb300", "configs", "albert_young_80x80.ini")
+    with pytest.raises(FileNotFoundError, match="AlbertYoung_chorus.h5"):
+        run.run(ini, root=str(tmp_path))
+    assert not (tmp_path / "output").exists()
 
 
 def test_config1_fixture_inputs():
@@ -73,7 +171,7 @@ def test_ini_semantics(tmp_path):
     """nsteps rounds down to a multiple of nplots and dt = T/nsteps (Parameters.cc:58-60)."""
     ini = tmp_path / "p.ini"
     ini.write_text("[basic]\nrun_id=x\nnalpha0=8\nnE=6\nalpha0min=5\nalpha0max=90\nEmin=0.2\nEmax=5\n"
-                   "T=1.0\nnsteps=1005\n[diagnostics]\nnplots=10\n")
+                   "T=1.0\nnsteps=1005\n[diagnostics]\nnplots=10\n[diffusion_coefficients]\ndID=X\n")
     rp = cases.read_ini(str(ini))
     assert rp.nsteps == 1000 and rp.save_every_step == 100
     assert rp.dt == 1.0 / 1000
