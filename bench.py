@@ -125,6 +125,10 @@ def parse():
                          "kernels inside graphs with conditional nodes)")
     ap.add_argument("--precision", choices=["dw", "fp64res"], default="dw",
                     help="refinement arithmetic of the headline: double-word (FP32 pairs) or IEEE FP64")
+    ap.add_argument("--precond", choices=["alpha_line", "jacobi"], default="alpha_line",
+                    help="inner-solve preconditioner of the headline (the other one is measured beside it)")
+    ap.add_argument("--oracle-sample", type=int, default=16,
+                    help="batch instances stepped by the oracle (SuperLU) for rel_err_vs_oracle (0: skip)")
     return ap.parse_args()
 
 
@@ -225,6 +229,42 @@ def cpu_baseline_single(seed, n, seconds):
                       "C restatement of Solver.cc assembly + SuperLU/COLAMD direct solve, one thread"}
 
 
+def _oracle_steps(args):
+    """The oracle (C restatement of the reference's assembly + SuperLU/COLAMD) stepping batch
+    instance k from f0 for nsteps steps: the checker of the GPU batch's results."""
+    k, seed, size, nsteps = args
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # checker / CPU baseline only
+
+    p = cases.batch_instance(k, seed, DT, size)
+    return k, oracle.step(p, None, nsteps, solver="splu")
+
+
+def oracle_errors(seed, sizes, f_gpu, stats, n):
+    """Relative L2 error against the oracle for n instances spread over the batch's size range
+    (quantiles of the cell count), each stepped by the oracle as many steps as the GPU batch took,
+    on all host cores (a spawned pool). Returns the summary and the per-instance records."""
+    import multiprocessing as mp
+
+    cells = np.array([x * y for x, y in sizes], dtype=np.int64)
+    order = np.argsort(cells, kind="stable")
+    pick = sorted({int(order[q]) for q in np.linspace(0, len(order) - 1, n).round().astype(int)})
+    jobs = [(k, seed, sizes[k], int(stats[k]["steps"])) for k in pick]
+    t0 = time.perf_counter()
+    with mp.get_context("spawn").Pool(min(len(jobs), os.cpu_count() or 1)) as pool:
+        res = dict(pool.map(_oracle_steps, jobs))
+    per = []
+    for k in pick:
+        ref = res[k]
+        per.append({"instance": k, "grid": list(sizes[k]), "steps": int(stats[k]["steps"]),
+                    "rel_err": float(np.linalg.norm(f_gpu[k] - ref) / np.linalg.norm(ref)),
+                    "min_f": float(stats[k]["min_f"]), "mass_drift": float(stats[k]["mass_drift"])})
+    errs = [r["rel_err"] for r in per]
+    return {"max": max(errs), "median": statistics.median(errs), "instances": len(per),
+            "oracle": "C restatement of Solver.cc assembly + SuperLU/COLAMD, every step from f0",
+            "seconds": time.perf_counter() - t0}, per
+
+
 def run_reference(a):
     """--impl reference: the oracle port on every host core, same config/metric."""
     import multiprocessing as mp
@@ -281,14 +321,27 @@ BYTES32 = {
 }
 
 
+# The same for the FP64 drop-in (mode 0): FP64 Krylov vectors and coefficients.
+BYTES64 = {
+    "assemble": BYTES32["assemble"],              # 8-byte coefficients either way (FP64 or hi+lo)
+    "resid": 8 + 8 + 8 + 4 * 8 + 8 + 8,           # y, x, R, coefs -> y', r
+    "bicg1": 4 * 8 + 4 * 8 + 2 * 8,               # r, p, v, r^, 4 coefs -> p', v'
+    "bicg2": 2 * 8 + 4 * 8 + 8,                   # r, v, 4 coefs -> t
+    "bicg3": 6 * 8 + 2 * 8,                       # r, v, p, t, r^, x -> x, r
+    "polish": BYTES32["polish"],
+}
+
+
 # DRAM bytes per processed cell measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the
 # 256-instance case of the same kernels (one ncu capture per kernel); traffic grows with the
 # cells processed, so a launch's traffic is this figure times the cells it processed.
 TRAFFIC32 = {"assemble": 175.2, "bicg1": 40.3, "bicg2": 27.9, "resid": 60.9, "polish": 92.9}
 
 
-def kernel_roofline(b, probs, peak, steps=2):
-    """Per-kernel event timing over `steps` steps; bytes from the cells each kernel processed."""
+def kernel_roofline(b, probs, peak, steps=2, model=None):
+    """Per-kernel event timing over `steps` steps; bytes from the cells each kernel processed
+    (model: bytes per cell per kernel, BYTES32 by default)."""
+    model = BYTES32 if model is None else model
     cells = np.array([p.nx * p.ny for p in probs], dtype=np.float64)
     before = [b.stats(k) for k in range(len(probs))]
     b.enable_timing(True)
@@ -302,8 +355,8 @@ def kernel_roofline(b, probs, peak, steps=2):
             "bicg1": (cells * it).sum(), "bicg2": (cells * it).sum(), "bicg3": (cells * it).sum()}
     out = {}
     for name, (ms, n) in kt.items():
-        if name in BYTES32 and n > 0:
-            byts = BYTES32[name] * proc[name]
+        if name in model and n > 0:
+            byts = model[name] * proc[name]
             out[name] = {"ms": ms, "launches": int(n), "bytes": byts, "GBps": byts / (ms * 1e-3) / 1e9,
                          "share": 0.0}
         else:
@@ -311,10 +364,11 @@ def kernel_roofline(b, probs, peak, steps=2):
     total = sum(v["ms"] for v in out.values())
     for v in out.values():
         v["share"] = v["ms"] / total if total else 0.0
-    dom = max((k for k in out if k in BYTES32), key=lambda k: out[k]["ms"])
+    dom = max((k for k in out if k in model), key=lambda k: out[k]["ms"])
     d = out[dom]
     ach = d["GBps"]
-    traffic = TRAFFIC32[dom] * d["bytes"] / BYTES32[dom] / d["launches"] if dom in TRAFFIC32 else None
+    traffic = (TRAFFIC32[dom] * d["bytes"] / BYTES32[dom] / d["launches"]
+               if dom in TRAFFIC32 and model is BYTES32 else None)
     roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak[0], "unit": "GB/s",
             "frac": ach / peak[0], "peak_source": peak[1], "traffic": traffic,
             "traffic_source": "ncu dram bytes per cell on 256 instances, scaled by the cells processed",
@@ -384,25 +438,37 @@ def run_serving(capi, arrivals, probs, steps, precision, budget_gb, lanes=2):
             "min_f": min_f, "not_converged": not_conv, "device_gb": info["device_bytes"] / 1e9}
 
 
-def run_1024(capi):
+def run_1024(capi, peak):
     """The single-instance 1024 x 1024 configuration (dt = 1e-2): device-timed steps/s of the
-    plain FP64 drop-in and of the double-word path, and their agreement."""
+    plain FP64 drop-in and of the double-word path, each with both inner-solve preconditioners;
+    iterations of the last step; the step's HBM fraction (model bytes of every kernel launch in two
+    host-loop steps, per step, over the graph step's time); the agreement of the results."""
     p = cases.synthetic_problem(1024, 1024, DT, seed=11)
-    out = {"grid": "1024 x 1024", "dt": DT}
+    out = {"grid": "1024 x 1024", "dt": DT, "peak_GBps": peak[0]}
     fs = {}
-    for name, prec in (("fp64", capi.FP64), ("fp32_refine_dw", capi.FP32_REFINE_DW)):
-        s = capi.Solver(p, precision=prec)
-        s.step(4)
-        s.record_event(0)
-        s.step(10)
-        s.record_event(1)
-        ms = s.elapsed_ms(0, 1) / 10
-        st = s.get_stats()
-        fs[name] = s.f()
-        out[name] = {"steps_per_s": 1e3 / ms, "ms_per_step": ms, "iterations_last_step": st["iterations"],
-                     "rel_residual": st["rel_residual"]}
-        s.close()
-    out["rel_err_dw_vs_fp64"] = float(np.linalg.norm(fs["fp32_refine_dw"] - fs["fp64"]) / np.linalg.norm(fs["fp64"]))
+    for name, prec, model in (("fp64", capi.FP64, BYTES64), ("fp32_refine_dw", capi.FP32_REFINE_DW, BYTES32)):
+        for pcn, pc in (("alpha_line", capi.PRECOND_ALPHA_LINE), ("jacobi", capi.PRECOND_JACOBI)):
+            s = capi.Solver(p, precision=prec, precond=pc)
+            s.step(4)
+            s.record_event(0)
+            s.step(10)
+            s.record_event(1)
+            ms = s.elapsed_ms(0, 1) / 10
+            st = s.get_stats()
+            fs[(name, pcn)] = s.f()
+            _, kern = kernel_roofline(s, [p], peak, steps=2, model=model)
+            step_bytes = sum(v.get("bytes", 0.0) for v in kern.values()) / 2
+            kms = sum(v["ms"] for v in kern.values()) / 2
+            out[f"{name}/{pcn}"] = {
+                "steps_per_s": 1e3 / ms, "ms_per_step": ms, "iterations_last_step": st["iterations"],
+                "refinements_last_step": st["refinements"], "rel_residual": st["rel_residual"],
+                "model_bytes_per_step": step_bytes, "hbm_frac_step": step_bytes / (ms * 1e-3) / 1e9 / peak[0],
+                "kernel_ms_per_step": kms, "hbm_frac_kernels": step_bytes / (kms * 1e-3) / 1e9 / peak[0],
+                "kernels": {k: {"ms": v["ms"] / 2, "launches": v["launches"] / 2} for k, v in kern.items()}}
+            s.close()
+    ref = fs[("fp64", "alpha_line")]
+    out["rel_err_vs_fp64_alpha_line"] = {f"{n}/{c}": float(np.linalg.norm(f - ref) / np.linalg.norm(ref))
+                                         for (n, c), f in fs.items() if (n, c) != ("fp64", "alpha_line")}
     return out
 
 
@@ -418,7 +484,8 @@ def run_ours(a, R: Ranks):
     ncells = int(sum(p.nx * p.ny for p in probs))
     prec = capi.FP32_REFINE_DW if a.precision == "dw" else capi.FP32_REFINE
     other = capi.FP32_REFINE if a.precision == "dw" else capi.FP32_REFINE_DW
-    b = capi.Batch(probs, precision=prec, use_graph=0 if a.no_graph else 1, device=R.local)
+    pc = capi.PRECOND_ALPHA_LINE if a.precond == "alpha_line" else capi.PRECOND_JACOBI
+    b = capi.Batch(probs, precision=prec, use_graph=0 if a.no_graph else 1, device=R.local, precond=pc)
     t0 = time.perf_counter()
     if a.launch_shape:
         b.set_launch_shape(*[int(v) for v in a.launch_shape.split(",")])
@@ -444,7 +511,8 @@ def run_ours(a, R: Ranks):
     roof, kern = kernel_roofline(b, probs, peak)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": R.world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded)",
+            "vs_baseline": None, "dtype": "f32+dw" if a.precision == "dw" else "f32+f64",
+            "data": "synthetic (seeded)",
             "config": {"workload": f"batched FP32 Krylov + refinement: {a.instances} instances, nalpha,nE~U[64,256], "
                                    f"rho~U[-0.9,0.9], tau~logU[0.1,10] d, dt={DT} day, refined to rel residual 1e-11",
                        "instances": R.world * a.instances, "instances_per_gpu": a.instances,
@@ -454,6 +522,8 @@ def run_ours(a, R: Ranks):
                        "precision": ("fp32_refine_dw: FP32 Krylov, double-word (FP32-pair, ~48-bit) residual/"
                                      "refinement/assembly/checks" if a.precision == "dw" else
                                      "fp32_refine: FP32 Krylov, IEEE FP64 residual/refinement/assembly/checks"),
+                       "precond": ("alpha-line 4-cell blocks (left-preconditioned BiCGSTAB)" if a.precond == "alpha_line"
+                                   else "Jacobi scaling only"),
                        "l2": f"working set {b.device_bytes() / 1e9:.1f} GB >> 129 MB L2 (no flush needed)",
                        "launch_shape": {"cells_per_chunk": shape[0], "blocks_per_sm": shape[1],
                                         "autotune_s": tune_s, "candidates": b.tuning_log()}},
@@ -466,6 +536,8 @@ def run_ours(a, R: Ranks):
     line["max_mass_drift"] = max(s["mass_drift"] for s in st)
     line["max_rel_residual"] = max(s["rel_residual"] for s in st)
     line["not_converged"] = int(sum(1 for s in st if s["status"] != 0))
+    line["mean_inner_iterations"] = sum(s["total_iterations"] for s in st) / max(1, sum(s["steps"] for s in st))
+    line["mean_refinements"] = sum(s["total_refinements"] for s in st) / max(1, sum(s["steps"] for s in st))
     for key, red in (("min_f", min), ("max_mass_drift", max), ("max_rel_residual", max)):
         line[key] = -R.max(-line[key]) if red is min else R.max(line[key])
     line["not_converged"] = int(R.sum(line["not_converged"]))
@@ -505,6 +577,22 @@ def run_ours(a, R: Ranks):
         name_o = "fp32_refine_fp64_residual" if a.precision == "dw" else "fp32_refine_dw"
         line[name_o] = {"value": a.instances / (mso * 1e-3), "unit": UNIT, "ms_per_step": mso}
         bo.close()
+        # the headline arithmetic with the other inner-solve preconditioner
+        pco = capi.PRECOND_JACOBI if pc == capi.PRECOND_ALPHA_LINE else capi.PRECOND_ALPHA_LINE
+        bp = capi.Batch(probs, precision=prec, precond=pco)
+        bp.autotune(2)
+        for _ in range(2):
+            bp.step(1, allow_not_converged=True)
+        i0 = sum(bp.stats(k)["total_iterations"] for k in range(len(probs)))
+        bp.record_event(0)
+        bp.step(5, allow_not_converged=True)
+        bp.record_event(1)
+        msp = bp.elapsed_ms(0, 1) / 5
+        i1 = sum(bp.stats(k)["total_iterations"] for k in range(len(probs)))
+        line["other_precond"] = {"precond": "jacobi" if pco == capi.PRECOND_JACOBI else "alpha_line",
+                                 "value": a.instances / (msp * 1e-3), "unit": UNIT, "ms_per_step": msp,
+                                 "mean_inner_iterations": (i1 - i0) / (5 * len(probs))}
+        bp.close()
         # batched FP64 on the same batch, same number of steps -> accuracy + precision gain
         b64 = capi.Batch(probs, precision=capi.FP64)
         b64.autotune(1)
@@ -537,7 +625,11 @@ def run_ours(a, R: Ranks):
                               "sample": f"first {ns} instances, 2 steps each, one sayram_create per instance"}
         line["speedup_vs_plain_fp64"] = value / plain
         line["cpu_baseline"] = cpu_baseline_single(a.seed, a.instances, a.cpu_seconds)
-        line["config_1024"] = run_1024(capi)
+        if a.oracle_sample > 0:
+            # the same leg checks the timed batch's results against the oracle (not timed)
+            line["rel_err_vs_oracle"], line["oracle_sample"] = oracle_errors(
+                a.seed, cases.batch_sizes(a.instances, a.seed), f32, st, a.oracle_sample)
+        line["config_1024"] = run_1024(capi, peak)
     b.close()
     if a.serve_requests > 0 and R.world == 1:
         arr, sprobs, ssteps = serving_requests(a.serve_requests, a.serve_rate, a.seed)

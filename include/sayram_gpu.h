@@ -94,7 +94,16 @@ typedef struct sayram_options {
   int max_refine;   /* FP64 residual evaluations (outer refinements) per step; default 6 */
   int device;       /* CUDA device ordinal; default 0 */
   int use_graph;    /* 1 (default): each step runs as one CUDA graph with device-side loops */
+  int precond;      /* preconditioner of the inner Krylov solve, applied on the left:
+                       SAYRAM_PRECOND_JACOBI (0): the unit-diagonal (Jacobi) scaling only;
+                       SAYRAM_PRECOND_ALPHA_LINE (1, default): also the alpha-line blocks -- the
+                       tridiagonal of the west/east couplings over each aligned 4-cell piece of a
+                       row, solved exactly (block Jacobi with 4-cell alpha-line blocks). A caller
+                       that zero-fills the struct instead of calling sayram_default_options gets
+                       Jacobi. The converged answer does not depend on it. */
 } sayram_options;
+
+enum { SAYRAM_PRECOND_JACOBI = 0, SAYRAM_PRECOND_ALPHA_LINE = 1 };
 
 typedef struct sayram_stats {
   long long steps;        /* steps taken since creation */
@@ -244,6 +253,10 @@ typedef struct sayram_server_config {
   int lanes;
   int lane_split_side;
   double lane_small_fraction;
+  /* Longest a tick waits on the host for a lane's step to finish (seconds; <= 0: 600). A tick
+   * that gives up returns SAYRAM_ERR_TIMEOUT and leaves the step in flight; a later tick waits
+   * for it again and collects it. */
+  double wait_seconds;
 } sayram_server_config;
 
 typedef struct sayram_server_info {

@@ -23,6 +23,7 @@ _dp = ctypes.POINTER(ctypes.c_double)
 
 OK, ERR_ARG, ERR_OOM, ERR_NOT_CONVERGED, ERR_NEGATIVE, ERR_TIMEOUT, ERR_CUDA, ERR_BUDGET, ERR_STATE, ERR_IO = range(10)
 FP64, FP32_REFINE, FP32_REFINE_DW = 0, 1, 2
+PRECOND_JACOBI, PRECOND_ALPHA_LINE = 0, 1
 
 
 class sayram_problem(ctypes.Structure):
@@ -40,7 +41,7 @@ class sayram_options(ctypes.Structure):
     _fields_ = [
         ("precision", ctypes.c_int), ("tol", ctypes.c_double), ("inner_tol", ctypes.c_double),
         ("max_iters", ctypes.c_int), ("max_refine", ctypes.c_int), ("device", ctypes.c_int),
-        ("use_graph", ctypes.c_int),
+        ("use_graph", ctypes.c_int), ("precond", ctypes.c_int),
     ]
 
 
@@ -64,7 +65,8 @@ class sayram_dtable(ctypes.Structure):
 
 class sayram_server_config(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_double), ("max_slots", ctypes.c_int), ("max_side", ctypes.c_int),
-                ("lanes", ctypes.c_int), ("lane_split_side", ctypes.c_int), ("lane_small_fraction", ctypes.c_double)]
+                ("lanes", ctypes.c_int), ("lane_split_side", ctypes.c_int), ("lane_small_fraction", ctypes.c_double),
+                ("wait_seconds", ctypes.c_double)]
 
 
 class sayram_server_info(ctypes.Structure):
@@ -214,11 +216,16 @@ class _Pack:
 
 
 def options(precision: int = FP64, tol: float = 0.0, inner_tol: float = -1.0, max_iters: int = 500,
-            max_refine: int = 6, device: int = 0, use_graph: int = 1) -> sayram_options:
+            max_refine: int = 6, device: int = 0, use_graph: int = 1,
+            precond: Optional[int] = None) -> sayram_options:
+    """sayram_default_options with the given fields replaced (precond None: the library's
+    default)."""
     o = sayram_options()
     load().sayram_default_options(ctypes.byref(o))
     o.precision, o.tol, o.inner_tol = precision, tol, inner_tol
     o.max_iters, o.max_refine, o.device, o.use_graph = max_iters, max_refine, device, use_graph
+    if precond is not None:
+        o.precond = precond
     return o
 
 
@@ -387,11 +394,11 @@ class Server:
 
     def __init__(self, hbm_budget_bytes: float, max_slots: int = 4096, max_side: int = 1024,
                  opts: Optional[sayram_options] = None, lanes: int = 1, split_side: int = 0,
-                 small_fraction: float = 0.0, **kw):
+                 small_fraction: float = 0.0, wait_seconds: float = 0.0, **kw):
         L = load()
         self._L = L
         cfg = sayram_server_config(float(hbm_budget_bytes), int(max_slots), int(max_side), int(lanes),
-                                   int(split_side), float(small_fraction))
+                                   int(split_side), float(small_fraction), float(wait_seconds))
         opts = opts if opts is not None else options(**kw)
         h = ctypes.c_void_p()
         check(L.sayram_server_create(ctypes.byref(cfg), ctypes.byref(opts), ctypes.byref(h)), "sayram_server_create")

@@ -361,6 +361,8 @@ int sayram_batch_s::set_options(const sayram_options* o) {
   if (opt.inner_tol < 0) opt.inner_tol = 0;
   if (opt.max_iters < 1) opt.max_iters = 1;
   if (opt.max_refine < 2) opt.max_refine = 2;
+  if (opt.precond != SAYRAM_PRECOND_JACOBI && opt.precond != SAYRAM_PRECOND_ALPHA_LINE)
+    return fail(SAYRAM_ERR_ARG, "unknown preconditioner");
   mixed = opt.precision != SAYRAM_FP64;
   dwm = opt.precision == SAYRAM_FP32_REFINE_DW;
   return SAYRAM_OK;
@@ -456,6 +458,7 @@ int sayram_batch_s::alloc_storage(long long cells, int slots, int chunks_cap, in
   cm.part = d_part;
   cm.dyn = d_dyn;
   cm.hist_cap = sg::kHist;
+  cm.precond = opt.precond;
   return SAYRAM_OK;
 }
 
@@ -986,6 +989,7 @@ void sayram_default_options(sayram_options* o) {
   o->max_refine = 6;
   o->device = 0;
   o->use_graph = 1;
+  o->precond = SAYRAM_PRECOND_ALPHA_LINE;
 }
 
 void* sayram_host_alloc(size_t bytes) {
@@ -1722,6 +1726,7 @@ struct ServerLane {
 struct sayram_server_s {
   std::vector<std::unique_ptr<ServerLane>> lanes;
   int split = 0;
+  double wait_seconds = 600.0;  // longest host wait of one tick for a lane's step
   std::map<long long, Result> results;
   long long next_id = 1;
 
@@ -1740,9 +1745,8 @@ struct sayram_server_s {
     for (auto& L : lanes) any = any || L->inflight;
     if (!any) return SAYRAM_OK;
     // wait for the first lane whose step finishes, then collect every finished lane (a step
-    // takes milliseconds; one that has not finished after kWaitSeconds is reported, and a later
+    // takes milliseconds; one that has not finished after wait_seconds is reported, and a later
     // tick waits for it again)
-    constexpr double kWaitSeconds = 600.0;
     const double t_wait = now_seconds();
     int total = 0;
     for (;;) {
@@ -1758,8 +1762,9 @@ struct sayram_server_s {
         done = true;
       }
       if (done) break;
-      if (now_seconds() - t_wait > kWaitSeconds)
-        return fail(SAYRAM_ERR_TIMEOUT, "server step still running after 600 s");
+      if (now_seconds() - t_wait > wait_seconds)
+        return fail(SAYRAM_ERR_TIMEOUT, "server step still running after " + std::to_string(wait_seconds) +
+                                            " s (the next tick waits for it again)");
       std::this_thread::yield();
     }
     if (ncomp) *ncomp = total;
@@ -1783,6 +1788,7 @@ int sayram_server_create(const sayram_server_config* cfg, const sayram_options* 
   std::unique_ptr<sayram_server_s> s(new (std::nothrow) sayram_server_s());
   if (!s) return fail(SAYRAM_ERR_OOM, "host allocation failed");
   s->split = split;
+  s->wait_seconds = c.wait_seconds > 0 ? c.wait_seconds : 600.0;
   for (int k = 0; k < nl; ++k) {
     sayram_server_config lc = c;
     if (nl == 2) {

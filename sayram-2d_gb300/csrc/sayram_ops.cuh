@@ -50,6 +50,7 @@ struct Common {
   int use_cond;
   int guard_refine, guard_iters;  // hard caps on loop trips, whatever the bookkeeping says
   int hist_cap;  // history depth used for the starting point (kHist; 1 when the buffers alias)
+  int precond;   // 1: the inner Krylov solve is preconditioned on the left by the alpha-line blocks
 };
 
 __device__ __forceinline__ int n_chunks(const Common& cm) { return cm.dyn ? cm.dyn[0] : cm.nchunks; }
@@ -846,6 +847,43 @@ __device__ __forceinline__ Q4<T> stencil_sm(const T* sm, long long o, int P, con
   return r;
 }
 
+// ------------------------------------------------------------------------------ preconditioner
+// Alpha-line block preconditioner. Every 4-cell group of the padded layout lies inside one row
+// (rows start at multiples of 4), and B is the tridiagonal of the group's own west/east couplings
+// -- unit diagonal, -cw below, -ce above -- with the couplings to the neighbouring groups dropped:
+// block Jacobi with 4-cell alpha-line blocks, the direction in which the scaled systems are
+// stiffest (Dxx/dalpha^2 against Dyy/dlogE^2). line4 returns B^-1 q by Thomas elimination
+// without pivoting (B is a column-diagonally-dominant M-matrix: every column of the outflow
+// fractions sums to < 1, so each pivot stays in (0, 1]). The factors are formed in FP32 with
+// separately rounded intrinsics whatever the vector precision, so every kernel that applies
+// B^-1 applies the same linear map; padding cells (q = cw = ce = 0) stay 0.
+__device__ __forceinline__ float fmaT(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fmaT(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float mulT(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mulT(double a, double b) { return __dmul_rn(a, b); }
+
+template <typename T, typename CT>
+__device__ __forceinline__ Q4<T> line4(const Q4<T>& q, const Q4<CT>& cw, const Q4<CT>& ce) {
+  const float w1 = (float)cw.a[1], w2 = (float)cw.a[2], w3 = (float)cw.a[3];
+  const float c0 = (float)ce.a[0];
+  const float i1 = __frcp_rn(__fmaf_rn(-w1, c0, 1.0f));
+  const float c1 = __fmul_rn((float)ce.a[1], i1);
+  const float i2 = __frcp_rn(__fmaf_rn(-w2, c1, 1.0f));
+  const float c2 = __fmul_rn((float)ce.a[2], i2);
+  const float i3 = __frcp_rn(__fmaf_rn(-w3, c2, 1.0f));
+  // forward: d_j = (q_j + w_j d_(j-1)) / pivot_j; backward: z_j = d_j + c_j z_(j+1)
+  const T d0 = q.a[0];
+  const T d1 = mulT(fmaT((T)w1, d0, q.a[1]), (T)i1);
+  const T d2 = mulT(fmaT((T)w2, d1, q.a[2]), (T)i2);
+  const T d3 = mulT(fmaT((T)w3, d2, q.a[3]), (T)i3);
+  Q4<T> z;
+  z.a[3] = d3;
+  z.a[2] = fmaT((T)c2, d3, d2);
+  z.a[1] = fmaT((T)c1, z.a[2], d1);
+  z.a[0] = fmaT((T)c0, z.a[1], d0);
+  return z;
+}
+
 // Coefficients of a row in the wide arithmetic: from the FP64 arrays or the (hi, lo) split
 template <typename C, typename A>
 struct CoefW;
@@ -908,8 +946,8 @@ __device__ __forceinline__ Q4<typename A::V> stencilW(const Q4<typename A::V>& c
 }
 
 // ------------------------------------------------------------------------------ outer residual
-// r = R - A~ (y + x) in the wide arithmetic; writes y + x to the other y buffer and r (T precision).
-// Partials: ||r||^2, ||R||^2.
+// r = R - A~ (y + x) in the wide arithmetic; writes y + x to the other y buffer and the Krylov's
+// right-hand side B^-1 r (T precision, scaled). Partials: ||r||^2, ||R||^2, ||B^-1 r||^2.
 template <typename T, typename C, typename A, int CH>
 __global__ void __launch_bounds__(kThreads, 4) k_resid(Common cm, Fields fl, Coef<C> co, Kry<T> kr,
                                                         double tol, double inner_tol, int max_refine) {
@@ -942,6 +980,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_resid(Common cm, Fields fl, Coe
     });
     __syncthreads();
     typename A::Acc q0 = 0, q1 = 0;
+    T q2 = (T)0;
 #pragma unroll 1
     for (int g = 0; g < CH / (4 * kThreads); ++g) {
       const long long K = c0 + 4 * (threadIdx.x + g * kThreads);
@@ -963,15 +1002,23 @@ __global__ void __launch_bounds__(kThreads, 4) k_resid(Common cm, Fields fl, Coe
           q0 += A::sq_scaled(rv, sc);
           q1 += A::sq_scaled(R.a[m], sc);
         }
+        if (cm.precond) {  // the Krylov matrix's couplings (the hi parts in the FP32 modes)
+          r = line4<T, C>(r, ld4(co.cw + K), ld4(co.ce + K));
+#pragma unroll
+          for (int m = 0; m < 4; ++m) q2 += r.a[m] * r.a[m];
+        }
         A::st4(yout + K, yc);
         st4(kr.r + K, r);
       }
     }
-    const double w[2] = {A::warp_total(q0), A::warp_total(q1)};
-    double tot[2], mine[2];
-    block_sum_lane0<2>(w, mine);
-    if (chunk_finish<2>(st, PH_RESID, I.chunk0, I.nchunks, c, cm.part, mine, tot) && threadIdx.x == 0) {
-      // tot holds ||r*sc||^2 and ||R*sc||^2
+    double w3 = (double)q2;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) w3 += __shfl_xor_sync(0xffffffffu, w3, o);
+    const double w[3] = {A::warp_total(q0), A::warp_total(q1), w3};
+    double tot[3], mine[3];
+    block_sum_lane0<3>(w, mine);
+    if (chunk_finish<3>(st, PH_RESID, I.chunk0, I.nchunks, c, cm.part, mine, tot) && threadIdx.x == 0) {
+      // tot holds ||r*sc||^2, ||R*sc||^2 and ||B^-1 r*sc||^2
       st.ycur ^= 1;
       st.has_x = 0;
       if (st.refines == 0) st.bb = tot[1];
@@ -992,8 +1039,12 @@ __global__ void __launch_bounds__(kThreads, 4) k_resid(Common cm, Fields fl, Coe
         st.fresh = 1;
         st.restart = 1;
         st.iters = 0;
-        st.rr = tot[0];
-        const double a = inner_tol * inner_tol * tot[0], bnd = 0.0625 * tol * tol * st.bb;
+        // the Krylov's residual is B^-1 r: its target is the relative reduction asked, or the
+        // final tolerance carried into preconditioned units by this pass's norm ratio
+        const double rrk = cm.precond ? tot[2] : tot[0];
+        st.rr = rrk;
+        const double a = inner_tol * inner_tol * rrk;
+        const double bnd = 0.0625 * tol * tol * st.bb * (cm.precond && tot[0] > 0.0 ? rrk / tot[0] : 1.0);
         st.rr_target = a > bnd ? a : bnd;
         atomicAdd(&cm.ctl->n_inner, 1);
       }
@@ -1003,9 +1054,11 @@ __global__ void __launch_bounds__(kThreads, 4) k_resid(Common cm, Fields fl, Coe
 }
 
 // ------------------------------------------------------------------------------ BiCGSTAB
+// Left-preconditioned BiCGSTAB on B^-1 A~ x = B^-1 r (B = I without the preconditioner; the
+// residual r the kernels carry is the preconditioned one, and x is the correction itself).
 // k1: p = r + beta (p_old - omega v_old)  (p = r on a restart, which also sets r^ = r);
-//     v = A~ p;  partial (r^, v). p is computed once per cell into shared memory (chunk plus one
-//     row above and below) and the stencil reads it there.
+//     v = B^-1 A~ p;  partial (r^, v). p is computed once per cell into shared memory (chunk plus
+//     one row above and below) and the stencil reads it there.
 template <typename T, int CH>
 __global__ void __launch_bounds__(kThreads, krylov_blocks<T>()) k_bicg1(Common cm, Coef<T> co, Kry<T> kr) {
   count_launch(cm.ctl);
@@ -1044,7 +1097,9 @@ __global__ void __launch_bounds__(kThreads, krylov_blocks<T>()) k_bicg1(Common c
       if (K < c1) {
         const long long o = K - e0;
         const Q4<T> pcv = *reinterpret_cast<const Q4<T>*>(sm + o);
-        const Q4<T> v = stencil_sm<T>(sm, o, P, ld4(co.cw + K), ld4(co.ce + K), ld4(co.cs + K), ld4(co.cn + K));
+        const Q4<T> cwq = ld4(co.cw + K), ceq = ld4(co.ce + K);
+        Q4<T> v = stencil_sm<T>(sm, o, P, cwq, ceq, ld4(co.cs + K), ld4(co.cn + K));
+        if (cm.precond) v = line4<T, T>(v, cwq, ceq);  // v = B^-1 A~ p
         st4(pn + K, pcv);
         st4(vn + K, v);
         Q4<T> rh;
@@ -1077,7 +1132,7 @@ __global__ void __launch_bounds__(kThreads, krylov_blocks<T>()) k_bicg1(Common c
   });
 }
 
-// k2: s = r - alpha v;  t = A~ s;  partials (t, s), (t, t). s is staged like p in k1.
+// k2: s = r - alpha v;  t = B^-1 A~ s;  partials (t, s), (t, t). s is staged like p in k1.
 template <typename T, int CH>
 __global__ void __launch_bounds__(kThreads, krylov_blocks<T>()) k_bicg2(Common cm, Coef<T> co, Kry<T> kr) {
   count_launch(cm.ctl);
@@ -1109,7 +1164,9 @@ __global__ void __launch_bounds__(kThreads, krylov_blocks<T>()) k_bicg2(Common c
       if (K < c1) {
         const long long o = K - e0;
         const Q4<T> sc = *reinterpret_cast<const Q4<T>*>(sm + o);
-        const Q4<T> t = stencil_sm<T>(sm, o, P, ld4(co.cw + K), ld4(co.ce + K), ld4(co.cs + K), ld4(co.cn + K));
+        const Q4<T> cwq = ld4(co.cw + K), ceq = ld4(co.ce + K);
+        Q4<T> t = stencil_sm<T>(sm, o, P, cwq, ceq, ld4(co.cs + K), ld4(co.cn + K));
+        if (cm.precond) t = line4<T, T>(t, cwq, ceq);  // t = B^-1 A~ s
         st4(kr.t + K, t);
 #pragma unroll
         for (int m = 0; m < 4; ++m) {

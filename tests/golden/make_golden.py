@@ -29,9 +29,13 @@ the reference's Albert_Young / Albert_Young_LC, and f at every save (/f/1 .. /f/
 reference's own Solver.
 
 The reference tree is $SAYRAM_REFERENCE (default /root/reference). Run where it exists:
-  python tests/golden/make_golden.py [cases|ay80|config1]
+  python tests/golden/make_golden.py [cases|ay80|config1|config1_full]
 ("cases" regenerates only ref_cases.npz, "ay80" the case fixtures and ref_ay_80x80.npz,
-"config1" only the config-1 prefix, ~6 min)
+"config1" only the config-1 prefix, ~6 min, "config1_full" the 500-step config-1 fixture
+ref_c1_1024_full.npz, about an hour on one core)
+
+ref_c1_1024_full.npz pins config 1 over all 500 steps with the tight-residual solve
+(oracle.solve_tight), which agrees with the SuperLU prefix to <= 1e-12 over its 10 steps.
 """
 import hashlib
 import os
@@ -192,11 +196,58 @@ def write_config1_prefix(nsteps=10):
     np.savez_compressed(os.path.join(HERE, "ref_c1_1024_prefix.npz"), **out)
 
 
+C1_SAVES = (10, 100, 250, 500)
+
+
+def write_config1_full(nsteps=500):
+    """Config 1 over all 500 steps: the restated assembly and the tight-residual solve
+    (oracle.solve_tight: BiCGSTAB with an alpha-line preconditioner inside iterative refinement,
+    residuals in extended precision, down to the rounding floor of a float64 solution), warm
+    started from the previous step. Stores, at steps 10, 100, 250 and 500, a strided sample of f,
+    its row and column sums, sum of squares and minimum, plus the largest relative residual of
+    any step; the first 10 steps are also checked against the SuperLU prefix fixture (the direct
+    solve), and the agreement is stored."""
+    import time
+
+    p = config1_problem()
+    z = np.load(os.path.join(HERE, "ref_c1_1024_prefix.npz"))
+    out = {"digest": np.frombuffer(bytes.fromhex(input_digest(p)), dtype=np.uint8),
+           "saves": np.array(C1_SAVES)}
+    f = p.f0.copy()
+    worst, iters, t0 = 0.0, 0, time.time()
+    for k in range(1, nsteps + 1):
+        M5, R = oracle.assemble(p, f)
+        x, rel, its = oracle.solve_tight(p.nx, p.ny, M5, R, oracle.field_to_sys(f))
+        f = oracle.sys_to_field(p.nx, p.ny, x)
+        worst, iters = max(worst, rel), iters + its
+        if k in (1, 10):
+            pre = "f1" if k == 1 else "fN"
+            agree = max(float(np.linalg.norm(f[::8, ::8] - z[pre + "_sub"]) / np.linalg.norm(z[pre + "_sub"])),
+                        float(np.linalg.norm(f.sum(axis=1) - z[pre + "_rows"]) / np.linalg.norm(z[pre + "_rows"])))
+            out[f"agree_superlu_step{k}"] = np.array([agree])
+            print(f"step {k}: tight vs SuperLU {agree:.2e}", flush=True)
+            assert agree <= 1e-12, agree
+        if k in C1_SAVES:
+            out[f"f{k}_sub"] = f[::8, ::8].copy()
+            out[f"f{k}_rows"], out[f"f{k}_cols"] = f.sum(axis=1), f.sum(axis=0)
+            out[f"f{k}_ssq"] = np.array([float((f * f).sum())])
+            out[f"f{k}_min"] = np.array([float(f.min())])
+        if k % 10 == 0:
+            print(f"step {k}: rel {rel:.2e} its {its} ({time.time() - t0:.0f} s)", flush=True)
+    out["max_rel_residual"] = np.array([worst])
+    out["inner_iterations"] = np.array([iters])
+    np.savez_compressed(os.path.join(HERE, "ref_c1_1024_full.npz"), **out)
+
+
 def main():
     oracle.build()
     if sys.argv[1:] == ["config1"]:
         write_config1_prefix()
         print("wrote ref_c1_1024_prefix.npz")
+        return
+    if sys.argv[1:] == ["config1_full"]:
+        write_config1_full()
+        print("wrote ref_c1_1024_full.npz")
         return
     if oracle.build_ref(REFERENCE) is None:
         raise SystemExit("the reference sources are needed to generate fixtures ($SAYRAM_REFERENCE)")

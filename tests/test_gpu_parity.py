@@ -502,3 +502,54 @@ def test_stiff_steps(capi, oracle, prec):
         assert rel(f, ref) <= tol, (prec, k, rel(f, ref))
         assert f.min() >= 0.0 and st["status"] == 0 and st["mass_drift"] <= 1e-8, (prec, k, st)
     b.close()
+
+
+@pytest.mark.parametrize("precond", [0, 1])
+@pytest.mark.parametrize("prec", [0, 1, 2])
+def test_preconditioners_meet_parity(capi, oracle, prec, precond):
+    """Both inner-solve preconditioners (Jacobi scaling only; alpha-line 4-cell blocks, the
+    default) give the reference's answer to each mode's tolerance on the small fixtures (ragged,
+    1-wide, non-uniform, all-Dirichlet, all-zero-flux) and on stiff steps (dt = 1 day, |rho| =
+    0.99, fast and no loss): the preconditioner steers the iteration, not the converged answer."""
+    tol = TOL64 if prec == 0 else TOL32
+    for name in NAMES:
+        p = problem_from(Z, name)
+        s = capi.Solver(p, precision=prec, precond=precond)
+        s.step(10)
+        f = s.f()
+        st = s.get_stats()
+        s.close()
+        assert rel(f, Z[f"{name}/f10"]) <= tol, (name, prec, precond, rel(f, Z[f"{name}/f10"]))
+        assert f.min() >= 0.0 and st["status"] == 0
+    probs = [cases.synthetic_problem(40 + 7 * k, 36 + 5 * k, 1.0, seed=90 + k, tau=tau, rho=rho)
+             for k, (tau, rho) in enumerate(((0.01, 0.99), (100.0, -0.99), (0.3, 0.5), (None, -0.9)))]
+    b = capi.Batch(probs, precision=prec, precond=precond)
+    b.step(4)
+    for k, p in enumerate(probs):
+        ref = oracle.step(p, None, 4)
+        assert rel(b.f(k), ref) <= tol, (prec, precond, k, rel(b.f(k), ref))
+        assert b.f(k).min() >= 0.0 and b.stats(k)["status"] == 0
+    b.close()
+
+
+@pytest.mark.parametrize("prec", [0, 2])
+def test_alpha_line_blocks_cut_iterations(capi, prec):
+    """On a stiff 256 x 256 instance (dt = 1e-2 day, the configuration of the single large
+    instance) the alpha-line blocks take fewer inner iterations than Jacobi scaling alone, and both
+    end at the same state to the mode's tolerance."""
+    p = cases.synthetic_problem(256, 256, 1e-2, seed=11)
+    out = {}
+    for precond in (0, 1):
+        s = capi.Solver(p, precision=prec, precond=precond)
+        s.step(5)
+        out[precond] = (s.f(), s.get_stats()["total_iterations"])
+        s.close()
+    tol = TOL64 if prec == 0 else TOL32
+    assert rel(out[1][0], out[0][0]) <= tol
+    assert out[1][1] < 0.8 * out[0][1], (prec, out[0][1], out[1][1])
+
+
+def test_unknown_preconditioner_is_refused(capi):
+    p = cases.synthetic_problem(8, 8, 1e-2, seed=1)
+    with pytest.raises(RuntimeError, match="unknown preconditioner"):
+        capi.Solver(p, precision=capi.FP64, precond=7)

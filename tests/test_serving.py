@@ -1,6 +1,8 @@
 """Serving (continuous batching): requests of different grid sizes and step counts arrive while
 others run; each result must equal the same request run alone (FP64: 1e-12, FP32 modes: 1e-8 in
 relative L2), admission respects the HBM budget, and oversized requests are refused."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -114,3 +116,33 @@ def test_oversized_request_refused(capi):
     with pytest.raises(RuntimeError, match="max_side"):
         srv.submit(p, 3)
     srv.close()
+
+
+def test_tick_gives_up_after_its_wait_limit_and_a_later_tick_collects(capi):
+    """The host wait of a tick is bounded (sayram_server_config.wait_seconds): with a limit of a
+    microsecond, a legitimately long step (a 512 x 512 FP64 request) is still running when the
+    tick gives up and returns SAYRAM_ERR_TIMEOUT; the step stays in flight, later ticks wait for it
+    again, and the result is the request alone. Nothing on the GPU waits or hangs: only the host
+    stops waiting."""
+    p = cases.synthetic_problem(512, 512, 1e-2, seed=7)
+    srv = capi.Server(4e9, max_slots=4, max_side=512, precision=capi.FP64, wait_seconds=1e-6)
+    rid = srv.submit(p, 3)
+    L = capi.load()
+    n = ctypes.c_int(0)
+    rc = L.sayram_server_tick(srv.h, ctypes.byref(n))
+    assert rc == capi.ERR_TIMEOUT, (rc, capi.last_error())
+    assert "still running" in capi.last_error()
+    got = None
+    for _ in range(100000):
+        rc = L.sayram_server_tick(srv.h, ctypes.byref(n))
+        assert rc in (capi.OK, capi.ERR_TIMEOUT), capi.last_error()
+        got = srv.poll(rid)
+        if got is not None:
+            break
+    info = srv.info()
+    srv.close()
+    assert got is not None and info["completed"] == 1
+    f, st, _, _ = got
+    assert st["steps"] == 3
+    ref = _alone(capi, p, 3, capi.FP64)
+    assert rel(f, ref) <= 1e-12
