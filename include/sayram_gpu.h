@@ -309,7 +309,9 @@ void sayram_server_destroy(sayram_server s);
  * round_up((ny+2) * round_up(nx,4), 32) + 64 <= 73728 cells and nx, ny <= 4096 (256 x 256
  * fits); larger grids return SAYRAM_ERR_ARG with a message saying so.
  * The first call on a device looks up the array's device address (cudaGetSymbolAddress) and
- * keeps it for later calls; make that first call before any stream capture begins.
+ * keeps it for later calls; make that first call before any stream capture begins. The kept
+ * address does not survive cudaDeviceReset: calls after a reset are not supported. Every call
+ * waits for its stream between launches (it reads the loops' control words back to the host).
  * All calls share the array: each call clears it at its start and the array keeps the last
  * call's contents afterwards. Calls that overlap on the GPU (several host threads or streams at
  * once) race on it and must be serialized by the caller. */

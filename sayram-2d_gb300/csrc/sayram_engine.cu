@@ -413,8 +413,7 @@ int sayram_batch_s::alloc_storage(long long cells, int slots, int chunks_cap, in
     SG_ALLOC(*g, cells);
     cell_arrays.push_back({*g, 8});
   }
-  double** fs[10] = {&fl.f, &fl.fh[0], &fl.fh[1], &fl.fh[2], &fl.fh[3], &fl.invD, &fl.R, &fl.colsum, &fl.y64[0],
-                      &fl.y64[1]};
+  double** fs[9] = {&fl.f, &fl.fh[0], &fl.fh[1], &fl.fh[2], &fl.invD, &fl.R, &fl.colsum, &fl.y64[0], &fl.y64[1]};
   for (auto f : fs) {
     SG_ALLOC(*f, cells);
     cell_arrays.push_back({*f, 8});
@@ -457,8 +456,9 @@ int sayram_batch_s::alloc_storage(long long cells, int slots, int chunks_cap, in
   cm.dirv = d_dirv;
   cm.part = d_part;
   cm.dyn = d_dyn;
-  cm.hist_cap = sg::kHist;
+  cm.hist_cap = sg::kOrder;
   cm.precond = opt.precond;
+  fl.decay = geo.decay;
   return SAYRAM_OK;
 }
 
@@ -883,24 +883,26 @@ int sayram_batch_s::set_dtable(int idx, const sayram_dtable* t) {
 }
 
 // Times `steps` steps of every launch shape (cells per chunk x blocks per SM) from the same
-// state and keeps the fastest; f, the history of earlier states and the per-instance state are
-// restored afterwards, so tuning does not advance the simulation.
+// state and keeps the fastest; f, the history of earlier states, the extrapolated start (in the
+// y buffers) and the per-instance state are restored afterwards, so tuning does not advance the
+// simulation.
 int sayram_batch_s::autotune(int steps, int* best_chunk, int* best_grid) {
   if (steps < 1) steps = 1;
   SG_CUDA(cudaSetDevice(dev));
-  double* snap = nullptr;  // f and the history states
-  if (cudaMalloc(&snap, sizeof(double) * (1 + sg::kHist) * ncell) != cudaSuccess) {
+  constexpr int kSnap = 3 + sg::kHist;
+  double* snap = nullptr;  // f, the history states and both y buffers
+  if (cudaMalloc(&snap, sizeof(double) * kSnap * ncell) != cudaSuccess) {
     cudaGetLastError();
     return fail(SAYRAM_ERR_OOM, "autotune: no room for the state snapshot");
   }
-  double* const saved[1 + sg::kHist] = {fl.f, fl.fh[0], fl.fh[1], fl.fh[2], fl.fh[3]};
+  double* const saved[kSnap] = {fl.f, fl.fh[0], fl.fh[1], fl.fh[2], fl.y64[0], fl.y64[1]};
   std::vector<InstState> hs(cap_slots);
-  for (int k = 0; k < 1 + sg::kHist; ++k)
+  for (int k = 0; k < kSnap; ++k)
     SG_CUDA(cudaMemcpyAsync(snap + k * ncell, saved[k], sizeof(double) * ncell, cudaMemcpyDeviceToDevice, stream));
   SG_CUDA(cudaMemcpyAsync(hs.data(), d_st, sizeof(InstState) * cap_slots, cudaMemcpyDeviceToHost, stream));
   SG_CUDA(cudaStreamSynchronize(stream));
   auto restore = [&]() -> int {
-    for (int k = 0; k < 1 + sg::kHist; ++k)
+    for (int k = 0; k < kSnap; ++k)
       SG_CUDA(cudaMemcpyAsync(saved[k], snap + k * ncell, sizeof(double) * ncell, cudaMemcpyDeviceToDevice, stream));
     SG_CUDA(cudaMemcpyAsync(d_st, hs.data(), sizeof(InstState) * cap_slots, cudaMemcpyHostToDevice, stream));
     SG_CUDA(cudaStreamSynchronize(stream));
@@ -1396,7 +1398,7 @@ void sayram_batch_destroy(sayram_batch b) { delete b; }
 size_t sayram_instance_bytes(int nx, int ny, int precision) {
   const long long pitch = round_up(nx, 4);
   const long long cells = round_up((long long)(ny + 2) * pitch, 32);
-  const long long per = 20 * 8 + (precision != SAYRAM_FP64 ? 8 * 4 + 8 * 4 : 4 * 8 + 8 * 8) + 8;
+  const long long per = 19 * 8 + (precision != SAYRAM_FP64 ? 8 * 4 + 8 * 4 : 4 * 8 + 8 * 8) + 8;
   return (size_t)(cells * per + 4096);
 }
 
@@ -1907,8 +1909,9 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 std::mutex g_noalloc_mu;
 unsigned char* g_noalloc_base[128] = {};  // device address of g_noalloc_scratch, per device
 
-// Per-cell face factors from separate coefficient arrays (alpha-major); same arithmetic as
-// k_setup, which reads one packed staging buffer instead.
+// Per-cell set-up from separate coefficient arrays (alpha-major) in the caller's device memory:
+// sg::setup_cell, the same per-cell definition k_setup uses (k_setup reads one packed staging
+// buffer instead).
 __global__ void k_setup_fields(sg::Common cm, sg::Geo geo, const double* G, const double* Dxx,
                                const double* Dxy, const double* Dyy, const double* itau,
                                const double* xe, const double* ye) {
@@ -1918,25 +1921,7 @@ __global__ void k_setup_fields(sg::Common cm, sg::Geo geo, const double* G, cons
        c += (long long)gridDim.x * blockDim.x) {
     const int i = (int)(c / I.ny), j = (int)(c % I.ny);
     const long long K = I.base + (long long)j * I.pitch + i;
-    const double xl = xe[i], xr = xe[i + 1];
-    const double yb = ye[j], yt = ye[j + 1];
-    const double dx = __dadd_rn(xr, -xl), dy = __dadd_rn(yt, -yb);
-    const double Kx = __dmul_rn(0.5, __dadd_rn(xl, xr)), Ky = __dmul_rn(0.5, __dadd_rn(yb, yt));
-    const double g = G[c];
-    const double L[4] = {__dmul_rn(Dxx[c], g), __dmul_rn(Dxy[c], g), __dmul_rn(Dxy[c], g),
-                         __dmul_rn(Dyy[c], g)};
-    double aa, ab;
-    sg::face_pair(Kx, Ky, xl, yt, xl, yb, -1.0, 0.0, L, &aa, &ab);
-    geo.aAx[K] = aa;
-    geo.aBx[K] = ab;
-    geo.Sx[K] = __dadd_rn(aa, ab);
-    sg::face_pair(Kx, Ky, xl, yb, xr, yb, 0.0, -1.0, L, &aa, &ab);
-    geo.aAy[K] = aa;
-    geo.aBy[K] = ab;
-    geo.Sy[K] = __dadd_rn(aa, ab);
-    const double ukk = __dmul_rn(g, __ddiv_rn(__dmul_rn(dx, dy), I.dt));
-    geo.ukk[K] = ukk;
-    geo.sdiag[K] = __dmul_rn(ukk, __dadd_rn(1.0, __dmul_rn(I.dt, itau[c])));
+    sg::setup_cell<sg::F64A>(geo, K, xe[i], xe[i + 1], ye[j], ye[j + 1], I.dt, G[c], Dxx[c], Dxy[c], Dyy[c], itau[c]);
   }
 }
 
@@ -2063,8 +2048,8 @@ extern "C" int sayram_step_noalloc(const sayram_problem* pd, const sayram_option
     *a = lay.take<double>(kNoAllocCells);
     if (!*a) return fail(SAYRAM_ERR_ARG, "cell arrays exceed the scratch");
   }
-  fl.fh[1] = fl.fh[2] = fl.fh[3] = fl.fh[0];  // one history buffer: linear extrapolation (hist_cap = 1);
-                                    // geo.decay stays null (no loss compensation on this path)
+  fl.fh[1] = fl.fh[2] = fl.fh[0];  // one history buffer: linear extrapolation (hist_cap = 1);
+                                    // geo.decay / fl.decay stay null (no loss compensation here)
   unsigned char* used_end = lay.cur;
 
   // ---- every call starts from zero: padding, pad rows, state and counters must be 0

@@ -91,11 +91,13 @@ struct Coef {  // row-oriented scaled off-diagonal magnitudes (hi parts when spl
   float *lw, *le, *ls, *ln;  // low parts for the FP32-split storage (null for FP64)
 };
 
-constexpr int kHist = 4;  // earlier states kept for the extrapolated start of each solve
+constexpr int kOrder = 4;  // earlier states the extrapolated start of each solve goes back
+constexpr int kHist = 3;   // history buffers: with f^n (the state the polish replaces) they hold kOrder
 
 struct Fields {
   double* f;       // state, padded system order
-  double* fh[kHist];  // earlier states f^(n-1) .. f^(n-4), rotated per instance (InstState::hslot)
+  double* fh[kHist];  // earlier states f^(n-1) .. f^(n-3), rotated per instance (InstState::hslot)
+  const double* decay;  // 1 / (1 + dt/tau) per cell (the extrapolated start); null: 1
   double* invD;    // 1 / diag(M)
   double* R;       // right-hand side
   double* colsum;  // 1^T M per column (conservation check)
@@ -128,12 +130,12 @@ struct F64A {
   __device__ static V div(V a, V b) { return a / b; }
   __device__ static V abs(V a) { return fabs(a); }
   __device__ static V neg(V a) { return -a; }
-  // D g with g the polynomial extrapolation in time through f and n earlier states (n = 1..4) of
+  // g, the polynomial extrapolation in time through f and n earlier states h1..h4 (n = 1..4) of
   // the loss-compensated sequence c_k = h_k r^k (r = 1/(1 + dt/tau), one step of pure loss), times
   // r: g = r (c0 + d1), r (c0 + 2 d1 - d2), r (c0 + 3 (d1 - d2) + d3),
   // r (c0 + 4 (d1 + d3) - 6 d2 - d4) with d_m = c_(m-1) - c_m, c0 = f. Exact for pure loss;
-  // r = 1 gives the plain polynomial.
-  __device__ static V start(V D, V f, V h1, V h2, V h3, V h4, int n, V r) {
+  // r = 1 gives the plain polynomial. The next solve starts from y0 = D g.
+  __device__ static V extrap(V f, V h1, V h2, V h3, V h4, int n, V r) {
     const double c1 = h1 * r;
     const double d1 = f - c1;
     double c = d1;
@@ -148,7 +150,7 @@ struct F64A {
         c = n == 3 ? 3.0 * (d1 - d2) + d3 : 4.0 * (d1 + d3) - 6.0 * d2 - (c3 - h4 * (r3 * r));
       }
     }
-    return D * (r * (f + c));
+    return r * (f + c);
   }
   __device__ static V rsub1(V a) { return 1.0 - a; }
   __device__ static V max0(V a) { return fmax(a, 0.0); }
@@ -211,10 +213,10 @@ struct DWA {
   __device__ static V div(V a, V b) { return dw_div(a, b); }
   __device__ static V abs(V a) { return dw_abs(a); }
   __device__ static V neg(V a) { return dw_neg(a); }
-  // as F64A::start, in double-word: with loss rates up to 10 per day an increment is ~10 % of f,
+  // as F64A::extrap, in double-word: with loss rates up to 10 per day an increment is ~10 % of f,
   // so FP32 increments would leave ~1e-8 of f in the start, above what the extrapolation achieves; the
   // starting point only steers the iteration, the converged answer does not depend on it
-  __device__ static V start(V D, V f, V h1, V h2, V h3, V h4, int n, V r) {
+  __device__ static V extrap(V f, V h1, V h2, V h3, V h4, int n, V r) {
     const dw c1 = dw_mul(h1, r);
     const dw d1 = sub(f, c1);
     dw c = d1;
@@ -230,7 +232,7 @@ struct DWA {
                    : sub(sub(dw_mul_f(add(d1, d3), 4.0f), dw_mul_f(d2, 6.0f)), sub(c3, dw_mul(h4, dw_mul(r3, r))));
       }
     }
-    return dw_mul(D, dw_mul(r, add(f, c)));
+    return dw_mul(r, add(f, c));
   }
   __device__ static V rsub1(V a) { return dw_add_f(dw_neg(a), 1.0f); }  // 1 - a (DWPlusFP)
   __device__ static V max0(V a) { return dw_max0(a); }
@@ -316,6 +318,24 @@ __device__ __forceinline__ void setup_faces(const Geo& geo, long long K, double 
   A::st(geo.Sy, K, A::from_d(__dadd_rn(aa, ab)));
 }
 
+// Every time-independent per-cell value of cell K from its edges, dt, G, D and 1/tau: the face
+// factors (setup_faces), G (when kept), UKK = G * (dx*dy/dt), the diagonal term UKK*(1 + dt/tau)
+// (Solver.cc:190-199, Mesh.h:61-63) and the one-step loss factor 1/(1 + dt/tau) (when kept). The
+// one definition k_setup and the allocation-free entry point's set-up both call.
+template <typename A>
+__device__ __forceinline__ void setup_cell(const Geo& geo, long long K, double xl, double xr, double yb,
+                                           double yt, double dt, double g, double dxx, double dxy, double dyy,
+                                           double itau) {
+  const double dx = __dadd_rn(xr, -xl), dy = __dadd_rn(yt, -yb);
+  setup_faces<A>(geo, K, xl, xr, yb, yt, g, dxx, dxy, dyy);
+  if (geo.G) geo.G[K] = g;
+  const double ukk = __dmul_rn(g, __ddiv_rn(__dmul_rn(dx, dy), dt));
+  A::st(geo.ukk, K, A::from_d(ukk));
+  const double lossd = __dadd_rn(1.0, __dmul_rn(dt, itau));
+  A::st(geo.sdiag, K, A::from_d(__dmul_rn(ukk, lossd)));
+  if (geo.decay) A::st(geo.decay, K, A::from_d(__ddiv_rn(1.0, lossd)));
+}
+
 // One instance: stage holds alpha-major G, Dxx, Dxy, Dyy, inv_tau, f0 (each nx*ny). mask bits
 // 0-4 select the coefficient sections (all five together), bit 5 the initial state. Values are
 // computed in FP64 and stored in the policy's wide format.
@@ -334,20 +354,9 @@ __global__ void k_setup(Common cm, Geo geo, double* f, const double* stage, cons
        c += (long long)gridDim.x * blockDim.x) {
     const int i = (int)(c / I.ny), j = (int)(c % I.ny);
     const long long K = I.base + (long long)j * I.pitch + i;
-    if (mask & 31) {
-      const double xl = xe[I.xe + i], xr = xe[I.xe + i + 1];
-      const double yb = ye[I.ye + j], yt = ye[I.ye + j + 1];
-      const double dx = __dadd_rn(xr, -xl), dy = __dadd_rn(yt, -yb);
-      const double g = G[c];
-      setup_faces<A>(geo, K, xl, xr, yb, yt, g, Dxx[c], Dxy[c], Dyy[c]);
-      if (geo.G) geo.G[K] = g;
-      // UKK = G * (dx*dy/dt); diagonal UKK*(1 + dt/tau) (Solver.cc:190-199, Mesh.h:61-63)
-      const double ukk = __dmul_rn(g, __ddiv_rn(__dmul_rn(dx, dy), I.dt));
-      A::st(geo.ukk, K, A::from_d(ukk));
-      const double lossd = __dadd_rn(1.0, __dmul_rn(I.dt, itau[c]));
-      A::st(geo.sdiag, K, A::from_d(__dmul_rn(ukk, lossd)));
-      if (geo.decay) A::st(geo.decay, K, A::from_d(__ddiv_rn(1.0, lossd)));
-    }
+    if (mask & 31)
+      setup_cell<A>(geo, K, xe[I.xe + i], xe[I.xe + i + 1], ye[I.ye + j], ye[I.ye + j + 1], I.dt, G[c], Dxx[c],
+                    Dxy[c], Dyy[c], itau[c]);
     if (mask & 32) A::st(f, K, A::from_d(f0[c]));
   }
 }
@@ -592,11 +601,11 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
     const int i0 = (lt % I.ntx) * kTX, j0 = (lt / I.ntx) * kTY;
     const int nx = I.nx, ny = I.ny, P = I.pitch;
     const long long base = I.base;
-    const int nh = min(cm.st[b].nhist, cm.hist_cap), hs = cm.st[b].hslot;
-    const double* h1p = fl.fh[hs];
-    const double* h2p = fl.fh[(hs + kHist - 1) % kHist];
-    const double* h3p = fl.fh[(hs + kHist - 2) % kHist];
-    const double* h4p = fl.fh[(hs + kHist - 3) % kHist];
+    // the extrapolated start g the last polish left in the idle y buffer (none before the first
+    // step or after the state was replaced: then y0 = D f)
+    const bool has_g = cm.st[b].nhist > 0;
+    const int yc = cm.st[b].ycur;
+    const double* gp = fl.y64[yc ^ 1];
     // the per-cell data of step 4 is only needed after three barriers: start its trip to L2 now
 #pragma unroll
     for (int q = threadIdx.x; q < kTX * kTY; q += kAsmThreads) {
@@ -605,11 +614,7 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
         const long long K = base + (long long)j * P + i;
         asm volatile("prefetch.global.L2 [%0];" ::"l"(geo.sdiag + K));
         asm volatile("prefetch.global.L2 [%0];" ::"l"(geo.ukk + K));
-        if (nh > 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(h1p + K));
-        if (nh > 1) asm volatile("prefetch.global.L2 [%0];" ::"l"(h2p + K));
-        if (nh > 2) asm volatile("prefetch.global.L2 [%0];" ::"l"(h3p + K));
-        if (nh > 3) asm volatile("prefetch.global.L2 [%0];" ::"l"(h4p + K));
-        if (nh > 0 && geo.decay) asm volatile("prefetch.global.L2 [%0];" ::"l"(geo.decay + K));
+        if (has_g) asm volatile("prefetch.global.L2 [%0];" ::"l"(gp + K));
       }
     }
     // 1) f and 1/(f+eps) on the tile plus a one-cell halo
@@ -742,18 +747,10 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
       A::st(fl.invD, K, inv);
       A::st(fl.R, K, Rv);
       A::st(fl.colsum, K, A::addp(sd, dir));
-      // start the solve from the loss-compensated polynomial extrapolation in time through f^n and
-      // up to four earlier states (only the starting point of the iteration; the converged
-      // answer does not depend on it)
-      V y0;
-      if (nh == 0) {
-        y0 = A::mul(D, fK);
-      } else {
-        const V h1 = A::ld(h1p, K), h2 = nh >= 2 ? A::ld(h2p, K) : h1, h3 = nh >= 3 ? A::ld(h3p, K) : h2;
-        const V h4 = nh >= 4 ? A::ld(h4p, K) : h3;
-        y0 = A::start(D, fK, h1, h2, h3, h4, nh, geo.decay ? A::ld(geo.decay, K) : A::k(1.0));
-      }
-      A::st(fl.y64[cm.st[b].ycur], K, y0);
+      // start the solve from D g, g the loss-compensated polynomial extrapolation in time the
+      // last polish formed (only the starting point of the iteration; the converged answer does
+      // not depend on it)
+      A::st(fl.y64[yc], K, A::mul(D, has_g ? A::ld(gp, K) : fK));
       if (wIn) AsmOut<C, A>::put(co, 1, K - 1, A::mul(Aw, inv));  // row K-1, east entry
       if (eIn) AsmOut<C, A>::put(co, 0, K + 1, A::mul(Ae, inv));  // row K+1, west entry
       if (sIn) AsmOut<C, A>::put(co, 3, K - P, A::mul(As, inv));  // row K-P, north entry
@@ -1255,6 +1252,8 @@ __global__ void __launch_bounds__(kThreads, krylov_blocks<T>()) k_bicg3(Common c
 // y' = R + (I - A~) max(y, 0) >= 0 (R >= 0, fractions >= 0), f = y' / D; partials: sum colsum*f,
 // sum R, clamped count; the chunk minimum of f travels in part slot 3. Chunks [c0, c1) of the
 // list (c1 < 0: all); a range must hold whole instances.
+// It also forms the next solve's start g (extrap over the new f, f^n and up to kOrder - 1 earlier
+// states from the history) into the idle y buffer, and moves f^n into the oldest history slot.
 template <typename C, typename A, int CH>
 __global__ void __launch_bounds__(kThreads, 3) k_polish(Common cm, Fields fl, Coef<C> co, int c0, int c1) {
   using V = typename A::V;
@@ -1267,6 +1266,13 @@ __global__ void __launch_bounds__(kThreads, 3) k_polish(Common cm, Fields fl, Co
     InstState& st = cm.st[b];
     const InstDev I = cm.inst[b];
     const double* y = fl.y64[st.ycur];
+    double* gout = fl.y64[st.ycur ^ 1];
+    // earlier states for the next start: f^n (the current f) and up to kOrder - 1 from the history
+    const int nh = min(min(st.nhist + 1, kOrder), cm.hist_cap), hs = st.hslot;
+    const double* h2p = fl.fh[hs];
+    const double* h3p = fl.fh[(hs + 2) % kHist];
+    const double* h4p = fl.fh[(hs + 1) % kHist];
+    double* hw = fl.fh[(hs + 1) % kHist];  // the oldest slot (f^(n-3)) takes f^n
     const int P = I.pitch;
     const long long c0 = chunk_start<CH>(c, I);
     const long long c1 = min(c0 + (long long)CH, inst_end(I));
@@ -1305,7 +1311,18 @@ __global__ void __launch_bounds__(kThreads, 3) k_polish(Common cm, Fields fl, Co
             mn = fminf(mn, A::f32(fv));
           }
         }
-        A::st4(fl.fh[(st.hslot + 1) % kHist] + K, A::ld4(fl.f + K));  // f^n into the oldest slot
+        const Q4<V> fn = A::ld4(fl.f + K);
+        Q4<V> g;
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+          // the states read here (the oldest one included) are read before the slot is replaced
+          const V h2 = nh >= 2 ? A::ld(h2p, K + m) : fn.a[m];
+          const V h3 = nh >= 3 ? A::ld(h3p, K + m) : h2;
+          const V h4 = nh >= 4 ? A::ld(h4p, K + m) : h3;
+          g.a[m] = A::extrap(fo.a[m], fn.a[m], h2, h3, h4, nh, fl.decay ? A::ld(fl.decay, K + m) : A::k(1.0));
+        }
+        A::st4(gout + K, g);
+        A::st4(hw + K, fn);  // f^n into the oldest slot
         A::st4(fl.f + K, fo);
       }
     }
@@ -1343,7 +1360,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_polish(Common cm, Fields fl, Co
         st.mass_drift = tot[1] != 0.0 ? fabs(tot[0] - tot[1]) / fabs(tot[1]) : 0.0;
         st.steps += 1;
         st.hslot = (st.hslot + 1) % kHist;
-        st.nhist = min(st.nhist + 1, kHist);
+        st.nhist = min(st.nhist + 1, kOrder);
         if (!(gmin >= 0.0)) st.status = ST_NEGATIVE;
       }
     }
