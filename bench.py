@@ -118,6 +118,10 @@ def parse():
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
     ap.add_argument("--serve-lanes", type=int, default=2, help="server lanes (2: grids <= 128 in their own lane)")
     ap.add_argument("--serve-only", action="store_true")
+    ap.add_argument("--saturate", type=int, default=1000,
+                    help="requests submitted at once for the serving-capacity run (0: skip)")
+    ap.add_argument("--plain-serve-sample", type=int, default=24,
+                    help="requests of that burst run through the one-at-a-time plain FP64 drop-in")
     ap.add_argument("--launch-shape", default="",
                     help="CHUNK,BLOCKS_PER_SM instead of the autotuner (e.g. 4096,32; for profiling)")
     ap.add_argument("--no-graph", action="store_true",
@@ -312,12 +316,13 @@ def run_reference(a):
 # Algorithmic bytes per real cell per launch (FP32+refine path): reads + writes of the arrays
 # each kernel must touch once (neighbour re-reads served by cache are not counted).
 BYTES32 = {
-    "assemble": 6 * 8 + 8 * 8 + 4 * (4 + 4) + 4 * 8,  # f, 4 earlier states, loss factor, 8 factors -> 4 hi+lo coefs, invD/R/colsum/y
+    "assemble": 2 * 8 + 8 * 8 + 4 * (4 + 4) + 4 * 8,  # f, start g, 8 factors -> 4 hi+lo coefs, invD/R/colsum/y
     "resid": 8 + 4 + 8 + 4 * (4 + 4) + 8 + 4,     # y, x, R, hi+lo coefs -> y', r
     "bicg1": 4 * 4 + 4 * 4 + 2 * 4,               # r, p, v, r^, 4 coefs -> p', v'
     "bicg2": 2 * 4 + 4 * 4 + 4,                   # r, v, 4 coefs -> t
     "bicg3": 6 * 4 + 2 * 4,                       # r, v, p, t, r^, x -> x, r
-    "polish": 8 + 4 * (4 + 4) + 3 * 8 + 8 + 2 * 8,  # y, hi+lo coefs, R, invD, colsum -> f; f -> history
+    "polish": 8 + 4 * (4 + 4) + 3 * 8 + 8 + 3 * 8 + 8 + 3 * 8,  # y, hi+lo coefs, R, invD, colsum, f, 3 earlier
+                                                            # states, loss factor -> f, history slot, start g
 }
 
 
@@ -332,10 +337,16 @@ BYTES64 = {
 }
 
 
+# The algorithmic bytes per cell of the hot-path analysis, for the assembly: read f, Lxx, Lxy,
+# Lyy, UKK, s (48 B), write 5 coefficients and R (48 B). The roofline's `achieved` and `frac` use
+# it; the design's own model above (what this layout must move) is reported beside it.
+ANALYSIS_BYTES = {"assemble": 96}
+
+
 # DRAM bytes per processed cell measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the
 # 256-instance case of the same kernels (one ncu capture per kernel); traffic grows with the
 # cells processed, so a launch's traffic is this figure times the cells it processed.
-TRAFFIC32 = {"assemble": 175.2, "bicg1": 40.3, "bicg2": 27.9, "resid": 60.9, "polish": 92.9}
+TRAFFIC32 = {"assemble": 146.5, "bicg1": 40.3, "bicg2": 27.9, "resid": 60.9, "polish": 137.3}
 
 
 def kernel_roofline(b, probs, peak, steps=2, model=None):
@@ -361,7 +372,7 @@ def kernel_roofline(b, probs, peak, steps=2, model=None):
                          "share": 0.0}
         else:
             out[name] = {"ms": ms, "launches": int(n)}
-    total = sum(v["ms"] for v in out.values())
+    total = sum(v["ms"] for k, v in out.items() if not k.startswith("krylov_"))
     for v in out.values():
         v["share"] = v["ms"] / total if total else 0.0
     dom = max((k for k in out if k in model), key=lambda k: out[k]["ms"])
@@ -369,10 +380,17 @@ def kernel_roofline(b, probs, peak, steps=2, model=None):
     ach = d["GBps"]
     traffic = (TRAFFIC32[dom] * d["bytes"] / BYTES32[dom] / d["launches"]
                if dom in TRAFFIC32 and model is BYTES32 else None)
+    design = ach
+    if dom in ANALYSIS_BYTES:
+        ach = design * ANALYSIS_BYTES[dom] / model[dom]
     roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak[0], "unit": "GB/s",
             "frac": ach / peak[0], "peak_source": peak[1], "traffic": traffic,
+            "bytes_per_cell_analysis": ANALYSIS_BYTES.get(dom, model[dom]),
+            "achieved_design_model": design, "frac_design_model": design / peak[0],
+            "bytes_per_cell_design_model": model[dom],
             "traffic_source": "ncu dram bytes per cell on 256 instances, scaled by the cells processed",
-            "bytes_per_launch": d["bytes"] / d["launches"], "avg_launch_ms": d["ms"] / d["launches"]}
+            "bytes_per_launch": d["bytes"] / d["launches"] * (ANALYSIS_BYTES.get(dom, model[dom]) / model[dom]),
+            "avg_launch_ms": d["ms"] / d["launches"]}
     return roof, out
 
 
@@ -438,6 +456,53 @@ def run_serving(capi, arrivals, probs, steps, precision, budget_gb, lanes=2):
             "min_f": min_f, "not_converged": not_conv, "device_gb": info["device_bytes"] / 1e9}
 
 
+def run_saturation(capi, probs, steps, precision, budget_gb, lanes=2):
+    """Serving capacity: every request is submitted at once (arrivals far above what the device
+    drains) and the server ticks until all have completed. Reports the drain throughput
+    (instance-steps and cell-steps per second over the whole drain) and the same over the time
+    in which the first 90 % of the instance-steps were done (the last requests, the longest
+    ones, finish with few instances resident), with p50/p99 completion times."""
+    srv = capi.Server(budget_gb * 1e9, max_slots=4096, max_side=512, precision=precision, lanes=lanes,
+                      split_side=128, small_fraction=0.25)
+    total_is = int(sum(int(n) for n in steps))
+    total_cs = float(sum(p.nx * p.ny * int(n) for p, n in zip(probs, steps)))
+    t0 = time.monotonic()
+    live = {srv.submit(p, int(n)): k for k, (p, n) in enumerate(zip(probs, steps))}
+    done_t, trace = [], []
+    while live:
+        if srv.tick() > 0:
+            for rid in srv.completed_ids():
+                srv.poll(rid, want_f=False)
+                live.pop(rid)
+                done_t.append(time.monotonic() - t0)
+        trace.append((time.monotonic() - t0, srv.info()["instance_steps"]))
+    wall = time.monotonic() - t0
+    info = srv.info()
+    srv.close()
+    t90 = next(t for t, n in trace if n >= 0.9 * total_is)
+    ct = np.array(done_t) * 1e3
+    return {"requests": len(probs), "lanes": lanes, "wall_s": wall,
+            "instance_steps_per_s": total_is / wall, "cell_steps_per_s": total_cs / wall,
+            "instance_steps_per_s_first90": 0.9 * total_is / t90, "t90_s": t90,
+            "completion_p50_ms": float(np.percentile(ct, 50)), "completion_p99_ms": float(np.percentile(ct, 99)),
+            "ticks": info["ticks"], "device_gb": info["device_bytes"] / 1e9}
+
+
+def run_plain_dropin(capi, probs, steps):
+    """The one-at-a-time plain FP64 drop-in on the same requests: one sayram_create per request,
+    its steps, the result read back, destroyed; instance-steps and cell-steps per second."""
+    t0 = time.monotonic()
+    for p, n in zip(probs, steps):
+        s = capi.Solver(p, precision=capi.FP64)
+        s.step(int(n), allow_not_converged=True)
+        s.f()
+        s.close()
+    wall = time.monotonic() - t0
+    return {"requests": len(probs), "wall_s": wall,
+            "instance_steps_per_s": sum(int(n) for n in steps) / wall,
+            "cell_steps_per_s": float(sum(p.nx * p.ny * int(n) for p, n in zip(probs, steps))) / wall}
+
+
 def run_1024(capi, peak):
     """The single-instance 1024 x 1024 configuration (dt = 1e-2): device-timed steps/s of the
     plain FP64 drop-in and of the double-word path, each with both inner-solve preconditioners;
@@ -458,7 +523,7 @@ def run_1024(capi, peak):
             fs[(name, pcn)] = s.f()
             _, kern = kernel_roofline(s, [p], peak, steps=2, model=model)
             step_bytes = sum(v.get("bytes", 0.0) for v in kern.values()) / 2
-            kms = sum(v["ms"] for v in kern.values()) / 2
+            kms = sum(v["ms"] for k, v in kern.items() if not k.startswith("krylov_")) / 2
             out[f"{name}/{pcn}"] = {
                 "steps_per_s": 1e3 / ms, "ms_per_step": ms, "iterations_last_step": st["iterations"],
                 "refinements_last_step": st["refinements"], "rel_residual": st["rel_residual"],
@@ -509,6 +574,7 @@ def run_ours(a, R: Ranks):
     value = R.world * a.instances * a.steps / (ms * 1e-3)
     peak = peak_hbm()
     roof, kern = kernel_roofline(b, probs, peak)
+    tail = kern.get("krylov_tail10", {"ms": 0.0, "share": 0.0})
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": R.world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+dw" if a.precision == "dw" else "f32+f64",
@@ -528,6 +594,9 @@ def run_ours(a, R: Ranks):
                        "launch_shape": {"cells_per_chunk": shape[0], "blocks_per_sm": shape[1],
                                         "autotune_s": tune_s, "candidates": b.tuning_log()}},
             "gpu_launches": int(launches), "roofline": roof, "kernels": kern, "clocks": clocks,
+            "krylov_tail10": {"share_of_step_kernel_time": tail["share"],
+                              "what": "BiCGSTAB iterations in which < 10 % of the instances were still iterating "
+                                      "(host-loop timing steps)"},
             "status_last_step": rc, "setup_s": {"generate": gen_s}}
     # accuracy: per-instance stats and rel L2 against the batched FP64 path after the same steps
     st = [b.stats(k) for k in range(len(probs))]
@@ -640,7 +709,28 @@ def run_ours(a, R: Ranks):
         if not a.quick:
             line["serving_plain_fp64"] = {"config": cfg, "precision": "fp64",
                                           **run_serving(capi, arr, sprobs, ssteps, capi.FP64, a.serve_budget_gb, a.serve_lanes)}
+    if a.saturate > 0 and R.world == 1 and not a.quick:
+        line["serving_capacity"] = saturation(capi, a)
     R.emit(line)
+
+
+def saturation(capi, a):
+    """Serving capacity on a burst of --saturate requests of the serving distribution (seeded):
+    dw serving, plain FP64 serving and the one-at-a-time plain FP64 drop-in (on the burst's first
+    --plain-serve-sample requests); the ratios use cell-steps/s, which does not depend on which
+    requests a sample holds."""
+    _, bprobs, bsteps = serving_requests(a.saturate, 1.0, a.seed + 1)
+    out = {"config": f"{a.saturate} requests submitted at once, n~logU[32,512] (n x n), steps~logU[10,2000], "
+                     f"dt={DT} day, HBM budget {a.serve_budget_gb} GB, {a.serve_lanes} lanes"}
+    out["fp32_refine_dw"] = run_saturation(capi, bprobs, bsteps, capi.FP32_REFINE_DW, a.serve_budget_gb, a.serve_lanes)
+    out["fp64"] = run_saturation(capi, bprobs, bsteps, capi.FP64, a.serve_budget_gb, a.serve_lanes)
+    m = min(a.plain_serve_sample, a.saturate)
+    out["plain_fp64_dropin"] = {"sample": f"first {m} requests of the burst", **run_plain_dropin(capi, bprobs[:m], bsteps[:m])}
+    cs = lambda k: out[k]["cell_steps_per_s"]
+    out["speedup_cell_steps"] = {"dw_serving_vs_plain_dropin": cs("fp32_refine_dw") / cs("plain_fp64_dropin"),
+                                 "dw_serving_vs_fp64_serving": cs("fp32_refine_dw") / cs("fp64"),
+                                 "fp64_serving_vs_plain_dropin": cs("fp64") / cs("plain_fp64_dropin")}
+    return out
 
 
 def run_serve_only(a):

@@ -209,7 +209,9 @@ int sayram_batch_record_event(sayram_batch b, int slot);
 int sayram_batch_elapsed_ms(sayram_batch b, int slot0, int slot1, double* ms);
 /* Per-kernel timing: when enabled, every launch is bracketed by CUDA events on the batch's
  * stream (steps then run without graphs). sayram_batch_kernel_times fills up to cap entries of
- * names/total milliseconds/launch counts and returns the number of kernels. */
+ * names/total milliseconds/launch counts and returns the number of entries: one per kernel, plus
+ * "krylov_tail10" and "krylov_rest", the time of whole BiCGSTAB iterations (their three kernels)
+ * in which fewer than 10 % / at least 10 % of the enabled instances were still iterating. */
 int sayram_batch_enable_timing(sayram_batch b, int enable);
 int sayram_batch_kernel_times(sayram_batch b, const char** names, double* total_ms,
                               long long* launches, int cap);

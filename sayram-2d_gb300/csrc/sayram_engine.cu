@@ -293,6 +293,11 @@ struct sayram_batch_s {
   };
   std::vector<Tuned> tune_log;
   int grid_tiles() const { return std::max(1, std::min(cap_tiles, nsm * 8)); }
+  int n_enabled() const {
+    int k = 0;
+    for (int b = 0; b < n && b < (int)hinst.size(); ++b) k += hinst[b].enabled ? 1 : 0;
+    return k;
+  }
 
   int build(const sayram_problem* probs, int count, const sayram_options* o);
   int set_options(const sayram_options* o);
@@ -661,11 +666,24 @@ int sayram_batch_s::step_once(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, c
     if (rc) return rc;
     if (h_ctl->n_outer == 0) break;
     for (int it = 0; it < opt.max_iters; ++it) {
-      launch("bicg1", [&] { k_bicg1<T, CH><<<gs, kThreads, smem_spmv<T>(), stream>>>(cm, ck, kr); });
-      launch("bicg2", [&] { k_bicg2<T, CH><<<gs, kThreads, smem_spmv<T>(), stream>>>(cm, ck, kr); });
-      launch("bicg3", [&] { k_bicg3<T, CH><<<gs, kThreads, 0, stream>>>(cm, kr, opt.max_iters); });
+      // per-kernel timing also splits the Krylov time by how many instances are still
+      // iterating: "krylov_tail10" holds the iterations in which fewer than 10 % are
+      bool tail = false;
+      if (timing) {
+        if (it > 0) {
+          rc = read_ctl();
+          if (rc) return rc;
+          if (h_ctl->n_inner == 0) break;
+        }
+        tail = 10LL * h_ctl->n_inner < (long long)n_enabled();
+      }
+      launch(tail ? "krylov_tail10" : "krylov_rest", [&] {
+        launch("bicg1", [&] { k_bicg1<T, CH><<<gs, kThreads, smem_spmv<T>(), stream>>>(cm, ck, kr); });
+        launch("bicg2", [&] { k_bicg2<T, CH><<<gs, kThreads, smem_spmv<T>(), stream>>>(cm, ck, kr); });
+        launch("bicg3", [&] { k_bicg3<T, CH><<<gs, kThreads, 0, stream>>>(cm, kr, opt.max_iters); });
+      });
       SG_CUDA(cudaGetLastError());
-      if (it < 4 || (it & 3) == 3) {
+      if (!timing && (it < 4 || (it & 3) == 3)) {
         rc = read_ctl();
         if (rc) return rc;
         if (h_ctl->n_inner == 0) break;
