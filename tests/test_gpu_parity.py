@@ -325,6 +325,34 @@ def test_config1_prefix_against_superlu_fixture(capi):
         assert f.min() >= 0.0
 
 
+@pytest.mark.parametrize("prec", [0, 2])
+def test_config1_all_500_steps_against_tight_oracle(capi, prec):
+    """Config 1 over its whole run (1024 x 1024, dt = 1e-2, 500 steps) against the tight-residual
+    oracle (restated assembly, alpha-line-preconditioned BiCGSTAB inside refinement with
+    extended-precision residuals; it agrees with the SuperLU direct solve over the first 10
+    steps): a strided sample of f, its row and column sums and its sum of squares at steps 10,
+    100, 250 and 500, FP64 drop-in <= 1e-10, double-word path <= 1e-8, min f >= 0."""
+    path = os.path.join(GOLDEN, "ref_c1_1024_full.npz")
+    if not os.path.exists(path):
+        pytest.skip("ref_c1_1024_full.npz not generated (tests/golden/make_golden.py config1_full)")
+    z = np.load(path)
+    p = cases.synthetic_problem(1024, 1024, 1e-2, seed=11)
+    tol = TOL64 if prec == 0 else TOL32
+    s = capi.Solver(p, precision=prec)
+    done = 0
+    for n in [int(v) for v in z["saves"]]:
+        s.step(n - done)
+        done = n
+        f = s.f()
+        assert f.min() >= 0.0
+        _c1_close(z, f"f{n}", f, tol)
+        ssq = float((f * f).sum())
+        assert abs(ssq - z[f"f{n}_ssq"][0]) <= 2 * tol * z[f"f{n}_ssq"][0], (n, ssq)
+    st = s.get_stats()
+    s.close()
+    assert st["steps"] == 500 and st["status"] == 0
+
+
 def test_config1_size_1024(capi, oracle):
     """The single-instance configuration at full size (1024 x 1024, dt = 1e-2): one step of the
     FP64 path against SuperLU, then size-independent properties over further steps -- the

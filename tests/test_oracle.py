@@ -167,6 +167,35 @@ def test_config1_fixture_inputs():
     assert z["fN_min"][0] >= 0.0 and (z["fN_sub"] >= 0).all()
 
 
+def test_config1_full_fixture(oracle):
+    """The 500-step config-1 fixture: made from the seeded generator's inputs (digest), its tight
+    solves reached a relative residual of <= 1e-12 at every step and agreed with the SuperLU prefix
+    to <= 1e-12 after 1 and 10 steps; one step of the tight solve here reproduces the prefix's
+    first step (the direct solve) to the same bound."""
+    import hashlib
+
+    path = os.path.join(GOLDEN, "ref_c1_1024_full.npz")
+    if not os.path.exists(path):
+        pytest.skip("ref_c1_1024_full.npz not generated (tests/golden/make_golden.py config1_full)")
+    z = np.load(path)
+    pre = np.load(os.path.join(GOLDEN, "ref_c1_1024_prefix.npz"))
+    p = cases.synthetic_problem(1024, 1024, 1e-2, seed=11)
+    h = hashlib.sha256()
+    for k in ("x_edges", "y_edges", "G", "Dxx", "Dxy", "Dyy", "inv_tau", "f0"):
+        h.update(np.ascontiguousarray(getattr(p, k)).tobytes())
+    assert bytes(z["digest"]) == bytes.fromhex(h.hexdigest())
+    assert list(z["saves"]) == [10, 100, 250, 500]
+    assert z["max_rel_residual"][0] <= 1e-12
+    assert z["agree_superlu_step1"][0] <= 1e-12 and z["agree_superlu_step10"][0] <= 1e-12
+    for n in z["saves"]:
+        assert z[f"f{n}_min"][0] >= 0.0 and (z[f"f{n}_sub"] >= 0).all()
+        r, c = z[f"f{n}_rows"], z[f"f{n}_cols"]
+        assert abs(r.sum() - c.sum()) <= 1e-12 * abs(r.sum())
+    np.testing.assert_allclose(z["f10_rows"], pre["fN_rows"], rtol=1e-11, atol=0)
+    f1 = oracle.step(p, None, 1, solver="tight")
+    assert np.linalg.norm(f1[::8, ::8] - pre["f1_sub"]) <= 1e-12 * np.linalg.norm(pre["f1_sub"])
+
+
 def test_ini_semantics(tmp_path):
     """nsteps rounds down to a multiple of nplots and dt = T/nsteps (Parameters.cc:58-60)."""
     ini = tmp_path / "p.ini"
