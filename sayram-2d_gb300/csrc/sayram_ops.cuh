@@ -184,7 +184,9 @@ struct F64A {
 
 struct DWA {
   using V = dw;
-  static constexpr int kAsmBlocks = 4;  // k_assemble: 4 resident blocks (64 registers, no spill)
+  // k_assemble: 5 resident blocks (48 registers, no spill); measured on the 4096-instance batch:
+  // 4 blocks 6.21 ms, 5 blocks 6.08 ms, 6 blocks (40 registers) 6.41 ms per launch
+  static constexpr int kAsmBlocks = 5;
   __device__ static V ld(const double* p, long long i) {
     const float2 q = reinterpret_cast<const float2*>(p)[i];
     return dw{q.x, q.y};
@@ -591,6 +593,8 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
   // side the slot of the missing outside cell holds the face's RHS part instead.
   __shared__ V xL[kTY][VX], xR[kTY][VX];
   __shared__ V yB[VY][kTX], yT[VY][kTX];
+  __shared__ V wS[VX][2];  // the tile's vertex columns: bilinear weights (wL, wR), Solver.cc:333-336
+  __shared__ V hS[VY][2];  // its vertex rows: (wB, wT)
   const V zero = A::k(0.0);
   const int nt_ = t1 < 0 ? n_tiles(cm) : t1;
   for (int t = t0 + blockIdx.x; t < nt_; t += gridDim.x) {
@@ -617,7 +621,21 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
         if (has_g) asm volatile("prefetch.global.L2 [%0];" ::"l"(gp + K));
       }
     }
-    // 1) f and 1/(f+eps) on the tile plus a one-cell halo
+    // 1) the tile's bilinear weights (interior vertex columns / rows only), then f and 1/(f+eps)
+    //    on the tile plus a one-cell halo
+    for (int q = threadIdx.x; q < VX + VY; q += blockDim.x) {
+      if (q < VX) {
+        const int Iv = i0 + q;
+        const bool in = Iv > 0 && Iv < nx;
+        wS[q][0] = in ? A::ld(cm.wx, 2 * (I.xe + Iv)) : zero;
+        wS[q][1] = in ? A::ld(cm.wx, 2 * (I.xe + Iv) + 1) : zero;
+      } else {
+        const int Jv = j0 + (q - VX);
+        const bool in = Jv > 0 && Jv < ny;
+        hS[q - VX][0] = in ? A::ld(cm.wy, 2 * (I.ye + Jv)) : zero;
+        hS[q - VX][1] = in ? A::ld(cm.wy, 2 * (I.ye + Jv) + 1) : zero;
+      }
+    }
     for (int q = threadIdx.x; q < HX * HY; q += blockDim.x) {
       const int hx = q % HX, hy = q / HX;
       const int i = i0 + hx - 1, j = j0 + hy - 1;
@@ -649,14 +667,14 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
         const V f01 = fS[cj1 - j0 + 1][ci0 - i0 + 1], f11 = fS[cj1 - j0 + 1][ci1 - i0 + 1];
         const bool xin = Iv > 0 && Iv < nx, yin = Jv > 0 && Jv < ny;
         if (xin && yin) {
-          const V wL = A::ld(cm.wx, 2 * (I.xe + Iv)), wR = A::ld(cm.wx, 2 * (I.xe + Iv) + 1);
-          const V wB = A::ld(cm.wy, 2 * (I.ye + Jv)), wT = A::ld(cm.wy, 2 * (I.ye + Jv) + 1);
+          const V wL = wS[vx][0], wR = wS[vx][1];
+          const V wB = hS[vy][0], wT = hS[vy][1];
           val = A::fmap(wB, A::fmap(wL, f00, A::mul(wR, f10)), A::mul(wT, A::fmap(wL, f01, A::mul(wR, f11))));
         } else if (yin) {  // vertical boundary edge: linear in y
-          const V wB = A::ld(cm.wy, 2 * (I.ye + Jv)), wT = A::ld(cm.wy, 2 * (I.ye + Jv) + 1);
+          const V wB = hS[vy][0], wT = hS[vy][1];
           val = A::fmap(wB, f00, A::mul(wT, f01));
         } else if (xin) {  // horizontal boundary edge: linear in x
-          const V wL = A::ld(cm.wx, 2 * (I.xe + Iv)), wR = A::ld(cm.wx, 2 * (I.xe + Iv) + 1);
+          const V wL = wS[vx][0], wR = wS[vx][1];
           val = A::fmap(wL, f00, A::mul(wR, f10));
         } else {
           val = f00;  // corner: the single adjacent cell
