@@ -505,7 +505,8 @@ def run_plain_dropin(capi, probs, steps):
 
 def run_1024(capi, peak):
     """The single-instance 1024 x 1024 configuration (dt = 1e-2): device-timed steps/s of the
-    plain FP64 drop-in and of the double-word path, each with both inner-solve preconditioners;
+    plain FP64 drop-in and of the double-word path, each with both inner-solve preconditioners
+    and the launch shape the autotuner picks for it;
     iterations of the last step; the step's HBM fraction (model bytes of every kernel launch in two
     host-loop steps, per step, over the graph step's time); the agreement of the results."""
     p = cases.synthetic_problem(1024, 1024, DT, seed=11)
@@ -514,6 +515,7 @@ def run_1024(capi, peak):
     for name, prec, model in (("fp64", capi.FP64, BYTES64), ("fp32_refine_dw", capi.FP32_REFINE_DW, BYTES32)):
         for pcn, pc in (("alpha_line", capi.PRECOND_ALPHA_LINE), ("jacobi", capi.PRECOND_JACOBI)):
             s = capi.Solver(p, precision=prec, precond=pc)
+            shape = s.autotune(2)  # restores the state: the run below starts from f0
             s.step(4)
             s.record_event(0)
             s.step(10)
@@ -526,6 +528,7 @@ def run_1024(capi, peak):
             kms = sum(v["ms"] for k, v in kern.items() if not k.startswith("krylov_")) / 2
             out[f"{name}/{pcn}"] = {
                 "steps_per_s": 1e3 / ms, "ms_per_step": ms, "iterations_last_step": st["iterations"],
+                "launch_shape": {"cells_per_chunk": shape[0], "blocks_per_sm": shape[1]},
                 "refinements_last_step": st["refinements"], "rel_residual": st["rel_residual"],
                 "model_bytes_per_step": step_bytes, "hbm_frac_step": step_bytes / (ms * 1e-3) / 1e9 / peak[0],
                 "kernel_ms_per_step": kms, "hbm_frac_kernels": step_bytes / (kms * 1e-3) / 1e9 / peak[0],
