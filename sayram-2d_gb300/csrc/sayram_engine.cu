@@ -50,9 +50,7 @@ struct sayram_batch_s {
   int dev = 0;
   int nsm = 0;
   cudaStream_t stream = nullptr;
-  // host copies of sayram_batch_step_host, in pieces spread over kCopyStreams streams
-  static constexpr int kCopyStreams = 1;
-  cudaStream_t cstreams[kCopyStreams] = {};
+  cudaStream_t cstream = nullptr;           // host copies of sayram_batch_step_host, in pieces
   std::vector<cudaEvent_t> piece_ev;        // one per piece and direction
   int n = 0;
   std::vector<InstDev> hinst;
@@ -129,8 +127,8 @@ struct sayram_batch_s {
       if (e) cudaEventDestroy(e), e = nullptr;
     for (auto e : piece_ev) cudaEventDestroy(e);
     piece_ev.clear();
-    for (auto& c : cstreams)
-      if (c) cudaStreamDestroy(c), c = nullptr;
+    if (cstream) cudaStreamDestroy(cstream);
+    cstream = nullptr;
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
   }
@@ -383,7 +381,7 @@ int sayram_batch_s::init_device() {
   SG_CUDA(cudaSetDevice(dev));
   SG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   SG_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-  for (auto& c : cstreams) SG_CUDA(cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking));
+  SG_CUDA(cudaStreamCreateWithFlags(&cstream, cudaStreamNonBlocking));
   return SAYRAM_OK;
 }
 
@@ -1056,7 +1054,7 @@ int sayram_batch_step(sayram_batch b, int nsteps) {
 }
 
 // The instances are split into up to kPieces runs of about equal size at instance boundaries;
-// while the copy engines move one run between host and staging memory (cstreams), the layout
+// while the copy engine moves one run between host and staging memory (cstream), the layout
 // kernel transforms the run before it (stream). Copies go through the copy engine, which is
 // faster than kernels reading host memory over the CPU-GPU link (208 against 153 GB/s on GB300).
 int sayram_batch_step_host(sayram_batch b, int nsteps, const double* f_in, double* f_out) {
@@ -1111,17 +1109,17 @@ int sayram_batch_step_host(sayram_batch b, int nsteps, const double* f_in, doubl
   };
   auto copy_in = [&](size_t k) -> int {  // H2D of piece k on the copy stream, then an event
     const Piece& pc = pieces[k];
-    cudaStream_t cs = b->cstreams[k % sayram_batch_s::kCopyStreams];
-    SG_CUDA(cudaMemcpyAsync(b->d_stage + pc.off, f_in + pc.off, sizeof(double) * pc.len, cudaMemcpyHostToDevice, cs));
-    SG_CUDA(cudaEventRecord(b->piece_ev[k], cs));
+    SG_CUDA(cudaMemcpyAsync(b->d_stage + pc.off, f_in + pc.off, sizeof(double) * pc.len, cudaMemcpyHostToDevice,
+                            b->cstream));
+    SG_CUDA(cudaEventRecord(b->piece_ev[k], b->cstream));
     return SAYRAM_OK;
   };
   auto copy_out = [&](size_t k) -> int {  // after piece k's transform: D2H on the copy stream
     const Piece& pc = pieces[k];
     SG_CUDA(cudaEventRecord(b->piece_ev[np + k], b->stream));
-    cudaStream_t cs = b->cstreams[k % sayram_batch_s::kCopyStreams];
-    SG_CUDA(cudaStreamWaitEvent(cs, b->piece_ev[np + k], 0));
-    SG_CUDA(cudaMemcpyAsync(f_out + pc.off, b->d_stage + pc.off, sizeof(double) * pc.len, cudaMemcpyDeviceToHost, cs));
+    SG_CUDA(cudaStreamWaitEvent(b->cstream, b->piece_ev[np + k], 0));
+    SG_CUDA(cudaMemcpyAsync(f_out + pc.off, b->d_stage + pc.off, sizeof(double) * pc.len, cudaMemcpyDeviceToHost,
+                            b->cstream));
     return SAYRAM_OK;
   };
   // An instance whose state changed restarts its extrapolation history; one given back its own
@@ -1164,7 +1162,7 @@ int sayram_batch_step_host(sayram_batch b, int nsteps, const double* f_in, doubl
         return rc;
       }
     }
-    for (auto c : b->cstreams) SG_CUDA(cudaStreamSynchronize(c));
+    SG_CUDA(cudaStreamSynchronize(b->cstream));
     SG_CUDA(cudaStreamSynchronize(b->stream));
     return b->finish_status();
   }
@@ -1183,7 +1181,7 @@ int sayram_batch_step_host(sayram_batch b, int nsteps, const double* f_in, doubl
       int rc2 = copy_out(k);
       if (rc2) return rc2;
     }
-    for (auto c : b->cstreams) SG_CUDA(cudaStreamSynchronize(c));
+    SG_CUDA(cudaStreamSynchronize(b->cstream));
     SG_CUDA(cudaStreamSynchronize(b->stream));
     if (b->timing) b->collect_timing();
   }
