@@ -346,7 +346,7 @@ ANALYSIS_BYTES = {"assemble": 96}
 # DRAM bytes per processed cell measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the
 # 256-instance case of the same kernels (one ncu capture per kernel); traffic grows with the
 # cells processed, so a launch's traffic is this figure times the cells it processed.
-TRAFFIC32 = {"assemble": 146.5, "bicg1": 40.3, "bicg2": 27.9, "resid": 60.9, "polish": 137.3}
+TRAFFIC32 = {"assemble": 147.8, "bicg1": 40.3, "bicg2": 27.9, "resid": 63.0, "polish": 140.4}
 
 
 def kernel_roofline(b, probs, peak, steps=2, model=None):

@@ -581,3 +581,29 @@ def test_unknown_preconditioner_is_refused(capi):
     p = cases.synthetic_problem(8, 8, 1e-2, seed=1)
     with pytest.raises(RuntimeError, match="unknown preconditioner"):
         capi.Solver(p, precision=capi.FP64, precond=7)
+
+
+def test_per_kernel_timing_and_krylov_split(capi):
+    """Per-kernel timing (host-loop steps bracketed by CUDA events) names every step kernel, and
+    its split of the Krylov time -- whole BiCGSTAB iterations with fewer than / at least 10 % of
+    the instances still iterating -- adds up to the three Krylov kernels' own time; the result is
+    the same as stepping without timing."""
+    probs = [cases.synthetic_problem(40 + 9 * k, 30 + 7 * k, 1e-2, seed=60 + k, tau=0.2 + k) for k in range(12)]
+    a = capi.Batch(probs, precision=capi.FP32_REFINE_DW)
+    b = capi.Batch(probs, precision=capi.FP32_REFINE_DW)
+    a.enable_timing(True)
+    a.step(3)
+    kt = a.kernel_times()
+    a.enable_timing(False)
+    b.step(3)
+    for k in range(len(probs)):
+        assert np.array_equal(a.f(k), b.f(k))
+    a.close()
+    b.close()
+    for name in ("begin", "assemble", "resid", "bicg1", "bicg2", "bicg3", "polish", "krylov_rest"):
+        assert name in kt and kt[name][1] > 0, (name, kt)
+    kry = sum(kt[n][0] for n in ("bicg1", "bicg2", "bicg3"))
+    split = kt["krylov_rest"][0] + kt.get("krylov_tail10", (0.0, 0))[0]
+    assert kry <= split * 1.001 and split <= kry * 1.5 + 0.5, (kry, split)
+    n_iter = kt["krylov_rest"][1] + kt.get("krylov_tail10", (0.0, 0))[1]
+    assert n_iter == kt["bicg1"][1] == kt["bicg3"][1]
