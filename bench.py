@@ -3,20 +3,25 @@
 
 Workload (the batched mixed-precision configuration the headline metric is quoted on): 4096
 independent instances, nalpha and nE each uniform in [64, 256], seeded synthetic D fields
-(rho ~ U[-0.9, 0.9], tau log-uniform in [0.1, 10] days), dt = 1e-2 day, advanced together with
-FP32 matrix/Krylov and FP64 residual/refinement to a relative residual of 1e-10.  One bench
-"step" is one backward-Euler step of every instance (assembly, solve, positivity polish).
+(rho ~ U[-0.9, 0.9], tau log-uniform in [0.1, 10] days), dt = 1e-2 day, advanced together with an
+FP32 Krylov solve (alpha-line block preconditioner) inside double-word (FP32-pair) residual and
+refinement, to a relative residual of 1e-11. One bench "step" is one backward-Euler step of every
+instance (assembly, solve, positivity polish).
 
 Prints ONE JSON line:
   value        instance-steps/s, device-timed (CUDA events on the batch stream), inputs resident
   e2e          the same metric through sayram_batch_step_host with pinned host buffers: every step
                copies all instances' f host->device and the result device->host
-  roofline     the dominant kernel: algorithmic bytes / event-timed duration vs measured HBM peak
+  roofline     the dominant kernel: the analysis' algorithmic bytes / event-timed duration vs the
+               measured HBM copy bandwidth (the design's own byte model beside it)
   cpu_baseline the oracle port (C assembly restatement + SuperLU/COLAMD, the algorithm family of
                the reference's Eigen SparseLU) on one host core, on a bounded sample
   plain_fp64   the single-instance FP64 drop-in (sayram_create/sayram_update) on a sample of the
                same batch, one instance after another
-and accuracy against FP64 (rel L2 per instance vs the batched FP64 path), min cell, mass drift.
+and accuracy: rel L2 error against the oracle on a size-spread sample of the batch and against
+the batched FP64 path, min cell, mass drift; the other arithmetic and preconditioner on the same
+batch; the 1024^2 single instance; serving latency (Poisson stream) and serving capacity (a burst
+against plain-FP64 serving and the one-at-a-time drop-in).
 
 --impl reference times the oracle port on all host cores instead (the reference's own build needs
 Eigen/xtensor/HDF5, which are not available here).
