@@ -119,6 +119,28 @@ def test_batch_vs_oracle(capi, oracle, prec):
 
 
 @pytest.mark.parametrize("prec", [0, 2])
+def test_benchmark_batch_sample_vs_oracle(capi, oracle, prec):
+    """The benchmark's batch distribution (nalpha, nE ~ U[64, 256], rho ~ U[-0.9, 0.9], tau
+    log-uniform in [0.1, 10] days, dt = 1e-2): 48 instances stepped together 4 times; 8 of them,
+    spread over the size range, against the oracle (restated assembly + SuperLU) stepped alone;
+    FP64 <= 1e-10, double-word path <= 1e-8; every instance non-negative and mass-conserving."""
+    sizes = cases.batch_sizes(48, 2024)
+    probs = [cases.batch_instance(k, 2024, 1e-2, sizes[k]) for k in range(48)]
+    b = capi.Batch(probs, precision=prec)
+    b.step(4)
+    tol = TOL64 if prec == 0 else TOL32
+    cells = np.array([a * e for a, e in sizes])
+    pick = sorted({int(np.argsort(cells)[q]) for q in np.linspace(0, 47, 8).round().astype(int)})
+    for k in pick:
+        ref = oracle.step(probs[k], None, 4, solver="splu")
+        assert rel(b.f(k), ref) <= tol, (prec, k, sizes[k], rel(b.f(k), ref))
+    for k in range(48):
+        st = b.stats(k)
+        assert st["min_f"] >= 0.0 and st["mass_drift"] <= 1e-9 and st["status"] == 0, (k, st)
+    b.close()
+
+
+@pytest.mark.parametrize("prec", [0, 2])
 def test_step_host_roundtrip(capi, prec):
     probs = cases.batch_problems(4, seed=2, dt=1e-2, lo=30, hi=70)
     b = capi.Batch(probs, precision=prec)
