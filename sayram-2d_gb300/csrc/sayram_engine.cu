@@ -1053,7 +1053,7 @@ int sayram_batch_step(sayram_batch b, int nsteps) {
   return b->run_steps(nsteps);
 }
 
-// The instances are split into up to kPieces runs of about equal size at instance boundaries;
+// The instances are split into about kPieces runs at instance boundaries (a small first run);
 // while the copy engine moves one run between host and staging memory (cstream), the layout
 // kernel transforms the run before it (stream). Copies go through the copy engine, which is
 // faster than kernels reading host memory over the CPU-GPU link (208 against 153 GB/s on GB300).
@@ -1069,12 +1069,16 @@ int sayram_batch_step_host(sayram_batch b, int nsteps, const double* f_in, doubl
   };
   std::vector<Piece> pieces;
   {
+    // the first run is small (1/32 of the cells): its copy in is what the first assembly waits
+    // for, and its polish is what the first copy out waits for; the rest are about equal
     const long long target = (b->nreal + kPieces - 1) / kPieces;
+    const long long first = (b->nreal + 4 * kPieces - 1) / (4 * kPieces);
     int a = 0;
     while (a < b->n) {
       long long len = 0;
       int e = a;
-      while (e < b->n && (len < target || e == a)) {
+      const long long want = pieces.empty() ? first : target;
+      while (e < b->n && (len < want || e == a)) {
         len += (long long)b->hinst[e].nx * b->hinst[e].ny;
         ++e;
       }
