@@ -292,7 +292,11 @@ struct sayram_batch_s {
     double ms_per_step;
   };
   std::vector<Tuned> tune_log;
-  int grid_tiles() const { return std::max(1, std::min(cap_tiles, nsm * 8)); }
+  // Assembly grid: many short-lived blocks (64 per SM, each a few dozen tiles) rather than one
+  // or two waves of blocks that each walk hundreds of tiles. On the 4096-instance batch the
+  // launch took 6.09 ms with 8 blocks per SM, 6.15 with 5 (one wave), 5.85 with 10, 5.60 with
+  // 20, 5.40 with 40, 5.27 with 64 and 5.32 with one block per tile.
+  int grid_tiles() const { return std::max(1, std::min(cap_tiles, nsm * sg::kAsmGridPerSm)); }
   int n_enabled() const {
     int k = 0;
     for (int b = 0; b < n && b < (int)hinst.size(); ++b) k += hinst[b].enabled ? 1 : 0;
@@ -2126,7 +2130,7 @@ extern "C" int sayram_step_noalloc(const sayram_problem* pd, const sayram_option
   k_setup_fields<<<sblocks, 256, 0, stream>>>(cm, geo, pd->G, pd->Dxx, pd->Dxy, pd->Dyy, pd->inv_tau,
                                              pd->x_edges, pd->y_edges);
   SG_CUDA(cudaGetLastError());
-  const int gt = std::max(1, std::min(cm.ntiles, nsm * 8));
+  const int gt = std::max(1, std::min(cm.ntiles, nsm * kAsmGridPerSm));
   const int gs = std::max(1, std::min(cm.nchunks, nsm * 16));
   k_field_in<F64A><<<gt, 256, 0, stream>>>(cm, fl.f, f_in, 0, 0, -1);
   const size_t smem_na = (size_t)(kNoAllocChunk + 2 * pitch) * sizeof(double);
