@@ -292,10 +292,11 @@ struct sayram_batch_s {
     double ms_per_step;
   };
   std::vector<Tuned> tune_log;
-  // Assembly grid: many short-lived blocks (64 per SM, each a few dozen tiles) rather than one
-  // or two waves of blocks that each walk hundreds of tiles. On the 4096-instance batch the
-  // launch took 6.09 ms with 8 blocks per SM, 6.15 with 5 (one wave), 5.85 with 10, 5.60 with
-  // 20, 5.40 with 40, 5.27 with 64 and 5.32 with one block per tile.
+  // Assembly grid: many short-lived blocks (96 per SM, each a few dozen tiles) rather than one
+  // or two waves of blocks that each walk hundreds of tiles. On the 4096-instance batch, with 5
+  // resident blocks per SM, the launch took 6.09 ms with 8 launched per SM, 6.15 with 5 (one
+  // wave), 5.85 with 10, 5.60 with 20, 5.40 with 40, 5.27 with 64 and 5.32 with one block per
+  // tile; with 6 resident, 5.22 with 48, 5.16 with 64 and 5.09 with 96.
   int grid_tiles() const { return std::max(1, std::min(cap_tiles, nsm * sg::kAsmGridPerSm)); }
   int n_enabled() const {
     int k = 0;

@@ -30,7 +30,7 @@ constexpr int kThreads = 256;  // threads per block of the streaming kernels
 constexpr int kTX = 32;        // assembly tile width (alpha0, contiguous)
 constexpr int kTY = 16;        // assembly tile height (log E)
 constexpr int kAsmThreads = 256;
-constexpr int kAsmGridPerSm = 64;  // k_assemble blocks launched per SM (grid-stride over tiles)
+constexpr int kAsmGridPerSm = 96;  // k_assemble blocks launched per SM (grid-stride over tiles)
 constexpr double kEps = DBL_EPSILON;  // gEPS, source/common.h:38
 
 enum { XMIN = 0, XMAX = 1, YMIN = 2, YMAX = 3 };
@@ -97,6 +97,18 @@ __device__ __forceinline__ void st4(float* p, const Q4<float>& q) {
 __device__ __forceinline__ void st4(double* p, const Q4<double>& q) {
   reinterpret_cast<double2*>(p)[0] = make_double2(q.a[0], q.a[1]);
   reinterpret_cast<double2*>(p)[1] = make_double2(q.a[2], q.a[3]);
+}
+
+// Element i of a small pointer array inside a kernel parameter, chosen by selects: indexing the
+// array with a run-time value makes every thread of every block copy the whole parameter to
+// local memory first (with a grid of ~14,000 assembly blocks, ~300 MB of local stores a launch).
+template <typename P>
+__device__ __forceinline__ P sel2(P const (&a)[2], int i) {
+  return i ? a[1] : a[0];
+}
+template <typename P>
+__device__ __forceinline__ P sel3(P const (&a)[3], int i) {
+  return i == 0 ? a[0] : (i == 1 ? a[1] : a[2]);
 }
 
 __device__ __forceinline__ void count_launch(Ctl* ctl) {

@@ -184,9 +184,10 @@ struct F64A {
 
 struct DWA {
   using V = dw;
-  // k_assemble: 5 resident blocks (48 registers, no spill); measured on the 4096-instance batch:
-  // 4 blocks 6.21 ms, 5 blocks 6.08 ms, 6 blocks (40 registers) 6.41 ms per launch
-  static constexpr int kAsmBlocks = 5;
+  // k_assemble: 6 resident blocks (40 registers, 12 bytes spilled); measured on the 4096-instance
+  // batch with 64 launched blocks per SM: 4 blocks 5.72 ms, 5 blocks (48 registers, no spill)
+  // 5.27 ms, 6 blocks 5.16 ms per launch (with 96 launched per SM: 5.09 ms)
+  static constexpr int kAsmBlocks = 6;
   __device__ static V ld(const double* p, long long i) {
     const float2 q = reinterpret_cast<const float2*>(p)[i];
     return dw{q.x, q.y};
@@ -609,7 +610,7 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
     // step or after the state was replaced: then y0 = D f)
     const bool has_g = cm.st[b].nhist > 0;
     const int yc = cm.st[b].ycur;
-    const double* gp = fl.y64[yc ^ 1];
+    const double* gp = sel2(fl.y64, yc ^ 1);
     // the per-cell data of step 4 is only needed after three barriers: start its trip to L2 now
 #pragma unroll
     for (int q = threadIdx.x; q < kTX * kTY; q += kAsmThreads) {
@@ -768,7 +769,7 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
       // start the solve from D g, g the loss-compensated polynomial extrapolation in time the
       // last polish formed (only the starting point of the iteration; the converged answer does
       // not depend on it)
-      A::st(fl.y64[yc], K, A::mul(D, has_g ? A::ld(gp, K) : fK));
+      A::st(sel2(fl.y64, yc), K, A::mul(D, has_g ? A::ld(gp, K) : fK));
       if (wIn) AsmOut<C, A>::put(co, 1, K - 1, A::mul(Aw, inv));  // row K-1, east entry
       if (eIn) AsmOut<C, A>::put(co, 0, K + 1, A::mul(Ae, inv));  // row K+1, west entry
       if (sIn) AsmOut<C, A>::put(co, 3, K - P, A::mul(As, inv));  // row K-P, north entry
@@ -974,8 +975,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_resid(Common cm, Fields fl, Coe
     const int b = cm.chunk_inst[c];
     InstState& st = cm.st[b];
     const InstDev I = cm.inst[b];
-    const double* yin = fl.y64[st.ycur];
-    double* yout = fl.y64[st.ycur ^ 1];
+    const double* yin = sel2(fl.y64, st.ycur);
+    double* yout = sel2(fl.y64, st.ycur ^ 1);
     const bool hx = st.has_x != 0;
     const float sc = rhs_scale(st.rmax_bits);  // r is handed over as r * sc
     const float isc = 1.0f / sc;                // exact: sc is a power of two
@@ -1087,10 +1088,10 @@ __global__ void __launch_bounds__(kThreads, krylov_blocks<T>()) k_bicg1(Common c
     const bool rs = st.restart != 0;
     const T beta = (T)st.beta, omega = (T)st.omega;
     const T* __restrict__ r = kr.r;
-    const T* __restrict__ po = kr.p[pc];
-    const T* __restrict__ vo = kr.v[pc];
-    T* __restrict__ pn = kr.p[pc ^ 1];
-    T* __restrict__ vn = kr.v[pc ^ 1];
+    const T* __restrict__ po = sel2(kr.p, pc);
+    const T* __restrict__ vo = sel2(kr.v, pc);
+    T* __restrict__ pn = sel2(kr.p, pc ^ 1);
+    T* __restrict__ vn = sel2(kr.v, pc ^ 1);
     const int P = I.pitch;
     const long long c0 = chunk_start<CH>(c, I);
     const long long c1 = min(c0 + (long long)CH, inst_end(I));
@@ -1159,7 +1160,7 @@ __global__ void __launch_bounds__(kThreads, krylov_blocks<T>()) k_bicg2(Common c
     const InstDev I = cm.inst[b];
     const T alpha = (T)st.alpha;
     const T* __restrict__ r = kr.r;
-    const T* __restrict__ vv = kr.v[st.pcur];
+    const T* __restrict__ vv = sel2(kr.v, st.pcur);
     const int P = I.pitch;
     const long long c0 = chunk_start<CH>(c, I);
     const long long c1 = min(c0 + (long long)CH, inst_end(I));
@@ -1214,8 +1215,8 @@ __global__ void __launch_bounds__(kThreads, krylov_blocks<T>()) k_bicg3(Common c
     const InstDev I = cm.inst[b];
     const T alpha = (T)st.alpha, omega = (T)st.omega;
     const bool fresh = st.fresh != 0;
-    const T* pp = kr.p[st.pcur];
-    const T* vv = kr.v[st.pcur];
+    const T* pp = sel2(kr.p, st.pcur);
+    const T* vv = sel2(kr.v, st.pcur);
     T q[2] = {(T)0, (T)0};
 #pragma unroll 2
     for (int g = 0; g < CH / (4 * kThreads); ++g) {
@@ -1285,14 +1286,14 @@ __global__ void __launch_bounds__(kThreads, 4) k_polish(Common cm, Fields fl, Co
     const int b = cm.chunk_inst[c];
     InstState& st = cm.st[b];
     const InstDev I = cm.inst[b];
-    const double* y = fl.y64[st.ycur];
-    double* gout = fl.y64[st.ycur ^ 1];
+    const double* y = sel2(fl.y64, st.ycur);
+    double* gout = sel2(fl.y64, st.ycur ^ 1);
     // earlier states for the next start: f^n (the current f) and up to kOrder - 1 from the history
     const int nh = min(min(st.nhist + 1, kOrder), cm.hist_cap), hs = st.hslot;
-    const double* h2p = fl.fh[hs];
-    const double* h3p = fl.fh[(hs + 2) % kHist];
-    const double* h4p = fl.fh[(hs + 1) % kHist];
-    double* hw = fl.fh[(hs + 1) % kHist];  // the oldest slot (f^(n-3)) takes f^n
+    const double* h2p = sel3(fl.fh, hs);
+    const double* h3p = sel3(fl.fh, (hs + 2) % kHist);
+    const double* h4p = sel3(fl.fh, (hs + 1) % kHist);
+    double* hw = sel3(fl.fh, (hs + 1) % kHist);  // the oldest slot (f^(n-3)) takes f^n
     const int P = I.pitch;
     const long long c0 = chunk_start<CH>(c, I);
     const long long c1 = min(c0 + (long long)CH, inst_end(I));
