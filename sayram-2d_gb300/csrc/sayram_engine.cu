@@ -395,6 +395,8 @@ int sayram_batch_s::init_device() {
 int sayram_batch_s::alloc_storage(long long cells, int slots, int chunks_cap, int tiles_cap, long long xcap,
                                   long long ycap, long long dcap, long long stage_cap) {
   int rc;
+  // k_assemble indexes cells with 32-bit ints (2^31 cells would need ~330 GB of device memory)
+  if (cells >= (1LL << 31) - 1) return fail(SAYRAM_ERR_ARG, "a batch holds at most 2^31 - 2 padded cells");
 #define SG_ALLOC(p, cnt) \
   if ((rc = alloc(&(p), (cnt))) != SAYRAM_OK) return rc
   ncell = cells;

@@ -114,8 +114,10 @@ struct Kry {
 struct F64A {
   using V = double;
   static constexpr int kAsmBlocks = 4;  // k_assemble: resident blocks (64 registers)
-  __device__ static V ld(const double* p, long long i) { return p[i]; }
-  __device__ static void st(double* p, long long i, V v) { p[i] = v; }
+  template <typename Ix>
+  __device__ static V ld(const double* p, Ix i) { return p[i]; }
+  template <typename Ix>
+  __device__ static void st(double* p, Ix i, V v) { p[i] = v; }
   __device__ static Q4<V> ld4(const double* p) { return sg::ld4(p); }
   __device__ static void st4(double* p, const Q4<V>& q) { sg::st4(p, q); }
   __device__ static V add(V a, V b) { return a + b; }
@@ -188,11 +190,13 @@ struct DWA {
   // batch with 64 launched blocks per SM: 4 blocks 5.72 ms, 5 blocks (48 registers, no spill)
   // 5.27 ms, 6 blocks 5.16 ms per launch (with 96 launched per SM: 5.09 ms)
   static constexpr int kAsmBlocks = 6;
-  __device__ static V ld(const double* p, long long i) {
+  template <typename Ix>
+  __device__ static V ld(const double* p, Ix i) {
     const float2 q = reinterpret_cast<const float2*>(p)[i];
     return dw{q.x, q.y};
   }
-  __device__ static void st(double* p, long long i, V v) { reinterpret_cast<float2*>(p)[i] = make_float2(v.hi, v.lo); }
+  template <typename Ix>
+  __device__ static void st(double* p, Ix i, V v) { reinterpret_cast<float2*>(p)[i] = make_float2(v.hi, v.lo); }
   __device__ static Q4<V> ld4(const double* p) {
     const float4 a = reinterpret_cast<const float4*>(p)[0];
     const float4 b = reinterpret_cast<const float4*>(p)[1];
@@ -531,14 +535,16 @@ template <typename C, typename A>
 struct AsmOut;
 template <typename A>
 struct AsmOut<double, A> {
-  __device__ static void put(const Coef<double>& c, int which, long long idx, typename A::V v) {
+  template <typename Ix>
+  __device__ static void put(const Coef<double>& c, int which, Ix idx, typename A::V v) {
     double* a = which == 0 ? c.cw : which == 1 ? c.ce : which == 2 ? c.cs : c.cn;
     a[idx] = A::to_d(v);
   }
 };
 template <typename A>
 struct AsmOut<float, A> {
-  __device__ static void put(const Coef<float>& c, int which, long long idx, typename A::V v) {
+  template <typename Ix>
+  __device__ static void put(const Coef<float>& c, int which, Ix idx, typename A::V v) {
     float hi, lo;
     A::split(v, hi, lo);
     float* a = which == 0 ? c.cw : which == 1 ? c.ce : which == 2 ? c.cs : c.cn;
@@ -605,7 +611,9 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
     const int lt = t - I.tile0;
     const int i0 = (lt % I.ntx) * kTX, j0 = (lt / I.ntx) * kTY;
     const int nx = I.nx, ny = I.ny, P = I.pitch;
-    const long long base = I.base;
+    // 32-bit cell indices: every batch holds fewer than 2^31 cells (checked at allocation), and an
+    // int index makes each address one wide multiply-add
+    const int base = (int)I.base;
     // the extrapolated start g the last polish left in the idle y buffer (none before the first
     // step or after the state was replaced: then y0 = D f)
     const bool has_g = cm.st[b].nhist > 0;
@@ -616,7 +624,7 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
     for (int q = threadIdx.x; q < kTX * kTY; q += kAsmThreads) {
       const int i = i0 + (q % kTX), j = j0 + (q / kTX);
       if (i < nx && j < ny) {
-        const long long K = base + (long long)j * P + i;
+        const int K = base + j * P + i;
         asm volatile("prefetch.global.L2 [%0];" ::"l"(geo.sdiag + K));
         asm volatile("prefetch.global.L2 [%0];" ::"l"(geo.ukk + K));
         if (has_g) asm volatile("prefetch.global.L2 [%0];" ::"l"(gp + K));
@@ -642,7 +650,7 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
       const int i = i0 + hx - 1, j = j0 + hy - 1;
       V fv = zero, iv = zero;
       if (i >= 0 && i < nx && j >= 0 && j < ny) {
-        fv = A::ld(fl.f, base + (long long)j * P + i);
+        fv = A::ld(fl.f, base + j * P + i);
         iv = A::rcp(A::addp(fv, A::k(kEps)));
       }
       fS[hy][hx] = fv;
@@ -692,17 +700,17 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
       if (j < ny && Iv <= nx) {
         const V vLo = vS[ry][vx], vHi = vS[ry + 1][vx];  // vertices (Iv, j), (Iv, j+1)
         if (Iv > 0 && Iv < nx) {
-          const long long K = base + (long long)j * P + Iv, L = K - 1;
+          const int K = base + j * P + Iv, L = K - 1;
           // K's XNEG edge: A=(Iv, j+1), B=(Iv, j); L's XPOS edge: A=(Iv, j), B=(Iv, j+1)
           const V aK = A::fma(A::ld(geo.aAx, K), vHi, A::mul(A::ld(geo.aBx, K), vLo));
           const V aLs = A::fma(A::ld(geo.aAx, L), vLo, A::mul(A::ld(geo.aBx, L), vHi));
           inner_face<A>(aK, A::ld(geo.Sx, K), iS[ry + 1][vx + 1], aLs, A::ld(geo.Sx, L), iS[ry + 1][vx], &aR, &aL);
         } else if (Iv == 0 && I.bc[XMIN] == DIRICHLET) {
-          const long long K = base + (long long)j * P;
+          const int K = base + j * P;
           dirichlet_face<A>(A::fma(A::ld(geo.aAx, K), vHi, A::mul(A::ld(geo.aBx, K), vLo)), A::ld(geo.Sx, K),
                             iS[ry + 1][vx + 1], &aR, &bm);
         } else if (Iv == nx && I.bc[XMAX] == DIRICHLET) {
-          const long long K = base + (long long)j * P + nx - 1;  // XPOS edge: A=(nx, j), B=(nx, j+1)
+          const int K = base + j * P + nx - 1;  // XPOS edge: A=(nx, j), B=(nx, j+1)
           dirichlet_face<A>(A::fma(A::ld(geo.aAx, K), vLo, A::mul(A::ld(geo.aBx, K), vHi)), A::ld(geo.Sx, K),
                             iS[ry + 1][vx], &aL, &bm);
         }
@@ -718,17 +726,17 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
       if (i < nx && Jv <= ny) {
         const V vLe = vS[vy][cx], vRi = vS[vy][cx + 1];  // vertices (i, Jv), (i+1, Jv)
         if (Jv > 0 && Jv < ny) {
-          const long long K = base + (long long)Jv * P + i, L = K - P;
+          const int K = base + Jv * P + i, L = K - P;
           // K's YNEG edge: A=(i, Jv), B=(i+1, Jv); L's YPOS edge: A=(i+1, Jv), B=(i, Jv)
           const V aK = A::fma(A::ld(geo.aAy, K), vLe, A::mul(A::ld(geo.aBy, K), vRi));
           const V aLs = A::fma(A::ld(geo.aAy, L), vRi, A::mul(A::ld(geo.aBy, L), vLe));
           inner_face<A>(aK, A::ld(geo.Sy, K), iS[vy + 1][cx + 1], aLs, A::ld(geo.Sy, L), iS[vy][cx + 1], &aT, &aB);
         } else if (Jv == 0 && I.bc[YMIN] == DIRICHLET) {
-          const long long K = base + i;
+          const int K = base + i;
           dirichlet_face<A>(A::fma(A::ld(geo.aAy, K), vLe, A::mul(A::ld(geo.aBy, K), vRi)), A::ld(geo.Sy, K),
                             iS[vy + 1][cx + 1], &aT, &bm);
         } else if (Jv == ny && I.bc[YMAX] == DIRICHLET) {
-          const long long K = base + (long long)(ny - 1) * P + i;  // YPOS edge: A=(i+1,ny), B=(i,ny)
+          const int K = base + (ny - 1) * P + i;  // YPOS edge: A=(i+1,ny), B=(i,ny)
           dirichlet_face<A>(A::fma(A::ld(geo.aAy, K), vRi, A::mul(A::ld(geo.aBy, K), vLe)), A::ld(geo.Sy, K),
                             iS[vy][cx + 1], &aB, &bm);
         }
@@ -744,7 +752,7 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
       const int cx = q % kTX, cy = q / kTX;
       const int i = i0 + cx, j = j0 + cy;
       if (i >= nx || j >= ny) continue;
-      const long long K = base + (long long)j * P + i;
+      const int K = base + j * P + i;
       const V Aw = xR[cy][cx], Ae = xL[cy][cx + 1], As = yT[cy][cx], An = yB[cy + 1][cx];
       const bool wIn = i > 0, eIn = i < nx - 1, sIn = j > 0, nIn = j < ny - 1;
       V D = zero, Rv = zero, dir = zero;
