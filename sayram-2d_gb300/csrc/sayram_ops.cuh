@@ -124,6 +124,10 @@ struct F64A {
   __device__ static V sub(V a, V b) { return a - b; }
   __device__ static V mul(V a, V b) { return a * b; }
   __device__ static V fma(V a, V b, V c) { return a * b + c; }
+  // a*x + b*y and a*x - b*y (the same expression trees as fma(a, x, mul(b, y)) and
+  // sub(mul(a, x), mul(b, y)))
+  __device__ static V dot2(V a, V x, V b, V y) { return a * x + b * y; }
+  __device__ static V dot2s(V a, V x, V b, V y) { return a * x - b * y; }
   // sums whose terms all have the same sign (cheaper in double-word form)
   __device__ static V addp(V a, V b) { return a + b; }
   __device__ static V fmap(V a, V b, V c) { return a * b + c; }
@@ -213,6 +217,8 @@ struct DWA {
   __device__ static V sub(V a, V b) { return dw_add_same(a, dw_neg(b)); }
   __device__ static V mul(V a, V b) { return dw_mul(a, b); }
   __device__ static V fma(V a, V b, V c) { return dw_fma(a, b, c); }
+  __device__ static V dot2(V a, V x, V b, V y) { return dw_dot2(a, x, b, y); }
+  __device__ static V dot2s(V a, V x, V b, V y) { return dw_dot2(a, x, dw_neg(b), y); }
   __device__ static V addp(V a, V b) { return dw_add_same(a, b); }
   __device__ static V fmap(V a, V b, V c) { return dw_fma(a, b, c); }
   __device__ static V addf(V a, float b) { return dw_add_f(a, b); }
@@ -565,7 +571,7 @@ __device__ __forceinline__ void inner_face(typename A::V aK, typename A::V SK, t
   const V denom = A::addp(A::addp(absK, absL), A::k(2 * kEps));
   const V muK = A::div(A::addp(absL, A::k(kEps)), denom);
   const V muL = A::rsub1(muK);
-  const V B = A::sub(A::mul(muL, aL), A::mul(muK, aK));
+  const V B = A::dot2s(muL, aL, muK, aK);
   // B+ = (|B| + B)/2 goes to K's coefficient, B- = (|B| - B)/2 to L's; at most one is nonzero,
   // so only that one is multiplied by its 1/(f + eps) and added (all terms >= 0)
   const V mK = A::mul(muK, SK), mL = A::mul(muL, SL);
@@ -702,16 +708,16 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
         if (Iv > 0 && Iv < nx) {
           const int K = base + j * P + Iv, L = K - 1;
           // K's XNEG edge: A=(Iv, j+1), B=(Iv, j); L's XPOS edge: A=(Iv, j), B=(Iv, j+1)
-          const V aK = A::fma(A::ld(geo.aAx, K), vHi, A::mul(A::ld(geo.aBx, K), vLo));
-          const V aLs = A::fma(A::ld(geo.aAx, L), vLo, A::mul(A::ld(geo.aBx, L), vHi));
+          const V aK = A::dot2(A::ld(geo.aAx, K), vHi, A::ld(geo.aBx, K), vLo);
+          const V aLs = A::dot2(A::ld(geo.aAx, L), vLo, A::ld(geo.aBx, L), vHi);
           inner_face<A>(aK, A::ld(geo.Sx, K), iS[ry + 1][vx + 1], aLs, A::ld(geo.Sx, L), iS[ry + 1][vx], &aR, &aL);
         } else if (Iv == 0 && I.bc[XMIN] == DIRICHLET) {
           const int K = base + j * P;
-          dirichlet_face<A>(A::fma(A::ld(geo.aAx, K), vHi, A::mul(A::ld(geo.aBx, K), vLo)), A::ld(geo.Sx, K),
+          dirichlet_face<A>(A::dot2(A::ld(geo.aAx, K), vHi, A::ld(geo.aBx, K), vLo), A::ld(geo.Sx, K),
                             iS[ry + 1][vx + 1], &aR, &bm);
         } else if (Iv == nx && I.bc[XMAX] == DIRICHLET) {
           const int K = base + j * P + nx - 1;  // XPOS edge: A=(nx, j), B=(nx, j+1)
-          dirichlet_face<A>(A::fma(A::ld(geo.aAx, K), vLo, A::mul(A::ld(geo.aBx, K), vHi)), A::ld(geo.Sx, K),
+          dirichlet_face<A>(A::dot2(A::ld(geo.aAx, K), vLo, A::ld(geo.aBx, K), vHi), A::ld(geo.Sx, K),
                             iS[ry + 1][vx], &aL, &bm);
         }
       }
@@ -728,16 +734,16 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
         if (Jv > 0 && Jv < ny) {
           const int K = base + Jv * P + i, L = K - P;
           // K's YNEG edge: A=(i, Jv), B=(i+1, Jv); L's YPOS edge: A=(i+1, Jv), B=(i, Jv)
-          const V aK = A::fma(A::ld(geo.aAy, K), vLe, A::mul(A::ld(geo.aBy, K), vRi));
-          const V aLs = A::fma(A::ld(geo.aAy, L), vRi, A::mul(A::ld(geo.aBy, L), vLe));
+          const V aK = A::dot2(A::ld(geo.aAy, K), vLe, A::ld(geo.aBy, K), vRi);
+          const V aLs = A::dot2(A::ld(geo.aAy, L), vRi, A::ld(geo.aBy, L), vLe);
           inner_face<A>(aK, A::ld(geo.Sy, K), iS[vy + 1][cx + 1], aLs, A::ld(geo.Sy, L), iS[vy][cx + 1], &aT, &aB);
         } else if (Jv == 0 && I.bc[YMIN] == DIRICHLET) {
           const int K = base + i;
-          dirichlet_face<A>(A::fma(A::ld(geo.aAy, K), vLe, A::mul(A::ld(geo.aBy, K), vRi)), A::ld(geo.Sy, K),
+          dirichlet_face<A>(A::dot2(A::ld(geo.aAy, K), vLe, A::ld(geo.aBy, K), vRi), A::ld(geo.Sy, K),
                             iS[vy + 1][cx + 1], &aT, &bm);
         } else if (Jv == ny && I.bc[YMAX] == DIRICHLET) {
           const int K = base + (ny - 1) * P + i;  // YPOS edge: A=(i+1,ny), B=(i,ny)
-          dirichlet_face<A>(A::fma(A::ld(geo.aAy, K), vRi, A::mul(A::ld(geo.aBy, K), vLe)), A::ld(geo.Sy, K),
+          dirichlet_face<A>(A::dot2(A::ld(geo.aAy, K), vRi, A::ld(geo.aBy, K), vLe), A::ld(geo.Sy, K),
                             iS[vy][cx + 1], &aB, &bm);
         }
       }

@@ -2,7 +2,8 @@
 // (compiled and run by tests/test_dword.py). For each operation it prints the worst error over
 // random operands, in units of u^2 (u = 2^-24), measured against the bound the kernels rely on:
 //   add, mul, rcp, div, add_same (same signs), add_f, mul_f: relative to the exact result
-//   fma, add_same (any signs): relative to the operands' magnitudes (|x y| + |z|, |x| + |y|)
+//   fma, dot2, add_same (any signs): relative to the operands' magnitudes (|x y| + |z|,
+//   |x y| + |z w|, |x| + |y|)
 #include <cmath>
 #include <cstdio>
 #include <random>
@@ -24,9 +25,9 @@ static dw mk(std::mt19937_64& g, bool neg_ok) {
 int main() {
   std::mt19937_64 g(12345);
   const LD u2 = std::ldexp((LD)1, -48);
-  double w[9] = {0};
-  const char* names[9] = {"add", "add_same_same_sign", "add_same_any_sign_vs_magnitudes", "mul", "rcp", "div",
-                          "fma_vs_magnitudes", "add_f", "mul_f"};
+  double w[10] = {0};
+  const char* names[10] = {"add", "add_same_same_sign", "add_same_any_sign_vs_magnitudes", "mul", "rcp", "div",
+                           "fma_vs_magnitudes", "add_f", "mul_f", "dot2_vs_magnitudes"};
   for (int it = 0; it < 2000000; ++it) {
     dw x = mk(g, true), y = mk(g, true), z = mk(g, true);
     if (it % 4 == 0) {  // near-cancelling pairs
@@ -53,7 +54,16 @@ int main() {
     if (ex != 0) w[7] = std::fmax(w[7], (double)(fabsl(val(sg::dw_add_f(x, y.hi)) - ex) / fabsl(ex) / u2));
     ex = val(x) * (LD)y.hi;
     w[8] = std::fmax(w[8], (double)(fabsl(val(sg::dw_mul_f(x, y.hi)) - ex) / fabsl(ex) / u2));
+    // x*y + z*w, with near-cancelling second products in half of the draws
+    dw zw = mk(g, true), ww = mk(g, true);
+    if (it % 2 == 0) {
+      zw = sg::dw_neg(x);
+      ww = sg::dw_add_f(y, std::ldexp((float)((g() % 1000) + 1), -40) * y.hi);
+    }
+    ex = val(x) * val(y) + val(zw) * val(ww);
+    w[9] = std::fmax(w[9], (double)(fabsl(val(sg::dw_dot2(x, y, zw, ww)) - ex) /
+                                    (fabsl(val(x) * val(y)) + fabsl(val(zw) * val(ww))) / u2));
   }
-  for (int k = 0; k < 9; ++k) std::printf("%s %.3f\n", names[k], w[k]);
+  for (int k = 0; k < 10; ++k) std::printf("%s %.3f\n", names[k], w[k]);
   return 0;
 }

@@ -13,7 +13,7 @@ CSRC = os.path.join(ROOT, "sayram-2d_gb300", "csrc")
 
 BOUNDS = {  # published bounds (Joldes, Muller, Popescu 2017) or the bound stated in dword.cuh
     "add": 3.0, "add_same_same_sign": 3.0, "add_same_any_sign_vs_magnitudes": 3.0, "mul": 4.0,
-    "rcp": 6.0, "div": 8.0, "fma_vs_magnitudes": 6.0, "add_f": 2.0, "mul_f": 2.0,
+    "rcp": 6.0, "div": 8.0, "fma_vs_magnitudes": 6.0, "add_f": 2.0, "mul_f": 2.0, "dot2_vs_magnitudes": 6.0,
 }
 
 
