@@ -28,38 +28,54 @@ struct dw {
 
 #define SG_HD __host__ __device__ __forceinline__
 
+// Every operation below is rounded on its own, as the error-free transformations require: in
+// device code through the _rn intrinsics, which the compiler never fuses into multiply-adds
+// (nvcc fuses a plain a*b + c by default); in host code through plain operators, built with
+// -ffp-contract=off.
+#ifdef __CUDA_ARCH__
+#define DW_ADD(a, b) __fadd_rn((a), (b))
+#define DW_SUB(a, b) __fsub_rn((a), (b))
+#define DW_MUL(a, b) __fmul_rn((a), (b))
+#define DW_FMA(a, b, c) __fmaf_rn((a), (b), (c))
+#else
+#define DW_ADD(a, b) ((a) + (b))
+#define DW_SUB(a, b) ((a) - (b))
+#define DW_MUL(a, b) ((a) * (b))
+#define DW_FMA(a, b, c) fmaf((a), (b), (c))
+#endif
+
 SG_HD dw dw_make(float h, float l) { return dw{h, l}; }
 
 // Fast2Sum: exact s + t = a + b when |a| >= |b| (or a's exponent is at least b's)
 SG_HD dw fast2sum(float a, float b) {
-  const float s = a + b;
-  const float z = s - a;
-  return dw{s, b - z};
+  const float s = DW_ADD(a, b);
+  const float z = DW_SUB(s, a);
+  return dw{s, DW_SUB(b, z)};
 }
 
 // 2Sum: exact s + t = a + b for any a, b
 SG_HD dw two_sum(float a, float b) {
-  const float s = a + b;
-  const float ap = s - b;
-  const float bp = s - ap;
-  const float da = a - ap;
-  const float db = b - bp;
-  return dw{s, da + db};
+  const float s = DW_ADD(a, b);
+  const float ap = DW_SUB(s, b);
+  const float bp = DW_SUB(s, ap);
+  const float da = DW_SUB(a, ap);
+  const float db = DW_SUB(b, bp);
+  return dw{s, DW_ADD(da, db)};
 }
 
 // Fast2Mult: exact p + e = a * b (FMA)
 SG_HD dw two_prod(float a, float b) {
-  const float p = a * b;
-  return dw{p, fmaf(a, b, -p)};
+  const float p = DW_MUL(a, b);
+  return dw{p, DW_FMA(a, b, -p)};
 }
 
 // AccurateDWPlusDW
 SG_HD dw dw_add(dw x, dw y) {
   const dw s = two_sum(x.hi, y.hi);
   const dw t = two_sum(x.lo, y.lo);
-  const float c = s.lo + t.hi;
+  const float c = DW_ADD(s.lo, t.hi);
   const dw v = fast2sum(s.hi, c);
-  const float w = t.lo + v.lo;
+  const float w = DW_ADD(t.lo, v.lo);
   return fast2sum(v.hi, w);
 }
 
@@ -68,8 +84,8 @@ SG_HD dw dw_add(dw x, dw y) {
 // same sign (no cancellation).
 SG_HD dw dw_add_same(dw x, dw y) {
   const dw s = two_sum(x.hi, y.hi);
-  const float v = x.lo + y.lo;
-  const float w = s.lo + v;
+  const float v = DW_ADD(x.lo, y.lo);
+  const float w = DW_ADD(s.lo, v);
   return fast2sum(s.hi, w);
 }
 
@@ -82,9 +98,9 @@ SG_HD dw dw_sub(dw x, dw y) { return dw_add(x, dw_neg(y)); }
 // to a result that cancels (x.lo*y.lo, below u^2 |x y|, is left out).
 SG_HD dw dw_fma(dw x, dw y, dw z) {
   const dw p = two_prod(x.hi, y.hi);
-  const float t = fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, p.lo));
+  const float t = DW_FMA(x.hi, y.lo, DW_FMA(x.lo, y.hi, p.lo));
   const dw s = two_sum(p.hi, z.hi);
-  const float w = (t + z.lo) + s.lo;
+  const float w = DW_ADD(DW_ADD(t, z.lo), s.lo);
   return fast2sum(s.hi, w);
 }
 
@@ -96,32 +112,32 @@ SG_HD dw dw_dot2(dw x, dw y, dw z, dw w) {
   const dw p = two_prod(x.hi, y.hi);
   const dw q = two_prod(z.hi, w.hi);
   const dw s = two_sum(p.hi, q.hi);
-  const float t = fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, p.lo));
-  const float u = fmaf(z.hi, w.lo, fmaf(z.lo, w.hi, q.lo));
-  return fast2sum(s.hi, (t + u) + s.lo);
+  const float t = DW_FMA(x.hi, y.lo, DW_FMA(x.lo, y.hi, p.lo));
+  const float u = DW_FMA(z.hi, w.lo, DW_FMA(z.lo, w.hi, q.lo));
+  return fast2sum(s.hi, DW_ADD(DW_ADD(t, u), s.lo));
 }
 
 // DWPlusFP
 SG_HD dw dw_add_f(dw x, float y) {
   const dw s = two_sum(x.hi, y);
-  const float v = x.lo + s.lo;
+  const float v = DW_ADD(x.lo, s.lo);
   return fast2sum(s.hi, v);
 }
 
 // DWTimesFP3
 SG_HD dw dw_mul_f(dw x, float y) {
   const dw c = two_prod(x.hi, y);
-  const float cl3 = fmaf(x.lo, y, c.lo);
+  const float cl3 = DW_FMA(x.lo, y, c.lo);
   return fast2sum(c.hi, cl3);
 }
 
 // DWTimesDW3
 SG_HD dw dw_mul(dw x, dw y) {
   const dw c = two_prod(x.hi, y.hi);
-  const float tl0 = x.lo * y.lo;
-  const float tl1 = fmaf(x.hi, y.lo, tl0);
-  const float cl2 = fmaf(x.lo, y.hi, tl1);
-  const float cl3 = c.lo + cl2;
+  const float tl0 = DW_MUL(x.lo, y.lo);
+  const float tl1 = DW_FMA(x.hi, y.lo, tl0);
+  const float cl2 = DW_FMA(x.lo, y.hi, tl1);
+  const float cl3 = DW_ADD(c.lo, cl2);
   return fast2sum(c.hi, cl3);
 }
 
@@ -134,8 +150,8 @@ SG_HD dw dw_rcp(dw y) {
   const float t = 1.0f / y.hi;
 #endif
   const dw p = dw_mul_f(y, t);               // y*t ~ 1
-  const float e = (1.0f - p.hi) - p.lo;      // 1 - p.hi is exact (Sterbenz)
-  return fast2sum(t, t * e);
+  const float e = DW_SUB(DW_SUB(1.0f, p.hi), p.lo);  // 1 - p.hi is exact (Sterbenz)
+  return fast2sum(t, DW_MUL(t, e));
 }
 
 SG_HD dw dw_div(dw x, dw y) { return dw_mul(x, dw_rcp(y)); }
@@ -152,5 +168,9 @@ SG_HD dw dw_from_double(double v) {
 SG_HD double dw_to_double(dw x) { return (double)x.hi + (double)x.lo; }
 
 #undef SG_HD
+#undef DW_ADD
+#undef DW_SUB
+#undef DW_MUL
+#undef DW_FMA
 
 }  // namespace sg
