@@ -604,10 +604,18 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
   __shared__ V vS[VY][VX];
   // x-faces: outflow to the left / right cell; y-faces: to the cell below / above. On a Dirichlet
   // side the slot of the missing outside cell holds the face's RHS part instead.
-  __shared__ V xL[kTY][VX], xR[kTY][VX];
+  __shared__ V xLR[2][kTY][VX];
+  V(*const xL)[VX] = xLR[0];
+  V(*const xR)[VX] = xLR[1];
   __shared__ V yB[VY][kTX], yT[VY][kTX];
-  __shared__ V wS[VX][2];  // the tile's vertex columns: bilinear weights (wL, wR), Solver.cc:333-336
-  __shared__ V hS[VY][2];  // its vertex rows: (wB, wT)
+  __shared__ V hS[VY][2];  // the tile's vertex rows: bilinear weights (wB, wT), Solver.cc:333-336
+  // f interpolated along each halo row at each vertex column (steps 1-2 only: shares the face
+  // arrays' storage, which step 3 fills after a barrier)
+  static_assert(HY * VX <= 2 * kTY * VX, "row interpolations must fit in the x-face arrays");
+  V(*const rS)[VX] = reinterpret_cast<V(*)[VX]>(&xLR[0][0][0]);
+  // step 1's thread layout: kRowT threads own one vertex column each and walk its halo rows
+  constexpr int kRowT = VX * 7;
+  static_assert(kRowT < kAsmThreads && 3 * 7 >= HY, "step 1 layout");
   const V zero = A::k(0.0);
   const int nt_ = t1 < 0 ? n_tiles(cm) : t1;
   for (int t = t0 + blockIdx.x; t < nt_; t += gridDim.x) {
@@ -636,35 +644,56 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
         if (has_g) asm volatile("prefetch.global.L2 [%0];" ::"l"(gp + K));
       }
     }
-    // 1) the tile's bilinear weights (interior vertex columns / rows only), then f and 1/(f+eps)
-    //    on the tile plus a one-cell halo
-    for (int q = threadIdx.x; q < VX + VY; q += blockDim.x) {
-      if (q < VX) {
-        const int Iv = i0 + q;
-        const bool in = Iv > 0 && Iv < nx;
-        wS[q][0] = in ? A::ld(cm.wx, 2 * (I.xe + Iv)) : zero;
-        wS[q][1] = in ? A::ld(cm.wx, 2 * (I.xe + Iv) + 1) : zero;
-      } else {
-        const int Jv = j0 + (q - VX);
-        const bool in = Jv > 0 && Jv < ny;
-        hS[q - VX][0] = in ? A::ld(cm.wy, 2 * (I.ye + Jv)) : zero;
-        hS[q - VX][1] = in ? A::ld(cm.wy, 2 * (I.ye + Jv) + 1) : zero;
+    // 1) per vertex column Iv (threads below kRowT) and halo row j: f and 1/(f+eps) of the cell left
+    //    of the column, and r = wL f_left + wR f_right, f interpolated along the row at the column
+    //    (Solver.cc:333-336; a boundary column takes its adjacent cell's f). The remaining threads
+    //    take the right halo column and the vertex-row weights.
+    if (threadIdx.x < kRowT) {
+      const int vx = threadIdx.x % VX, Iv = i0 + vx;
+      const bool xin = Iv > 0 && Iv < nx;
+      const V wL = xin ? A::ld(cm.wx, 2 * (I.xe + Iv)) : zero;
+      const V wR = xin ? A::ld(cm.wx, 2 * (I.xe + Iv) + 1) : zero;
+      for (int hy = threadIdx.x / VX; hy < HY; hy += 7) {
+        const int j = j0 + hy - 1;
+        V fa = zero, ia = zero, r = zero;
+        if (j >= 0 && j < ny && Iv <= nx) {
+          const int K = base + j * P + Iv;  // the cell right of the column
+          V fb = zero;
+          if (Iv > 0) {
+            fa = A::ld(fl.f, K - 1);
+            ia = A::rcp(A::addp(fa, A::k(kEps)));
+          }
+          if (Iv < nx) fb = A::ld(fl.f, K);
+          r = xin ? A::fmap(wL, fa, A::mul(wR, fb)) : (Iv == 0 ? fb : fa);
+        }
+        fS[hy][vx] = fa;
+        iS[hy][vx] = ia;
+        rS[hy][vx] = r;
       }
-    }
-    for (int q = threadIdx.x; q < HX * HY; q += blockDim.x) {
-      const int hx = q % HX, hy = q / HX;
-      const int i = i0 + hx - 1, j = j0 + hy - 1;
-      V fv = zero, iv = zero;
-      if (i >= 0 && i < nx && j >= 0 && j < ny) {
-        fv = A::ld(fl.f, base + j * P + i);
-        iv = A::rcp(A::addp(fv, A::k(kEps)));
+    } else {
+      for (int q = threadIdx.x - kRowT; q < HY + VY; q += kAsmThreads - kRowT) {
+        if (q < HY) {
+          const int i = i0 + kTX, j = j0 + q - 1;
+          V fv = zero, iv = zero;
+          if (i < nx && j >= 0 && j < ny) {
+            fv = A::ld(fl.f, base + j * P + i);
+            iv = A::rcp(A::addp(fv, A::k(kEps)));
+          }
+          fS[q][HX - 1] = fv;
+          iS[q][HX - 1] = iv;
+        } else {
+          const int vy = q - HY, Jv = j0 + vy;
+          const bool in = Jv > 0 && Jv < ny;
+          hS[vy][0] = in ? A::ld(cm.wy, 2 * (I.ye + Jv)) : zero;
+          hS[vy][1] = in ? A::ld(cm.wy, 2 * (I.ye + Jv) + 1) : zero;
+        }
       }
-      fS[hy][hx] = fv;
-      iS[hy][hx] = iv;
     }
     __syncthreads();
     // 2) vertex values (Solver.cc:299-422): corners copy, interior bilinear, boundary edges
-    //    linear, then Dirichlet overrides with XMIN < XMAX < YMIN < YMAX precedence.
+    //    linear, then Dirichlet overrides with XMIN < XMAX < YMIN < YMAX precedence. The bilinear
+    //    value wB (wL f00 + wR f10) + wT (wL f01 + wR f11) is formed from the two row
+    //    interpolations of step 1 with the same operations in the same order.
     for (int q = threadIdx.x; q < VX * VY; q += blockDim.x) {
       const int vx = q % VX, vy = q / VX;
       const int Iv = i0 + vx, Jv = j0 + vy;
@@ -675,24 +704,14 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
       else if (Iv == nx && I.bc[XMAX] == DIRICHLET) val = A::ld(cm.dirv, I.dir[XMAX] + Jv);
       else if (Iv == 0 && I.bc[XMIN] == DIRICHLET) val = A::ld(cm.dirv, I.dir[XMIN] + Jv);
       else {
-        // cells around vertex (Iv, Jv) are (Iv-1|Iv, Jv-1|Jv); clamp to the domain at edges
-        const int ci0 = Iv > 0 ? Iv - 1 : 0, ci1 = Iv < nx ? Iv : nx - 1;
+        // cell rows below / above vertex row Jv, clamped to the domain at the edges
         const int cj0 = Jv > 0 ? Jv - 1 : 0, cj1 = Jv < ny ? Jv : ny - 1;
-        const V f00 = fS[cj0 - j0 + 1][ci0 - i0 + 1], f10 = fS[cj0 - j0 + 1][ci1 - i0 + 1];
-        const V f01 = fS[cj1 - j0 + 1][ci0 - i0 + 1], f11 = fS[cj1 - j0 + 1][ci1 - i0 + 1];
-        const bool xin = Iv > 0 && Iv < nx, yin = Jv > 0 && Jv < ny;
-        if (xin && yin) {
-          const V wL = wS[vx][0], wR = wS[vx][1];
-          const V wB = hS[vy][0], wT = hS[vy][1];
-          val = A::fmap(wB, A::fmap(wL, f00, A::mul(wR, f10)), A::mul(wT, A::fmap(wL, f01, A::mul(wR, f11))));
-        } else if (yin) {  // vertical boundary edge: linear in y
-          const V wB = hS[vy][0], wT = hS[vy][1];
-          val = A::fmap(wB, f00, A::mul(wT, f01));
-        } else if (xin) {  // horizontal boundary edge: linear in x
-          const V wL = wS[vx][0], wR = wS[vx][1];
-          val = A::fmap(wL, f00, A::mul(wR, f10));
+        const V r0 = rS[cj0 - j0 + 1][vx];
+        if (Jv > 0 && Jv < ny) {  // interior and vertical boundary edges: linear in y
+          const V r1 = rS[cj1 - j0 + 1][vx];
+          val = A::fmap(hS[vy][0], r0, A::mul(hS[vy][1], r1));
         } else {
-          val = f00;  // corner: the single adjacent cell
+          val = r0;  // horizontal boundary edges (linear in x) and corners
         }
       }
       vS[vy][vx] = val;
