@@ -351,7 +351,7 @@ ANALYSIS_BYTES = {"assemble": 96}
 # DRAM bytes per processed cell measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the
 # 256-instance case of the same kernels (one ncu capture per kernel); traffic grows with the
 # cells processed, so a launch's traffic is this figure times the cells it processed.
-TRAFFIC32 = {"assemble": 147.8, "bicg1": 40.3, "bicg2": 27.9, "resid": 63.0, "polish": 140.4}
+TRAFFIC32 = {"assemble": 142.5, "bicg1": 27.5, "bicg2": 26.5, "bicg3": 23.2, "resid": 58.1, "polish": 131.5}
 
 
 def kernel_roofline(b, probs, peak, steps=2, model=None):
