@@ -19,6 +19,7 @@
 
 #include <cuda_runtime.h>
 #include <math.h>
+#include <string.h>
 
 namespace sg {
 
@@ -166,6 +167,98 @@ SG_HD dw dw_from_double(double v) {
   return dw{h, (float)(v - (double)h)};
 }
 SG_HD double dw_to_double(dw x) { return (double)x.hi + (double)x.lo; }
+
+// The same conversions for the layout transforms at the API boundary, which convert every cell
+// once per call: there the FP64 pipe (which also carries the FP64<->FP32 conversions, 3-4 per
+// value above) set the time. These do the rounding with integer operations on the bits and give
+// the bits of dw_from_double / dw_to_double for every input; exponents outside the range handled
+// here (zeros, subnormal results, overflow, infinities, NaNs) take the conversions above.
+SG_HD unsigned long long dw_dbits(double v) {
+#ifdef __CUDA_ARCH__
+  return (unsigned long long)__double_as_longlong(v);
+#else
+  unsigned long long u;
+  memcpy(&u, &v, 8);
+  return u;
+#endif
+}
+SG_HD double dw_bitsd(unsigned long long u) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)u);
+#else
+  double v;
+  memcpy(&v, &u, 8);
+  return v;
+#endif
+}
+SG_HD unsigned int dw_fbits(float v) {
+#ifdef __CUDA_ARCH__
+  return __float_as_uint(v);
+#else
+  unsigned int u;
+  memcpy(&u, &v, 4);
+  return u;
+#endif
+}
+SG_HD float dw_bitsf(unsigned int u) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(u);
+#else
+  float v;
+  memcpy(&v, &u, 4);
+  return v;
+#endif
+}
+
+// v = (-1)^s 2^E 1.m with E in [-97, 126]: hi = RN(v) rounds the 53-bit significand to 24 bits
+// (to nearest, ties to even; a carry out of the top bit raises the exponent); v - hi is exactly
+// r 2^(E-52) with the remainder |r| <= 2^28, and lo = RN(r) * 2^(E-52), the one rounding of the
+// exact value: an int-to-float conversion of r (exact below 2^24), then a product by a power of
+// two that is exact whenever it is normal, which |r| >= 2^24 and E >= -97 ensure.
+SG_HD dw dw_from_double_int(double v) {
+  const unsigned long long u = dw_dbits(v);
+  const int e = (int)((u >> 52) & 0x7FF);
+  if (e < 1023 - 97 || e > 1023 + 126) return dw_from_double(v);
+  const unsigned long long full = (u & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  unsigned int keep = (unsigned int)(full >> 29);
+  const int rem = (int)(full & 0x1FFFFFFFull);
+  const bool up = rem > 0x10000000 || (rem == 0x10000000 && (keep & 1u));
+  keep += up ? 1u : 0u;
+  unsigned int ef = (unsigned int)(e - 1023 + 127);
+  if (keep >> 24) {
+    keep >>= 1;
+    ++ef;
+  }
+  const unsigned int sgn = (unsigned int)(u >> 63);
+  const float hi = dw_bitsf((sgn << 31) | (ef << 23) | (keep & 0x7FFFFFu));
+  int r = up ? rem - 0x20000000 : rem;
+  if (sgn) r = -r;
+  const int k = e - 1023 - 52;  // in [-149, 74]
+  const float scale = k >= -126 ? dw_bitsf((unsigned int)(k + 127) << 23) : dw_bitsf(1u << (k + 149));
+#ifdef __CUDA_ARCH__
+  const float rf = __int2float_rn(r);
+#else
+  const float rf = (float)r;
+#endif
+  return dw{hi, DW_MUL(rf, scale)};
+}
+
+// float -> double by moving the fields (normal numbers and zeros; others by conversion)
+SG_HD double dw_f2d_int(float f) {
+  const unsigned int u = dw_fbits(f);
+  const unsigned int e = (u >> 23) & 0xFFu;
+  const unsigned long long s = (unsigned long long)(u >> 31) << 63;
+  if ((u & 0x7FFFFFFFu) == 0u) return dw_bitsd(s);
+  if (e == 0u || e == 0xFFu) return (double)f;
+  return dw_bitsd(s | ((unsigned long long)(e - 127u + 1023u) << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29));
+}
+SG_HD double dw_to_double_int(dw x) {
+#ifdef __CUDA_ARCH__
+  return __dadd_rn(dw_f2d_int(x.hi), dw_f2d_int(x.lo));
+#else
+  return dw_f2d_int(x.hi) + dw_f2d_int(x.lo);
+#endif
+}
 
 #undef SG_HD
 #undef DW_ADD

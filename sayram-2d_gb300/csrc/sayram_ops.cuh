@@ -167,6 +167,9 @@ struct F64A {
   __device__ static float sq32(V a) { return (float)(a * a); }
   __device__ static double to_d(V a) { return a; }
   __device__ static V from_d(double a) { return a; }
+  // the conversions of the layout transforms (none here)
+  __device__ static double to_d_io(V a) { return a; }
+  __device__ static V from_d_io(double a) { return a; }
   __device__ static void split(V a, float& hi, float& lo) {
     hi = __double2float_rn(a);
     lo = __double2float_rn(a - (double)hi);
@@ -256,6 +259,9 @@ struct DWA {
   __device__ static float sq32(V a) { return a.hi * a.hi; }
   __device__ static double to_d(V a) { return dw_to_double(a); }
   __device__ static V from_d(double a) { return dw_from_double(a); }
+  // the same bits with integer rounding (the layout transforms convert every cell per call)
+  __device__ static double to_d_io(V a) { return dw_to_double_int(a); }
+  __device__ static V from_d_io(double a) { return dw_from_double_int(a); }
   __device__ static void split(V a, float& hi, float& lo) {
     hi = a.hi;
     lo = a.lo;
@@ -478,9 +484,9 @@ __global__ void k_field_in(Common cm, double* dst, const double* src, int restar
       if (i < I.nx && j < I.ny) {
         const long long K = I.base + (long long)j * I.pitch + i;
         const double v = tile[j - j0][i - i0];
-        if (restart && __double_as_longlong(A::to_d(A::ld(dst, K))) == __double_as_longlong(v)) continue;
+        if (restart && __double_as_longlong(A::to_d_io(A::ld(dst, K))) == __double_as_longlong(v)) continue;
         changed = 1;
-        A::st(dst, K, A::from_d(v));
+        A::st(dst, K, A::from_d_io(v));
       }
     }
     if (__syncthreads_or(restart && changed) && threadIdx.x == 0) cm.st[b].nhist = 0;
@@ -501,7 +507,7 @@ __global__ void k_field_out(Common cm, double* dst, const double* src, int t0, i
     const int lt = t - I.tile0, i0 = (lt % I.ntx) * kTX, j0 = (lt / I.ntx) * kTY;
     for (int q = threadIdx.x; q < kTX * kTY; q += blockDim.x) {
       const int i = i0 + (q % kTX), j = j0 + (q / kTX);  // i fastest
-      if (i < I.nx && j < I.ny) tile[j - j0][i - i0] = A::to_d(A::ld(src, I.base + (long long)j * I.pitch + i));
+      if (i < I.nx && j < I.ny) tile[j - j0][i - i0] = A::to_d_io(A::ld(src, I.base + (long long)j * I.pitch + i));
     }
     __syncthreads();
     for (int q = threadIdx.x; q < kTX * kTY; q += blockDim.x) {

@@ -31,3 +31,19 @@ def test_dword_error_bounds(tmp_path):
     assert set(worst) == set(BOUNDS)
     for k, b in BOUNDS.items():
         assert worst[k] <= b, (k, worst[k], b)
+
+
+def test_integer_conversions_match_the_fp64_ones(tmp_path):
+    """dw_from_double_int / dw_to_double_int (the layout transforms' conversions) give the bits of
+    dw_from_double / dw_to_double on every binary exponent of the double range, on rounding ties
+    with carries into the exponent, on special values and on arbitrary float pairs."""
+    cxx = shutil.which("g++")
+    cuda_inc = "/usr/local/cuda/include"
+    if not cxx or not os.path.isdir(cuda_inc):
+        pytest.skip("g++ or the CUDA headers are missing")
+    exe = str(tmp_path / "convert_check")
+    subprocess.run([cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-I", CSRC, "-I", cuda_inc,
+                    os.path.join(HERE, "dword", "convert_check.cc"), "-o", exe], check=True)
+    out = subprocess.run([exe], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout
+    assert "from_double_mismatches 0 to_double_mismatches 0" in out.stdout
