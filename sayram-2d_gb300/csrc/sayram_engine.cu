@@ -1105,9 +1105,9 @@ int sayram_batch_step_host(sayram_batch b, int nsteps, const double* f_in, doubl
   auto field_in = [&](const Piece& pc) {
     b->launch("field_in", [&] {
       if (b->dwm)
-        sg::k_field_in<sg::DWA><<<gt, 256, 0, b->stream>>>(b->cm, b->fl.f, b->d_stage, 1, pc.t0, pc.t1);
+        sg::k_field_in<sg::DWA><<<gt, sg::kFieldThreads, 0, b->stream>>>(b->cm, b->fl.f, b->d_stage, 1, pc.t0, pc.t1);
       else
-        sg::k_field_in<sg::F64A><<<gt, 256, 0, b->stream>>>(b->cm, b->fl.f, b->d_stage, 1, pc.t0, pc.t1);
+        sg::k_field_in<sg::F64A><<<gt, sg::kFieldThreads, 0, b->stream>>>(b->cm, b->fl.f, b->d_stage, 1, pc.t0, pc.t1);
     });
   };
   auto field_out = [&](const Piece& pc) {
@@ -2135,7 +2135,7 @@ extern "C" int sayram_step_noalloc(const sayram_problem* pd, const sayram_option
   SG_CUDA(cudaGetLastError());
   const int gt = std::max(1, std::min(cm.ntiles, nsm * kAsmGridPerSm));
   const int gs = std::max(1, std::min(cm.nchunks, nsm * 16));
-  k_field_in<F64A><<<gt, 256, 0, stream>>>(cm, fl.f, f_in, 0, 0, -1);
+  k_field_in<F64A><<<gt, kFieldThreads, 0, stream>>>(cm, fl.f, f_in, 0, 0, -1);
   const size_t smem_na = (size_t)(kNoAllocChunk + 2 * pitch) * sizeof(double);
   SG_CUDA(cudaFuncSetAttribute(k_bicg1<double, kNoAllocChunk>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_na));
   SG_CUDA(cudaFuncSetAttribute(k_bicg2<double, kNoAllocChunk>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_na));

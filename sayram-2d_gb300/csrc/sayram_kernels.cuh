@@ -31,6 +31,7 @@ constexpr int kTX = 32;        // assembly tile width (alpha0, contiguous)
 constexpr int kTY = 16;        // assembly tile height (log E)
 constexpr int kAsmThreads = 256;
 constexpr int kAsmGridPerSm = 96;  // k_assemble blocks launched per SM (grid-stride over tiles)
+constexpr int kFieldThreads = 256;  // threads per block of the layout transforms
 constexpr double kEps = DBL_EPSILON;  // gEPS, source/common.h:38
 
 enum { XMIN = 0, XMAX = 1, YMIN = 2, YMAX = 3 };

@@ -464,8 +464,12 @@ __global__ void k_dtable(Common cm, Geo geo, DTab t, const double* xe, const dou
 // an instance with any other cell loses its history of earlier states (the extrapolated start
 // restarts from the new state). An instance given back its own state is left exactly as it was.
 template <typename A>
-__global__ void k_field_in(Common cm, double* dst, const double* src, int restart, int t0, int t1) {
+__global__ void __launch_bounds__(kFieldThreads) k_field_in(Common cm, double* dst, const double* src, int restart,
+                                                             int t0, int t1) {
+  using V = typename A::V;
   count_launch(cm.ctl);
+  constexpr int kItems = kTX * kTY / kFieldThreads;
+  static_assert(kItems * kFieldThreads == kTX * kTY, "a tile splits evenly over the block");
   __shared__ double tile[kTY][kTX + 1];
   if (t1 < 0) t1 = n_tiles(cm);
   for (int t = t0 + blockIdx.x; t < t1; t += gridDim.x) {
@@ -473,20 +477,32 @@ __global__ void k_field_in(Common cm, double* dst, const double* src, int restar
     const InstDev I = cm.inst[b];
     if (!I.enabled) continue;
     const int lt = t - I.tile0, i0 = (lt % I.ntx) * kTX, j0 = (lt / I.ntx) * kTY;
-    for (int q = threadIdx.x; q < kTX * kTY; q += blockDim.x) {
+    // the stored values of this thread's cells of the second pass, loaded ahead of the barrier so
+    // that their latency overlaps the host-order loads
+    V old[kItems] = {};
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+      const int q = threadIdx.x + k * kFieldThreads;
+      const int i = i0 + (q % kTX), j = j0 + (q / kTX);  // i fastest
+      if (restart && i < I.nx && j < I.ny) old[k] = A::ld(dst, I.base + (long long)j * I.pitch + i);
+    }
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+      const int q = threadIdx.x + k * kFieldThreads;
       const int i = i0 + (q / kTY), j = j0 + (q % kTY);  // j fastest
       if (i < I.nx && j < I.ny) tile[j - j0][i - i0] = src[I.hoff + (long long)i * I.ny + j];
     }
     __syncthreads();
     int changed = 0;
-    for (int q = threadIdx.x; q < kTX * kTY; q += blockDim.x) {
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+      const int q = threadIdx.x + k * kFieldThreads;
       const int i = i0 + (q % kTX), j = j0 + (q / kTX);  // i fastest
       if (i < I.nx && j < I.ny) {
-        const long long K = I.base + (long long)j * I.pitch + i;
         const double v = tile[j - j0][i - i0];
-        if (restart && __double_as_longlong(A::to_d_io(A::ld(dst, K))) == __double_as_longlong(v)) continue;
+        if (restart && __double_as_longlong(A::to_d_io(old[k])) == __double_as_longlong(v)) continue;
         changed = 1;
-        A::st(dst, K, A::from_d_io(v));
+        A::st(dst, I.base + (long long)j * I.pitch + i, A::from_d_io(v));
       }
     }
     if (__syncthreads_or(restart && changed) && threadIdx.x == 0) cm.st[b].nhist = 0;
