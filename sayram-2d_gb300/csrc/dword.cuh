@@ -105,6 +105,12 @@ SG_HD dw dw_fma(dw x, dw y, dw z) {
   return fast2sum(s.hi, w);
 }
 
+// dw_fma(x, y, 0) without the operations on the zero addend (the same value)
+SG_HD dw dw_fma0(dw x, dw y) {
+  const dw p = two_prod(x.hi, y.hi);
+  return fast2sum(p.hi, DW_FMA(x.hi, y.lo, DW_FMA(x.lo, y.hi, p.lo)));
+}
+
 // x*y + z*w: both high-part products exact (Fast2Mult), their low parts and the cross terms
 // folded by FMA, one 2Sum of the high parts and one renormalisation -- 19 FP32 operations
 // against 24 for dw_fma(x, y, dw_mul(z, w)). Error within ~6u^2 (|x y| + |z w|) (the lo*lo terms,

@@ -127,6 +127,7 @@ struct F64A {
   // a*x + b*y and a*x - b*y (the same expression trees as fma(a, x, mul(b, y)) and
   // sub(mul(a, x), mul(b, y)))
   __device__ static V dot2(V a, V x, V b, V y) { return a * x + b * y; }
+  __device__ static V fma0(V a, V b) { return a * b; }  // fma(a, b, 0)
   __device__ static V dot2s(V a, V x, V b, V y) { return a * x - b * y; }
   // sums whose terms all have the same sign (cheaper in double-word form)
   __device__ static V addp(V a, V b) { return a + b; }
@@ -221,6 +222,7 @@ struct DWA {
   __device__ static V mul(V a, V b) { return dw_mul(a, b); }
   __device__ static V fma(V a, V b, V c) { return dw_fma(a, b, c); }
   __device__ static V dot2(V a, V x, V b, V y) { return dw_dot2(a, x, b, y); }
+  __device__ static V fma0(V a, V b) { return dw_fma0(a, b); }  // fma(a, b, 0)
   __device__ static V dot2s(V a, V x, V b, V y) { return dw_dot2(a, x, dw_neg(b), y); }
   __device__ static V addp(V a, V b) { return dw_add_same(a, b); }
   __device__ static V fmap(V a, V b, V c) { return dw_fma(a, b, c); }
@@ -802,25 +804,27 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
       const int K = base + j * P + i;
       const V Aw = xR[cy][cx], Ae = xL[cy][cx + 1], As = yT[cy][cx], An = yB[cy + 1][cx];
       const bool wIn = i > 0, eIn = i < nx - 1, sIn = j > 0, nIn = j < ny - 1;
-      V D = zero, Rv = zero, dir = zero;
-      // every term below is >= 0
-      if (wIn) D = A::addp(D, Aw);
+      // every term below is >= 0; a sum that is still zero takes its first term as it is (0 + x
+      // = x), which spares an interior cell three double-word additions
+      V D = wIn ? Aw : zero, Rv = zero, dir = zero;
+      bool has_dir = false;
       if (eIn) D = A::addp(D, Ae);
       if (sIn) D = A::addp(D, As);
       if (nIn) D = A::addp(D, An);
-      if (!wIn && I.bc[XMIN] == DIRICHLET) { D = A::addp(D, Aw); dir = A::addp(dir, Aw); Rv = A::addp(Rv, xL[cy][cx]); }
-      if (!eIn && I.bc[XMAX] == DIRICHLET) { D = A::addp(D, Ae); dir = A::addp(dir, Ae); Rv = A::addp(Rv, xR[cy][cx + 1]); }
-      if (!sIn && I.bc[YMIN] == DIRICHLET) { D = A::addp(D, As); dir = A::addp(dir, As); Rv = A::addp(Rv, yB[cy][cx]); }
-      if (!nIn && I.bc[YMAX] == DIRICHLET) { D = A::addp(D, An); dir = A::addp(dir, An); Rv = A::addp(Rv, yT[cy + 1][cx]); }
+      if (!wIn && I.bc[XMIN] == DIRICHLET) { D = A::addp(D, Aw); dir = A::addp(dir, Aw); Rv = A::addp(Rv, xL[cy][cx]); has_dir = true; }
+      if (!eIn && I.bc[XMAX] == DIRICHLET) { D = A::addp(D, Ae); dir = A::addp(dir, Ae); Rv = A::addp(Rv, xR[cy][cx + 1]); has_dir = true; }
+      if (!sIn && I.bc[YMIN] == DIRICHLET) { D = A::addp(D, As); dir = A::addp(dir, As); Rv = A::addp(Rv, yB[cy][cx]); has_dir = true; }
+      if (!nIn && I.bc[YMAX] == DIRICHLET) { D = A::addp(D, An); dir = A::addp(dir, An); Rv = A::addp(Rv, yT[cy + 1][cx]); has_dir = true; }
       const V sd = A::ld(geo.sdiag, K);
       D = A::addp(D, sd);
       const V fK = fS[cy + 1][cx + 1];
-      Rv = A::fmap(A::ld(geo.ukk, K), fK, Rv);
+      const V ukk = A::ld(geo.ukk, K);
+      Rv = has_dir ? A::fmap(ukk, fK, Rv) : A::fma0(ukk, fK);
       rmax = fmaxf(rmax, fabsf(A::f32(Rv)));
       const V inv = A::rcp(D);
       A::st(fl.invD, K, inv);
       A::st(fl.R, K, Rv);
-      A::st(fl.colsum, K, A::addp(sd, dir));
+      A::st(fl.colsum, K, has_dir ? A::addp(sd, dir) : sd);
       // start the solve from D g, g the loss-compensated polynomial extrapolation in time the
       // last polish formed (only the starting point of the iteration; the converged answer does
       // not depend on it)
