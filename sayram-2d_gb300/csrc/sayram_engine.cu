@@ -51,6 +51,7 @@ struct sayram_batch_s {
   int nsm = 0;
   cudaStream_t stream = nullptr;
   cudaStream_t cstream = nullptr;           // host copies of sayram_batch_step_host, in pieces
+  cudaStream_t tstream = nullptr;           // its layout transforms in, beside the assembly of earlier pieces
   std::vector<cudaEvent_t> piece_ev;        // one per piece and direction
   int n = 0;
   std::vector<InstDev> hinst;
@@ -129,6 +130,8 @@ struct sayram_batch_s {
     piece_ev.clear();
     if (cstream) cudaStreamDestroy(cstream);
     cstream = nullptr;
+    if (tstream) cudaStreamDestroy(tstream);
+    tstream = nullptr;
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
   }
@@ -387,6 +390,7 @@ int sayram_batch_s::init_device() {
   SG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   SG_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   SG_CUDA(cudaStreamCreateWithFlags(&cstream, cudaStreamNonBlocking));
+  SG_CUDA(cudaStreamCreateWithFlags(&tstream, cudaStreamNonBlocking));
   return SAYRAM_OK;
 }
 
@@ -1096,18 +1100,18 @@ int sayram_batch_step_host(sayram_batch b, int nsteps, const double* f_in, doubl
     }
   }
   const size_t np = pieces.size();
-  while (b->piece_ev.size() < 2 * np) {
+  while (b->piece_ev.size() < 3 * np + 1) {
     cudaEvent_t e;
     SG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     b->piece_ev.push_back(e);
   }
   const int gt = b->grid_tiles();
-  auto field_in = [&](const Piece& pc) {
+  auto field_in = [&](const Piece& pc, cudaStream_t s) {
     b->launch("field_in", [&] {
       if (b->dwm)
-        sg::k_field_in<sg::DWA><<<gt, sg::kFieldThreads, 0, b->stream>>>(b->cm, b->fl.f, b->d_stage, 1, pc.t0, pc.t1);
+        sg::k_field_in<sg::DWA><<<gt, sg::kFieldThreads, 0, s>>>(b->cm, b->fl.f, b->d_stage, 1, pc.t0, pc.t1);
       else
-        sg::k_field_in<sg::F64A><<<gt, sg::kFieldThreads, 0, b->stream>>>(b->cm, b->fl.f, b->d_stage, 1, pc.t0, pc.t1);
+        sg::k_field_in<sg::F64A><<<gt, sg::kFieldThreads, 0, s>>>(b->cm, b->fl.f, b->d_stage, 1, pc.t0, pc.t1);
     });
   };
   auto field_out = [&](const Piece& pc) {
@@ -1150,13 +1154,23 @@ int sayram_batch_step_host(sayram_batch b, int nsteps, const double* f_in, doubl
         if ((rc = b->launch_steps(1))) return rc;
         continue;
       }
+      if (head) {
+        // the transforms run on their own stream, so that piece k+1's transform overlaps piece
+        // k's assembly (different instances); it starts after everything queued so far
+        SG_CUDA(cudaEventRecord(b->piece_ev[3 * np], b->stream));
+        SG_CUDA(cudaStreamWaitEvent(b->tstream, b->piece_ev[3 * np], 0));
+      }
       if ((rc = b->launch_begin())) return rc;
       if (head) {
         for (size_t k = 0; k < np; ++k)
           if ((rc = copy_in(k))) return rc;
         for (size_t k = 0; k < np; ++k) {
-          SG_CUDA(cudaStreamWaitEvent(b->stream, b->piece_ev[k], 0));
-          field_in(pieces[k]);
+          SG_CUDA(cudaStreamWaitEvent(b->tstream, b->piece_ev[k], 0));
+          field_in(pieces[k], b->tstream);
+          SG_CUDA(cudaEventRecord(b->piece_ev[2 * np + k], b->tstream));
+        }
+        for (size_t k = 0; k < np; ++k) {
+          SG_CUDA(cudaStreamWaitEvent(b->stream, b->piece_ev[2 * np + k], 0));
           if ((rc = b->launch_assemble(pieces[k].t0, pieces[k].t1))) return rc;
         }
       } else if ((rc = b->launch_assemble(0, -1))) {
@@ -1181,7 +1195,7 @@ int sayram_batch_step_host(sayram_batch b, int nsteps, const double* f_in, doubl
     for (size_t k = 0; k < np; ++k) {
       if ((rc = copy_in(k))) return rc;
       SG_CUDA(cudaStreamWaitEvent(b->stream, b->piece_ev[k], 0));
-      field_in(pieces[k]);
+      field_in(pieces[k], b->stream);
     }
   }
   rc = b->run_steps(nsteps);
