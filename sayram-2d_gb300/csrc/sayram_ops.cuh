@@ -637,9 +637,10 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
   // arrays' storage, which step 3 fills after a barrier)
   static_assert(HY * VX <= 2 * kTY * VX, "row interpolations must fit in the x-face arrays");
   V(*const rS)[VX] = reinterpret_cast<V(*)[VX]>(&xLR[0][0][0]);
-  // step 1's thread layout: kRowT threads own one vertex column each and walk its halo rows
-  constexpr int kRowT = VX * 7;
-  static_assert(kRowT < kAsmThreads && 3 * 7 >= HY, "step 1 layout");
+  // step 1's thread layout: kRowT threads own one vertex column each and walk its halo rows,
+  // kRowS rows apart
+  constexpr int kRowS = 7, kRowT = VX * kRowS;
+  static_assert(kRowT < kAsmThreads && 3 * kRowS >= HY, "step 1 layout");
   const V zero = A::k(0.0);
   const int nt_ = t1 < 0 ? n_tiles(cm) : t1;
   for (int t = t0 + blockIdx.x; t < nt_; t += gridDim.x) {
@@ -677,7 +678,7 @@ __global__ void __launch_bounds__(kAsmThreads, A::kAsmBlocks) k_assemble(Common 
       const bool xin = Iv > 0 && Iv < nx;
       const V wL = xin ? A::ld(cm.wx, 2 * (I.xe + Iv)) : zero;
       const V wR = xin ? A::ld(cm.wx, 2 * (I.xe + Iv) + 1) : zero;
-      for (int hy = threadIdx.x / VX; hy < HY; hy += 7) {
+      for (int hy = threadIdx.x / VX; hy < HY; hy += kRowS) {
         const int j = j0 + hy - 1;
         V fa = zero, ia = zero, r = zero;
         if (j >= 0 && j < ny && Iv <= nx) {
