@@ -170,6 +170,8 @@ int sayram_set_dtable(sayram_solver s, const sayram_dtable* t);
 /* ---- batches: many independent instances advanced by the same launches ------------------- */
 typedef struct sayram_batch_s* sayram_batch;
 
+/* A batch holds fewer than 2^31 - 1 padded cells (SAYRAM_ERR_ARG otherwise): the assembly
+ * indexes cells with 32-bit integers, and that many cells would need ~330 GB of device memory. */
 int sayram_batch_create(const sayram_problem* probs, int n, const sayram_options* opt,
                         sayram_batch* out);
 int sayram_batch_size(sayram_batch b);
