@@ -160,6 +160,38 @@ def test_step_host_roundtrip(capi, prec):
     c.close()
 
 
+def test_layout_transforms_round_like_the_host(capi):
+    """The host-buffer step's layout transforms convert double <-> double word with integer
+    rounding on the device (dw_from_double_int / dw_to_double_int). A zero-step call round-trips
+    a state through both; every value must come back as float64(hi) + float64(lo) with
+    hi = float32(v), lo = float32(v - hi), the separately rounded IEEE conversions, bit for bit:
+    over 600 decades, signed zeros, float32 subnormals and boundaries, and rounding ties."""
+    probs = cases.batch_problems(3, seed=5, dt=1e-2, lo=30, hi=70)
+    b = capi.Batch(probs, precision=2)
+    n = sum(p.nx * p.ny for p in probs)
+    rng = np.random.default_rng(11)
+    v = rng.choice([-1.0, 1.0], n) * 10.0 ** rng.uniform(-300, 38, n)
+    h = rng.uniform(0.5, 1.0, n).astype(np.float32).astype(np.float64)
+    k = np.arange(n)
+    # ties of the 24-bit rounding: a float32 value in [0.5, 1) plus exactly half its last place
+    v[k % 7 == 1] = (h + 2.0 ** -25)[k % 7 == 1] * 2.0 ** rng.integers(-120, 120, n)[k % 7 == 1]
+    v[k % 7 == 2] = np.float64(np.float32(1.1754943508222875e-38)) * rng.uniform(0.5, 2.0, n)[k % 7 == 2]
+    v[k % 7 == 3] = 1.401298464324817e-45 * rng.uniform(0.0, 4.0, n)[k % 7 == 3]
+    v[k % 97 == 4] = 0.0
+    v[k % 97 == 5] = -0.0
+    v[k % 97 == 6] = 3.4028234663852886e38
+    fin = np.ascontiguousarray(v)
+    fout = np.empty_like(fin)
+    b.step_host(0, fin.ctypes.data, fout.ctypes.data)
+    with np.errstate(over="ignore", under="ignore", invalid="ignore"):
+        hi = fin.astype(np.float32)
+        lo = (fin - hi.astype(np.float64)).astype(np.float32)
+        want = hi.astype(np.float64) + lo.astype(np.float64)
+    bad = np.flatnonzero(fout.view(np.uint64) != want.view(np.uint64))
+    assert bad.size == 0, (bad.size, fin[bad[:3]], fout[bad[:3]], want[bad[:3]])
+    b.close()
+
+
 @pytest.mark.parametrize("prec", [0, 2])
 def test_step_host_forms_equal_device_stepping(capi, prec):
     """Every form of the host-buffer step (state in and out, in only, out only; one to five steps,
