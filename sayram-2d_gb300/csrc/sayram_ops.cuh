@@ -194,9 +194,9 @@ struct F64A {
 
 struct DWA {
   using V = dw;
-  // k_assemble: 6 resident blocks (40 registers, 12 bytes spilled); measured on the 4096-instance
-  // batch with 64 launched blocks per SM: 4 blocks 5.72 ms, 5 blocks (48 registers, no spill)
-  // 5.27 ms, 6 blocks 5.16 ms per launch (with 96 launched per SM: 5.09 ms)
+  // k_assemble: 6 resident blocks (40 registers, no spill); measured on the 4096-instance batch
+  // with 64 launched blocks per SM: 4 blocks 5.72 ms, 5 blocks (48 registers) 5.27 ms, 6 blocks
+  // 5.16 ms per launch (with 96 launched per SM: 5.09 ms)
   static constexpr int kAsmBlocks = 6;
   template <typename Ix>
   __device__ static V ld(const double* p, Ix i) {
