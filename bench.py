@@ -371,7 +371,11 @@ def kernel_roofline(b, probs, peak, steps=2, model=None):
             "bicg1": (cells * it).sum(), "bicg2": (cells * it).sum(), "bicg3": (cells * it).sum()}
     out = {}
     for name, (ms, n) in kt.items():
-        if name in model and n > 0:
+        if name == "solve_coop" and n > 0:  # the refinement loop as one cooperative kernel
+            byts = sum(model[k] * proc[k] for k in ("resid", "bicg1", "bicg2", "bicg3"))
+            out[name] = {"ms": ms, "launches": int(n), "bytes": byts, "GBps": byts / (ms * 1e-3) / 1e9,
+                         "share": 0.0}
+        elif name in model and n > 0:
             byts = model[name] * proc[name]
             out[name] = {"ms": ms, "launches": int(n), "bytes": byts, "GBps": byts / (ms * 1e-3) / 1e9,
                          "share": 0.0}

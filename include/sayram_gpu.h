@@ -222,6 +222,11 @@ int sayram_batch_kernel_times(sayram_batch b, const char** names, double* total_
  * fastest. The instances' state is restored afterwards, so tuning does not advance the
  * simulation. Writes the choice if the pointers are not NULL. */
 int sayram_batch_autotune(sayram_batch b, int steps, int* chunk_out, int* blocks_per_sm_out);
+/* The refinement loop of a step runs as one cooperative kernel (grid-wide barriers between its
+ * passes) when every chunk of the batch gets a block in one wave of co-resident blocks -- a
+ * single large instance or a few -- and as the graph's loops of separate kernels otherwise.
+ * on = 0 always uses the separate kernels (the results are the same bit for bit). Default: 1. */
+int sayram_batch_set_coop(sayram_batch b, int on);
 /* Sets the launch shape directly (chunk 1024, 2048 or 4096 cells; 1..64 blocks per SM), or reads
  * it back. The default is chosen from the batch size; results do not depend on it beyond the
  * order of the reductions. */

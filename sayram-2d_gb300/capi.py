@@ -120,6 +120,7 @@ SIGNATURES = {
     "sayram_batch_set_dtable": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(sayram_dtable)]),
     "sayram_set_dtable": (ctypes.c_int, [_P, ctypes.POINTER(sayram_dtable)]),
     "sayram_batch_set_launch_shape": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),
+    "sayram_batch_set_coop": (ctypes.c_int, [_P, ctypes.c_int]),
     "sayram_batch_get_launch_shape": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
     "sayram_batch_tuning_log": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), _dp, ctypes.c_int]),
     "sayram_batch_launches": (ctypes.c_longlong, [_P]),
@@ -338,6 +339,11 @@ class Batch:
             raise ValueError("Daa, Dap, Dpp must have shape (len(alpha0_deg), len(E))")
         t = sayram_dtable(na, ne, *[_ptr(a) for a in keep])
         check(self._L.sayram_batch_set_dtable(self.h, int(idx), ctypes.byref(t)), "sayram_batch_set_dtable")
+
+    def set_coop(self, on: bool) -> None:
+        """Run each step's refinement loop as one cooperative kernel when the batch's chunks fit in
+        one wave of co-resident blocks (default), or always as the loops of separate kernels."""
+        check(self._L.sayram_batch_set_coop(self.h, 1 if on else 0), "sayram_batch_set_coop")
 
     def set_launch_shape(self, chunk: int, blocks_per_sm: int) -> None:
         check(self._L.sayram_batch_set_launch_shape(self.h, int(chunk), int(blocks_per_sm)), "sayram_batch_set_launch_shape")

@@ -215,6 +215,58 @@ struct sayram_batch_s {
     SG_CUDA(cudaFuncSetAttribute(sg::k_bicg2<T, CH>, cudaFuncAttributeMaxDynamicSharedMemorySize, b1));
     SG_CUDA(cudaFuncSetAttribute(sg::k_resid<T, C, A, CH>, cudaFuncAttributeMaxDynamicSharedMemorySize, b2));
     SG_CUDA(cudaFuncSetAttribute(sg::k_polish<C, A, CH>, cudaFuncAttributeMaxDynamicSharedMemorySize, b2));
+    SG_CUDA(cudaFuncSetAttribute(sg::k_solve_coop<T, C, A, CH, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, b2));
+    SG_CUDA(cudaFuncSetAttribute(sg::k_solve_coop<T, C, A, CH, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, b2));
+    return SAYRAM_OK;
+  }
+  // The cooperative solve (k_solve_coop) replaces the graph's refinement loops when every chunk
+  // gets a block of its own in one wave of co-resident blocks (a fixed instance list; the server's
+  // lanes set coop = 0). Returns its grid (negative: the 4-blocks-per-SM form), or 0 when the
+  // loops of separate kernels are used.
+  int coop = 1;
+  template <typename T, typename C, typename A, int CH>
+  int coop_grid() {
+    if (!coop || nchunks < 1) return 0;
+    int can = 0;
+    if (cudaDeviceGetAttribute(&can, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !can) {
+      cudaGetLastError();
+      return 0;
+    }
+    int per_sm2 = 0, per_sm4 = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, sg::k_solve_coop<T, C, A, CH, 2>, sg::kThreads,
+                                                      smem_wide()) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm4, sg::k_solve_coop<T, C, A, CH, 4>, sg::kThreads,
+                                                      smem_wide()) != cudaSuccess) {
+      cudaGetLastError();
+      return 0;
+    }
+    if ((long long)nchunks <= (long long)per_sm2 * nsm) return nchunks;
+    if ((long long)nchunks <= (long long)per_sm4 * nsm) return -nchunks;
+    return 0;
+  }
+  template <typename T, typename C, typename A, int CH>
+  int launch_coop(int sgrid, const sg::Coef<C>& cfull, const sg::Coef<T>& ck, const sg::Kry<T>& kr) {
+    const int grid = sgrid < 0 ? -sgrid : sgrid;
+    sg::Common c2 = cm;
+    c2.use_cond = 2;
+    c2.guard_refine = opt.max_refine + 1;
+    c2.guard_iters = opt.max_iters + 1;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(sg::kThreads);
+    cfg.dynamicSmemBytes = smem_wide();
+    cfg.stream = stream;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    if (sgrid > 0)
+      SG_CUDA(cudaLaunchKernelEx(&cfg, sg::k_solve_coop<T, C, A, CH, 2>, c2, fl, cfull, ck, kr, opt.tol,
+                                 opt.inner_tol, opt.max_refine, opt.max_iters));
+    else
+      SG_CUDA(cudaLaunchKernelEx(&cfg, sg::k_solve_coop<T, C, A, CH, 4>, c2, fl, cfull, ck, kr, opt.tol,
+                                 opt.inner_tol, opt.max_refine, opt.max_iters));
     return SAYRAM_OK;
   }
   // dispatch of the per-step sequence on precision and chunk size (graph: build it; else: run it)
@@ -667,7 +719,18 @@ int sayram_batch_s::step_once(const sg::Coef<C>& cfull, const sg::Coef<T>& ck, c
   SG_CUDA(cudaMemsetAsync(d_ctl, 0, 2 * sizeof(int), stream));
   launch("begin", [&] { k_begin<<<(n + 255) / 256, 256, 0, stream>>>(cm); });
   launch("assemble", [&] { k_assemble<C, A><<<gt, kAsmThreads, 0, stream>>>(cm, geo, fl, cfull, 0, -1); });
-  for (int o = 0; o < opt.max_refine; ++o) {
+  int cgrid = coop_grid<T, C, A, CH>();
+  if (cgrid != 0) {
+    int crc = SAYRAM_OK;
+    launch("solve_coop", [&] { crc = launch_coop<T, C, A, CH>(cgrid, cfull, ck, kr); });
+    if (crc) {  // refused: the loops of separate kernels from now on
+      cudaGetLastError();
+      g_err.clear();
+      coop = 0;
+      cgrid = 0;
+    }
+  }
+  for (int o = 0; cgrid == 0 && o < opt.max_refine; ++o) {
     launch("resid", [&] {
       k_resid<T, C, A, CH><<<gs, kThreads, smem_wide(), stream>>>(cm, fl, cfull, kr, opt.tol, opt.inner_tol, opt.max_refine);
     });
@@ -728,6 +791,40 @@ int sayram_batch_s::build_graph(const sg::Coef<C>& cfull, const sg::Coef<T>& ck,
   cudaGraph_t g = nullptr;
   SG_CUDA(cudaGraphCreate(&g, 0));
   (prefix ? graph : graph_solve) = g;
+  int rc;
+  const int cgrid = coop_grid<T, C, A, CH>();
+  if (cgrid != 0) {
+    // [memset, begin, assemble,] the cooperative solve[, polish]
+    SG_CUDA(cudaStreamBeginCaptureToGraph(stream, g, nullptr, nullptr, 0, mode));
+    if (prefix) {
+      cudaMemsetAsync(d_ctl, 0, 2 * sizeof(int), stream);
+      k_begin<<<(n + 255) / 256, 256, 0, stream>>>(cm);
+      k_assemble<C, A><<<gt, kAsmThreads, 0, stream>>>(cm, geo, fl, cfull, 0, -1);
+    }
+    // a capture that refuses the cooperative launch or does not keep it cooperative falls back
+    // to the loops of separate kernels
+    bool coop_node = launch_coop<T, C, A, CH>(cgrid, cfull, ck, kr) == SAYRAM_OK;
+    cudaGraphNode_t cnode = nullptr;
+    if (coop_node) coop_node = last_captured(&cnode) == SAYRAM_OK;
+    if (coop_node) {
+      cudaLaunchAttributeValue cv = {};
+      coop_node = cudaGraphKernelNodeGetAttribute(cnode, cudaLaunchAttributeCooperative, &cv) == cudaSuccess &&
+                  cv.cooperative;
+    }
+    if (coop_node && prefix) k_polish<C, A, CH><<<gs, kThreads, smem_wide(), stream>>>(cm, fl, cfull, 0, -1);
+    cudaGraph_t gc = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(stream, &gc);
+    if (!coop_node || ce != cudaSuccess) {
+      cudaGetLastError();
+      g_err.clear();
+      cudaGraphDestroy(g);
+      (prefix ? graph : graph_solve) = nullptr;
+      coop = 0;
+      return build_graph<T, C, A, CH>(cfull, ck, kr, prefix);
+    }
+    SG_CUDA(cudaGraphInstantiate(prefix ? &gexec : &gexec_solve, g, 0));
+    return SAYRAM_OK;
+  }
   cudaGraphConditionalHandle hout, hin;
   SG_CUDA(cudaGraphConditionalHandleCreate(&hout, g, 1, cudaGraphCondAssignDefault));
   Common c2 = cm;
@@ -735,7 +832,6 @@ int sayram_batch_s::build_graph(const sg::Coef<C>& cfull, const sg::Coef<T>& ck,
   c2.h_outer = hout;
   c2.guard_refine = opt.max_refine + 1;
   c2.guard_iters = opt.max_iters + 1;
-  int rc;
   // prefix
   cudaGraphNode_t pre = nullptr;
   if (prefix) {
@@ -1397,6 +1493,15 @@ int sayram_batch_set_dtable(sayram_batch b, int idx, const sayram_dtable* t) {
 
 int sayram_set_dtable(sayram_solver s, const sayram_dtable* t) { return sayram_batch_set_dtable(s, 0, t); }
 
+int sayram_batch_set_coop(sayram_batch b, int on) {
+  if (!b) return fail(SAYRAM_ERR_ARG, "null handle");
+  SG_CUDA(cudaSetDevice(b->dev));
+  SG_CUDA(cudaStreamSynchronize(b->stream));
+  b->coop = on ? 1 : 0;
+  b->drop_graph();
+  return SAYRAM_OK;
+}
+
 int sayram_batch_set_launch_shape(sayram_batch b, int chunk, int blocks_per_sm) {
   if (!b) return fail(SAYRAM_ERR_ARG, "null handle");
   if (chunk != 1024 && chunk != 2048 && chunk != 4096) return fail(SAYRAM_ERR_ARG, "chunk must be 1024, 2048 or 4096");
@@ -1728,6 +1833,9 @@ struct ServerLane {
   int create(const sayram_server_config& c, const sayram_options* opt) {
     cfg = c;
     sayram_batch_s& e = eng;
+    // the lane's step graph outlives changes of its instance list; the cooperative solve's grid
+    // is sized to the list it was built for
+    e.coop = 0;
     int rc = e.set_options(opt);
     if (!rc) rc = e.init_device();
     if (rc) return rc;

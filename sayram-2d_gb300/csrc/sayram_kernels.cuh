@@ -76,6 +76,7 @@ struct Ctl {
   unsigned int kdone[8];        // blocks finished per kernel (graph-conditional updates)
   unsigned int outer_loops;     // residual evaluations run by the device-side loop this step
   unsigned int inner_loops;     // Krylov iterations run by the device-side loop this solve
+  int go_outer, go_inner;       // the loop decisions of the cooperative solve (k_solve_coop)
 };
 
 template <typename T>

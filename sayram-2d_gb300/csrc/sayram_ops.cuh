@@ -16,6 +16,8 @@
 // values) hold 8 bytes per entry in both: one double, or one (hi, lo) float pair.
 #pragma once
 
+#include <cooperative_groups.h>
+
 #include "dword.cuh"
 #include "sayram_kernels.cuh"
 
@@ -45,7 +47,8 @@ struct Common {
   // steps, as in the server) instead of the by-value counts above
   const int* dyn;
   int pmax;  // largest row pitch of any instance (shared-memory halo of the SpMV kernels)
-  // device-side loops of the per-step CUDA graph (use_cond = 0: the host drives the loops)
+  // device-side loops of the per-step CUDA graph (use_cond = 0: the host drives the loops; 1: the
+  // graph's WHILE nodes; 2: the cooperative solve kernel)
   unsigned long long h_outer, h_inner;  // cudaGraphConditionalHandle of the two WHILE nodes
   int use_cond;
   int guard_refine, guard_iters;  // hard caps on loop trips, whatever the bookkeeping says
@@ -71,14 +74,22 @@ __device__ __forceinline__ void loop_epilogue(const Common& cm, int which) {
       __threadfence();
       const int nout = atomicAdd(&cm.ctl->n_outer, 0);
       const int nin = atomicAdd(&cm.ctl->n_inner, 0);
+      unsigned go_o = 0u, go_i;
       if (which == 0) {
         const unsigned lo = atomicAdd(&cm.ctl->outer_loops, 1u) + 1u;
         atomicExch(&cm.ctl->inner_loops, 0u);
-        cudaGraphSetConditional(cm.h_outer, (nout > 0 && lo < (unsigned)cm.guard_refine) ? 1u : 0u);
-        cudaGraphSetConditional(cm.h_inner, (nin > 0 && lo < (unsigned)cm.guard_refine) ? 1u : 0u);
+        go_o = (nout > 0 && lo < (unsigned)cm.guard_refine) ? 1u : 0u;
+        go_i = (nin > 0 && lo < (unsigned)cm.guard_refine) ? 1u : 0u;
       } else {
         const unsigned li = atomicAdd(&cm.ctl->inner_loops, 1u) + 1u;
-        cudaGraphSetConditional(cm.h_inner, (nin > 0 && li < (unsigned)cm.guard_iters) ? 1u : 0u);
+        go_i = (nin > 0 && li < (unsigned)cm.guard_iters) ? 1u : 0u;
+      }
+      if (cm.use_cond == 1) {
+        if (which == 0) cudaGraphSetConditional(cm.h_outer, go_o);
+        cudaGraphSetConditional(cm.h_inner, go_i);
+      } else {  // read by every block of the cooperative solve after its next grid barrier
+        if (which == 0) atomicExch(&cm.ctl->go_outer, (int)go_o);
+        atomicExch(&cm.ctl->go_inner, (int)go_i);
       }
       atomicExch(&cm.ctl->kdone[which], 0u);
     }
@@ -557,6 +568,8 @@ __global__ void k_begin(Common cm) {
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     cm.ctl->outer_loops = 0u;
     cm.ctl->inner_loops = 0u;
+    cm.ctl->kdone[0] = 0u;
+    cm.ctl->kdone[1] = 0u;
   }
 }
 
@@ -1025,10 +1038,9 @@ __device__ __forceinline__ Q4<typename A::V> stencilW(const Q4<typename A::V>& c
 // r = R - A~ (y + x) in the wide arithmetic; writes y + x to the other y buffer and the Krylov's
 // right-hand side B^-1 r (T precision, scaled). Partials: ||r||^2, ||R||^2, ||B^-1 r||^2.
 template <typename T, typename C, typename A, int CH>
-__global__ void __launch_bounds__(kThreads, 4) k_resid(Common cm, Fields fl, Coef<C> co, Kry<T> kr,
-                                                        double tol, double inner_tol, int max_refine) {
+__device__ __forceinline__ void resid_body(Common cm, Fields fl, Coef<C> co, Kry<T> kr, double tol, double inner_tol,
+                                           int max_refine) {
   using V = typename A::V;
-  count_launch(cm.ctl);
   extern __shared__ __align__(16) unsigned char smraw[];
   V* sm = reinterpret_cast<V*>(smraw);
   for_active_chunks(cm, [&](int b_) { return cm.st[b_].outer_active != 0; }, [&](int c) {
@@ -1126,6 +1138,12 @@ __global__ void __launch_bounds__(kThreads, 4) k_resid(Common cm, Fields fl, Coe
       }
     }
   });
+}
+template <typename T, typename C, typename A, int CH>
+__global__ void __launch_bounds__(kThreads, 4) k_resid(Common cm, Fields fl, Coef<C> co, Kry<T> kr,
+                                                        double tol, double inner_tol, int max_refine) {
+  count_launch(cm.ctl);
+  resid_body<T, C, A, CH>(cm, fl, co, kr, tol, inner_tol, max_refine);
   loop_epilogue(cm, 0);
 }
 
@@ -1136,8 +1154,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_resid(Common cm, Fields fl, Coe
 //     v = B^-1 A~ p;  partial (r^, v). p is computed once per cell into shared memory (chunk plus
 //     one row above and below) and the stencil reads it there.
 template <typename T, int CH>
-__global__ void __launch_bounds__(kThreads, krylov_blocks<T>()) k_bicg1(Common cm, Coef<T> co, Kry<T> kr) {
-  count_launch(cm.ctl);
+__device__ __forceinline__ void bicg1_body(Common cm, Coef<T> co, Kry<T> kr) {
   extern __shared__ __align__(16) unsigned char smraw[];
   T* sm = reinterpret_cast<T*>(smraw);
   for_active_chunks(cm, [&](int b_) { return cm.st[b_].inner_active != 0; }, [&](int c) {
@@ -1207,11 +1224,15 @@ __global__ void __launch_bounds__(kThreads, krylov_blocks<T>()) k_bicg1(Common c
     }
   });
 }
+template <typename T, int CH>
+__global__ void __launch_bounds__(kThreads, krylov_blocks<T>()) k_bicg1(Common cm, Coef<T> co, Kry<T> kr) {
+  count_launch(cm.ctl);
+  bicg1_body<T, CH>(cm, co, kr);
+}
 
 // k2: s = r - alpha v;  t = B^-1 A~ s;  partials (t, s), (t, t). s is staged like p in k1.
 template <typename T, int CH>
-__global__ void __launch_bounds__(kThreads, krylov_blocks<T>()) k_bicg2(Common cm, Coef<T> co, Kry<T> kr) {
-  count_launch(cm.ctl);
+__device__ __forceinline__ void bicg2_body(Common cm, Coef<T> co, Kry<T> kr) {
   extern __shared__ __align__(16) unsigned char smraw[];
   T* sm = reinterpret_cast<T*>(smraw);
   for_active_chunks(cm, [&](int b_) { return cm.st[b_].inner_active != 0; }, [&](int c) {
@@ -1263,12 +1284,16 @@ __global__ void __launch_bounds__(kThreads, krylov_blocks<T>()) k_bicg2(Common c
     }
   });
 }
+template <typename T, int CH>
+__global__ void __launch_bounds__(kThreads, krylov_blocks<T>()) k_bicg2(Common cm, Coef<T> co, Kry<T> kr) {
+  count_launch(cm.ctl);
+  bicg2_body<T, CH>(cm, co, kr);
+}
 
 // k3: x += alpha p + omega s (x starts at 0 on the first iteration of a solve);
 //     r = s - omega t;  partials (r^, r), (r, r); convergence test.
 template <typename T, int CH>
-__global__ void __launch_bounds__(kThreads, krylov_blocks<T>()) k_bicg3(Common cm, Kry<T> kr, int max_iters) {
-  count_launch(cm.ctl);
+__device__ __forceinline__ void bicg3_body(Common cm, Kry<T> kr, int max_iters) {
   for_active_chunks(cm, [&](int b_) { return cm.st[b_].inner_active != 0; }, [&](int c) {
     const int b = cm.chunk_inst[c];
     InstState& st = cm.st[b];
@@ -1324,7 +1349,53 @@ __global__ void __launch_bounds__(kThreads, krylov_blocks<T>()) k_bicg3(Common c
       }
     }
   });
+}
+template <typename T, int CH>
+__global__ void __launch_bounds__(kThreads, krylov_blocks<T>()) k_bicg3(Common cm, Kry<T> kr, int max_iters) {
+  count_launch(cm.ctl);
+  bicg3_body<T, CH>(cm, kr, max_iters);
   loop_epilogue(cm, 1);
+}
+
+// The refinement loop of one step in one cooperative launch, for batches whose chunks fit in
+// one wave of co-resident blocks (one large instance: there the launch and ramp of each kernel
+// of the graph's loops cost more than its pass over the cells). The same chunk bodies as the
+// kernels above, separated by grid-wide barriers. The loop decisions are the graph's: the last
+// block of each deciding pass writes them (loop_epilogue, use_cond = 2) before the barrier,
+// every block reads them after it, and nothing rewrites them before every block has finished
+// the next pass -- so every block runs the same sequence of barriers, and the guards bound it.
+// Launch only cooperatively (cudaLaunchAttributeCooperative), with at most one block per chunk.
+// MINB resident blocks per SM: 2 (124 registers, no spill) when the chunks fit in 2 per SM,
+// else 4 (64 registers, some spilled); on one 1024 x 1024 instance in double-word mode the first
+// took 0.84 ms per step, the second 0.90, the separate kernels 0.98.
+template <typename T, typename C, typename A, int CH, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) k_solve_coop(Common cm, Fields fl, Coef<C> cfull, Coef<T> ck,
+                                                                Kry<T> kr, double tol, double inner_tol,
+                                                                int max_refine, int max_iters) {
+  count_launch(cm.ctl);
+  cooperative_groups::grid_group grid = cooperative_groups::this_grid();
+  const volatile int* go_outer = &cm.ctl->go_outer;
+  const volatile int* go_inner = &cm.ctl->go_inner;
+  // the trip counts are capped here as well (the same in every block), so the loops end even if
+  // the decisions were never written
+  for (int o = 0; o < cm.guard_refine; ++o) {
+    resid_body<T, C, A, CH>(cm, fl, cfull, kr, tol, inner_tol, max_refine);
+    loop_epilogue(cm, 0);
+    grid.sync();
+    const bool more = *go_outer != 0;
+    bool inner = *go_inner != 0;
+    for (int it = 0; inner && it < cm.guard_iters; ++it) {
+      bicg1_body<T, CH>(cm, ck, kr);
+      grid.sync();
+      bicg2_body<T, CH>(cm, ck, kr);
+      grid.sync();
+      bicg3_body<T, CH>(cm, kr, max_iters);
+      loop_epilogue(cm, 1);
+      grid.sync();
+      inner = *go_inner != 0;
+    }
+    if (!more) break;
+  }
 }
 
 // ------------------------------------------------------------------------------ polish + checks

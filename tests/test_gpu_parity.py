@@ -160,6 +160,32 @@ def test_step_host_roundtrip(capi, prec):
     c.close()
 
 
+@pytest.mark.parametrize("prec", [0, 2])
+def test_cooperative_solve_equals_separate_kernels(capi, prec):
+    """A batch whose chunks fit in one wave of co-resident blocks runs each step's refinement
+    loop as one cooperative kernel (grid-wide barriers between the passes); switched off, the
+    same loop runs as the graph's (or the host loop's) separate kernels. The states must agree
+    bit for bit, and the cooperative form must take far fewer launches."""
+    probs = [cases.synthetic_problem(200, 150, 1e-2, 3)] + cases.batch_problems(3, seed=4, dt=1e-2, lo=30, hi=90)
+    states, launches = {}, {}
+    for coop in (True, False):
+        for graph in (1, 0):
+            b = capi.Batch(probs, precision=prec, use_graph=graph)
+            b.set_coop(coop)
+            l0 = b.launches()
+            b.step(4)
+            launches[(coop, graph)] = b.launches() - l0
+            states[(coop, graph)] = [b.f(k) for k in range(len(probs))]
+            assert all(b.stats(k)["status"] == 0 for k in range(len(probs)))
+            b.close()
+    ref = states[(False, 1)]
+    for key, fs in states.items():
+        for k, (a, c) in enumerate(zip(ref, fs)):
+            assert np.array_equal(a, c), (key, k, rel(a, c))
+    assert launches[(True, 1)] < launches[(False, 1)] / 3, launches
+    assert launches[(True, 0)] < launches[(False, 0)] / 3, launches
+
+
 def test_layout_transforms_round_like_the_host(capi):
     """The host-buffer step's layout transforms convert double <-> double word with integer
     rounding on the device (dw_from_double_int / dw_to_double_int). A zero-step call round-trips
@@ -637,6 +663,26 @@ def test_unknown_preconditioner_is_refused(capi):
         capi.Solver(p, precision=capi.FP64, precond=7)
 
 
+def test_per_kernel_timing_of_the_cooperative_solve(capi):
+    """With the cooperative solve, per-kernel timing names it beside the assembly and the polish,
+    and the result is the same as stepping without timing."""
+    probs = [cases.synthetic_problem(40 + 9 * k, 30 + 7 * k, 1e-2, seed=60 + k, tau=0.2 + k) for k in range(4)]
+    a = capi.Batch(probs, precision=capi.FP32_REFINE_DW)
+    b = capi.Batch(probs, precision=capi.FP32_REFINE_DW)
+    a.enable_timing(True)
+    a.step(2)
+    kt = a.kernel_times()
+    a.enable_timing(False)
+    b.step(2)
+    for k in range(len(probs)):
+        assert np.array_equal(a.f(k), b.f(k))
+    a.close()
+    b.close()
+    for name in ("begin", "assemble", "solve_coop", "polish"):
+        assert name in kt and kt[name][1] == 2, (name, kt)
+    assert "bicg1" not in kt and "resid" not in kt, kt
+
+
 def test_per_kernel_timing_and_krylov_split(capi):
     """Per-kernel timing (host-loop steps bracketed by CUDA events) names every step kernel, and
     its split of the Krylov time -- whole BiCGSTAB iterations with fewer than / at least 10 % of
@@ -645,6 +691,7 @@ def test_per_kernel_timing_and_krylov_split(capi):
     probs = [cases.synthetic_problem(40 + 9 * k, 30 + 7 * k, 1e-2, seed=60 + k, tau=0.2 + k) for k in range(12)]
     a = capi.Batch(probs, precision=capi.FP32_REFINE_DW)
     b = capi.Batch(probs, precision=capi.FP32_REFINE_DW)
+    a.set_coop(False)  # a batch this small would run its loop as one cooperative kernel
     a.enable_timing(True)
     a.step(3)
     kt = a.kernel_times()
